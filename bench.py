@@ -1,0 +1,393 @@
+#!/usr/bin/env python
+"""DOF-steps/s of the scatter wave-propagation time loop on GB300.
+
+Workload (plain method at scale): box 60 x 40 x 30 m, structured hexa8 at 0.5 m
+(120 x 80 x 60 = 576,000 elements, 1,793,583 equations), two layers (top 5 m: E = 30 MPa,
+nu = 0.3, rho = 1800; below: E = 150 MPa, nu = 0.25, rho = 2000), Lysmer dashpots on the
+sides and base, Rayleigh 2 % at 1 and 50 Hz, moving point load 100 kN at 40 km/h along x on
+the surface, dt = 5e-5 s, FP64, velocities recorded at 50 surface receivers.  One bench step
+is one Newmark time step (graph launch: force, predictor, residual, device-side PCG loop,
+update).  Synthetic seeded inputs; no dataset.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl gb300|reference]
+
+Prints one JSON line.  --impl reference times the CPU restatement of the reference path
+(oracle/: numpy assembly + C Newmark/PCG loop on all host threads) on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DOF-steps/s batched vs single-solve on GB300 at ≤1e-5 rel err; adjoint/fwd cost"
+DT = 5e-5
+N_T = 10001  # 10,000 steps
+DIMS = (120, 80, 60, 0.5)
+MATERIALS = {"lower": {"density": 2000.0, "Young": 150e6, "poisson": 0.25},
+             "upper": {"density": 1800.0, "Young": 30e6, "poisson": 0.3}}
+LAYERS = [(0.0, "lower"), (35.0, "upper")]
+SETTINGS = {"int_order": 2, "damping": [1, 0.02, 50, 0.02], "absorbing_BC": [1, 1], "absorbing_BC_stiff": 1e3}
+LOAD = {"type": "moving_at_plane", "force": [0.0, -100e3, 0.0], "speed": 40 / 3.6, "direction": [1, 0],
+        "start_coord": [5.25, -15.25], "time": (N_T - 1) * DT}
+N_REC = 50
+
+
+def workload(dims=DIMS):
+    from scatter_gb300 import meshgen
+    from scatter_gb300.validator import ValidateLoad
+
+    nx, ny, nz, h = dims
+    model = meshgen.box_model(nx, ny, nz, h, layers=LAYERS, bottom="020", x_faces="200", z_faces="002")
+    load = dict(LOAD)
+    ValidateLoad.validate(load)
+    time_grid = np.linspace(0, load["time"], int(np.ceil(load["time"] / DT) + 1))
+    top_ids = model.top_nodes()
+    rng = np.random.default_rng(0)
+    rec_nodes = np.sort(rng.choice(top_ids, size=min(N_REC, len(top_ids)), replace=False))
+    rec_eq = model.eq_nb_dof[model.node_index()[rec_nodes], 1].astype(np.int64)
+    return model, load, time_grid, rec_eq
+
+
+def force_table(model, load, time_grid):
+    from scatter_gb300.force_external import Force
+
+    F = Force()
+    F.initialise_load(load, time_grid, model, None, top_surface_elements=model.get_top_surface())
+    return F.table
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """dram bytes per launch of the SpMV kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "k_spmv_box120x80x60.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("dram_bytes_per_launch_full_size:"):
+            return float(line.split(":")[1])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline_run(n, rowptr, cols, M, C, K, table, rec_eq, target_s=20.0, max_steps=None):
+    """Oracle C Newmark/PCG on the host cores, bounded to ~target_s of work."""
+    from oracle import cpu
+
+    s = cpu.NewmarkCPU.from_csr(n, rowptr, cols, M, C, K, DT)
+    t0 = time.perf_counter()
+    s.run(0, 1, table.f_ptr, table.f_eq, table.f_val, rec_eq)
+    t1 = time.perf_counter() - t0
+    steps = int(max(2, min(200, target_s / max(t1, 1e-6))))
+    if max_steps:
+        steps = min(steps, max_steps)
+    t0 = time.perf_counter()
+    s.run(1, steps, table.f_ptr, table.f_eq, table.f_val, rec_eq)
+    el = time.perf_counter() - t0
+    return {"value": n * steps / el, "unit": "DOF-steps/s", "cores": cpu.threads(), "kind": "port",
+            "sample": f"{steps} Newmark steps (steps 1..{steps}) of the same workload from rest, Jacobi-PCG "
+                      f"per step to rtol 1e-12, {cpu.threads()} OpenMP threads, {el:.1f} s"}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_gb300(args):
+    import torch
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from scatter_gb300 import _native
+    from scatter_gb300.solvers import NewmarkGPU
+    from scatter_gb300.system_matrix import GenerateMatrix
+
+    _native.load()
+    t_setup = time.perf_counter()
+    model, load, time_grid, rec_eq = workload()
+    table = force_table(model, load, time_grid)
+    t_host = time.perf_counter() - t_setup
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g = GenerateMatrix(model.number_eq, SETTINGS["int_order"])
+    g.generate_stiffness_and_mass(model, MATERIALS)
+    g.absorbing_boundaries(model, MATERIALS, SETTINGS["absorbing_BC"], SETTINGS["absorbing_BC_stiff"])
+    g.damping_Rayleigh(SETTINGS["damping"])
+    torch.cuda.synchronize()
+    t_assembly = time.perf_counter() - t0
+    n = model.number_eq
+    K_steps, W = args.steps, args.warmup
+    if W + K_steps + 1 > len(time_grid):
+        raise SystemExit("steps + warmup exceed the 10,000-step load history")
+    solver = NewmarkGPU(g.pattern, g.M_d, g.C_d, g.K_d, DT)
+    solver.set_force(table)
+    solver.set_output(1, rec_eq, len(time_grid), what=("v",))
+    solver.initial_acceleration()
+    solver.run(0, W)
+    rc, it_w, _ = solver.status()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record()
+        solver.run(W, W + K_steps)
+        e1.record()
+        torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ms = e0.elapsed_time(e1)
+    rc, it_all, it_max = solver.status()
+    if rc != 0:
+        raise SystemExit(f"solver status {rc} during the timed region")
+    iters = it_all - it_w
+    if ws > 1:
+        tt = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = ws * n * K_steps / (ms / 1e3)
+
+    # dominant kernel: the PCG SpMV, timed standalone on the solver's stream
+    import ctypes
+
+    mspl = ctypes.c_float()
+    bpl = ctypes.c_int64()
+    _native.call("sc_newmark_time_spmv", solver.h, 20, ctypes.byref(mspl), ctypes.byref(bpl))
+    peak, peak_kind = peaks()
+    achieved = bpl.value / (mspl.value * 1e-3) / 1e9
+    traffic = profile_traffic()
+
+    # end to end through the solver API: each step copies its force entries host->device from
+    # pinned memory and reads the step's receiver velocities back to pinned host memory
+    e2e = e2e_run(solver, table, rec_eq, W + K_steps, min(K_steps, len(time_grid) - 1 - (W + K_steps)), n)
+
+    out = {"metric": METRIC, "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": K_steps, "warmup": W,
+           "ms_per_step": ms / K_steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic (seeded structured mesh, moving point load)",
+           "config": {"workload": "plain Newmark FP64, box 60x40x30 m hexa8 0.5 m (120x80x60 el), 2 layers, "
+                                  "Lysmer sides+base, moving 100 kN at 40 km/h, dt 5e-5",
+                      "n_eq": n, "nnz": g.pattern.nnz, "elements": int(len(model.elem)), "receivers": len(rec_eq),
+                      "parallelism": f"replicas x{ws}",
+                      "l2": "inputs larger than L2 (CSR values+cols 5.1 GB), no flush",
+                      "solver": "Newmark beta=1/4 gamma=1/2, Jacobi-PCG rtol 1e-12 per step"},
+           "cg_iters_per_step": iters / K_steps, "cg_iters_max": it_max,
+           "setup_s": {"host_mesh_and_loads": round(t_host, 2), "gpu_assembly_lysmer_rayleigh": round(t_assembly, 3)},
+           "gpu_launches": 7 * K_steps + 3 * iters + 1,
+           "roofline": {"bound": "hbm", "kernel": "k_spmv (CSR FP64, w = A p)", "achieved": achieved,
+                        "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                        "traffic": traffic, "bytes_per_launch": bpl.value, "ms_per_launch": mspl.value},
+           "clocks": clk.summary(), "e2e": e2e}
+    # CPU baseline (rank 0 only, N = 1): the oracle's C loop on the host cores
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        rp = g.pattern.rowptr.cpu().numpy()
+        cl = g.pattern.cols.cpu().numpy()
+        Mh, Ch, Kh = (x.cpu().numpy() for x in (g.M_d, g.C_d, g.K_d))
+        out["cpu_baseline"] = cpu_baseline_run(n, rp, cl, Mh, Ch, Kh, table, rec_eq, target_s=args.cpu_seconds)
+    solver.close()
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def e2e_run(solver, table, rec_eq, t0, k, n):
+    import torch
+
+    if k <= 0:
+        return None
+    p, e, v = solver._keep_force
+    host_eq = torch.from_numpy(table.f_eq).pin_memory()
+    host_val = torch.from_numpy(table.f_val).pin_memory()
+    out_v = solver.out["v"].view(solver.n_out, solver.n_rec)
+    host_out = torch.empty((k, solver.n_rec), dtype=torch.float64).pin_memory()
+    ptr = table.f_ptr
+    h2d = 0
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    wall0 = time.perf_counter()
+    ev0.record()
+    for s in range(k):
+        t = t0 + s
+        a, b = int(ptr[t + 1]), int(ptr[t + 2]) if t + 2 < len(ptr) else int(ptr[t + 1])
+        if b > a:
+            e[a:b].copy_(host_eq[a:b], non_blocking=True)
+            v[a:b].copy_(host_val[a:b], non_blocking=True)
+            h2d += (b - a) * 12
+        solver.run(t, t + 1)
+        host_out[s].copy_(out_v[t + 1], non_blocking=True)
+    ev1.record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    ms = ev0.elapsed_time(ev1)
+    return {"value": n * k / (ms / 1e3), "unit": "DOF-steps/s", "h2d_bytes_per_step": h2d / k,
+            "d2h_bytes_per_step": solver.n_rec * 8, "steps": k, "host_wall_s": wall,
+            "api": "NewmarkGPU.run per step + pinned H2D force entries + pinned D2H receiver velocities"}
+
+
+def run_reference(args):
+    """CPU restatement of the reference path on the host cores (oracle: numpy element
+    integration + element-order assembly + Lysmer + Rayleigh, C Newmark/PCG loop)."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import scipy.sparse as sp
+
+    from oracle import assembly as asm
+    from oracle import elements as el
+    from oracle import lysmer
+
+    t0 = time.perf_counter()
+    model, load, time_grid, rec_eq = workload()
+    table = force_table(model, load, time_grid)
+    n = model.number_eq
+    idx = model.node_index()[model.elem]
+    X = model.nodes[:, 1:][idx]
+    names = {int(r[1]): r[2] for r in model.materials}
+    mi = model.materials_index
+    E = np.array([MATERIALS[names[int(i)]]["Young"] for i in mi])
+    nu = np.array([MATERIALS[names[int(i)]]["poisson"] for i in mi])
+    rho = np.array([MATERIALS[names[int(i)]]["density"] for i in mi])
+    rows, cols, kv, mv = [], [], [], []
+    eq = model.eq_nb_elem
+    for s in range(0, len(X), 20000):
+        Ke, Me = el.element_matrices("hexa8", X[s:s + 20000], E[s:s + 20000], nu[s:s + 20000], rho[s:s + 20000])
+        e = eq[s:s + 20000]
+        ok = ~np.isnan(e)
+        ei = np.where(ok, e, -1).astype(np.int64)
+        R = np.broadcast_to(ei[:, :, None], Ke.shape)
+        Cc = np.broadcast_to(ei[:, None, :], Ke.shape)
+        m = (R >= 0) & (Cc >= 0)
+        rows.append(R[m])
+        cols.append(Cc[m])
+        kv.append(Ke[m])
+        mv.append(Me[m])
+    rows, cols = np.concatenate(rows), np.concatenate(cols)
+    K0 = sp.coo_matrix((np.concatenate(kv), (rows, cols)), shape=(n, n)).tocsr()
+    M = sp.coo_matrix((np.concatenate(mv), (rows, cols)), shape=(n, n)).tocsr()
+    mdl = {"nodes": model.nodes, "elem": model.elem, "BC": model.BC, "BC_dir": model.BC_dir,
+           "eq_nb_dof": model.eq_nb_dof, "element_type": "hexa8", "number_eq": n}
+    Ca, Ka = lysmer.absorbing(mdl, (E, nu, rho), SETTINGS["absorbing_BC"], SETTINGS["absorbing_BC_stiff"])
+    K = asm.drop_zeros(K0 + Ka)
+    C = asm.rayleigh(M, K, Ca, SETTINGS["damping"])
+    setup = time.perf_counter() - t0
+    from oracle import cpu
+
+    s = cpu.NewmarkCPU(M, C, K, DT)
+    budget = args.cpu_seconds
+    t1 = time.perf_counter()
+    s.run(0, 1, table.f_ptr, table.f_eq, table.f_val, rec_eq)
+    one = time.perf_counter() - t1
+    steps = int(max(2, min(args.steps, budget / max(one, 1e-6))))
+    t1 = time.perf_counter()
+    s.run(1, steps, table.f_ptr, table.f_eq, table.f_val, rec_eq)
+    el_s = time.perf_counter() - t1
+    value = n * steps / el_s
+    cb = {"value": value, "unit": "DOF-steps/s", "cores": cpu.threads(), "kind": "port",
+          "sample": f"{steps} Newmark steps (1..{steps}) of the same workload from rest; oracle numpy assembly "
+                    f"({setup:.0f} s, untimed) + C Jacobi-PCG loop on {cpu.threads()} threads, {el_s:.1f} s"}
+    print(json.dumps({"metric": METRIC, "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": steps,
+                      "warmup": 1, "ms_per_step": el_s / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded structured mesh)",
+                      "config": {"workload": "plain Newmark FP64, box 60x40x30 m hexa8 0.5 m (120x80x60 el), "
+                                             "2 layers, Lysmer sides+base, moving 100 kN at 40 km/h, dt 5e-5",
+                                 "n_eq": n}, "impl": "reference", "cpu_baseline": cb,
+                      "e2e": {"value": value, "unit": "DOF-steps/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,168 @@
+/*
+ * scatter_gb300 -- C ABI of the GB300 (sm_103a) finite-element wave-propagation path.
+ *
+ * The reference (PlatypusBytes/scatter) is pure Python; its hot path is the element
+ * integration + assembly in scatter/system_matrix.py, the Lysmer boundaries and Rayleigh
+ * damping in the same file, and the Newmark time loop that scatter/scatter.py:120-159
+ * drives through PuggleSolvers.  Each entry point below replaces one of those pieces; the
+ * reference-side binding (ctypes) is shown in INTEGRATION.md.
+ *
+ * Conventions
+ *   - every pointer is a DEVICE pointer unless its name ends in _host;
+ *   - every function works on `stream` (a cudaStream_t passed as void*) and returns a status
+ *     code (SC_*).  The time-loop calls (sc_newmark_run) allocate nothing; the one-off setup
+ *     calls that need small temporaries or a flag read-back (incidence, adjacency, values,
+ *     Lysmer grouping) take them from the stream-ordered allocator and synchronise `stream`;
+ *   - doubles are IEEE binary64; integer index arrays are int32 unless typed int64_t;
+ *   - equation numbers follow the reference (scatter/mesher.py:276-310): node-major,
+ *     DOF-minor over the node list, fixed DOFs excluded (encoded here as -1).
+ */
+#ifndef SCATTER_GB300_H
+#define SCATTER_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (the Python layer raises RuntimeError(code, text)) */
+#define SC_OK 0
+#define SC_BAD_ARG 1
+#define SC_NOT_CONVERGED 2
+#define SC_BREAKDOWN 3
+#define SC_CAPACITY 4
+#define SC_CUDA_ERROR 5
+
+/* element type codes: element_types.py classes HexEight, HexTwenty, TetraFour, TetraTen,
+ * QuadFour, QuadEight, TriThree, TriSix (gmsh node order) */
+#define SC_HEXA8 0
+#define SC_HEXA20 1
+#define SC_TETRA4 2
+#define SC_TETRA10 3
+#define SC_QUAD4 4
+#define SC_QUAD8 5
+#define SC_TRI3 6
+#define SC_TRI6 7
+
+int sc_version(void);
+const char* sc_status_string(int status);
+/* last CUDA error text recorded by a failing call on this host thread */
+const char* sc_last_error(void);
+
+/* ------------------------------------------------------------------ element integration
+ * Replaces VolumeElement/SurfaceElement.generate + compute_stiffness + compute_mass
+ * (scatter/discretisation.py:83-222 and :241-418) with the isotropic D of
+ * scatter/material_models.py:5-43, as called per element in
+ * GenerateMatrix.generate_stiffness_and_mass (scatter/system_matrix.py:55-85).
+ *   coords  [n_elem][n_en][dim]   element node coordinates (3D: x,y,z; 2D: x,y)
+ *   young, poisson, density [n_elem]
+ *   Ke, Me  [n_elem][n_en*dim][n_en*dim]  (row-major; either may be NULL)
+ *   order   Gauss order per axis (discretisation.py:436-497): quad 1..3, tri 1..3, tetra 1..2 */
+int sc_element_matrices(int etype, int order, int n_elem, const double* coords, const double* young,
+                        const double* poisson, const double* density, double* Ke, double* Me, void* stream);
+
+/* Lysmer face mass F[a][b] = sum_g Na Nb detJ w on 2D faces (quad4, quad8, tri3, tri6), the
+ * matrix of SurfaceElement.compute_abs_bound (scatter/discretisation.py:420-433) without its
+ * 2-DOF expansion.  xy [n_face][nf][2] in-plane coordinates in the caller's node order. */
+int sc_face_matrices(int ftype, int order, int n_face, const double* xy, double* Fm, void* stream);
+
+/* ------------------------------------------------------------------ assembly
+ * Replaces the dict accumulation + COO->lil of GenerateMatrix.generate_stiffness_and_mass
+ * (scatter/system_matrix.py:87-121).  The sparsity pattern is the element graph over free
+ * DOFs with rows and columns sorted (the reference's M pattern); values are summed per
+ * entry in element order, as the reference's defaultdict does.  Deterministic, no atomics
+ * on values.
+ *
+ * Step 1: node -> element incidence (grouped, element ids ascending per node).
+ *   elem [n_elem][n_en] 0-based node indices.  inc_ptr [n_nodes+1], inc [n_elem*n_en],
+ *   work [n_nodes] int32 scratch. */
+int sc_node_incidence(int n_elem, int n_en, int n_nodes, const int* elem, int* inc_ptr, int* inc, int* work,
+                      void* stream);
+
+/* Step 2: node adjacency (sorted unique neighbour nodes, self included).
+ *   pass 0 (adj == NULL): writes deg[n_nodes]; pass 1: fills adj using adj_ptr [n_nodes+1]
+ *   (exclusive prefix of deg, e.g. from sc_exclusive_scan_i64).  Capacity: at most 2048
+ *   candidate (element, node) pairs per node, else SC_CAPACITY. */
+int sc_node_adjacency(int n_nodes, int n_en, const int* elem, const int* inc_ptr, const int* inc,
+                      const int64_t* adj_ptr, int* deg, int* adj, void* stream);
+
+/* exclusive prefix sum of n int64 values (out[n] = total); in == out allowed.
+ * work: int64 scratch of at least sc_scan_work_size(n) elements. */
+int64_t sc_scan_work_size(int64_t n);
+int sc_exclusive_scan_i64(int64_t n, const int64_t* in, int64_t* out, int64_t* work, void* stream);
+
+/* Step 3: CSR rows over free DOFs.  eqmap [n_nodes][dim] (-1 = fixed).
+ *   rowlen [n_eq] (pass: cols == NULL) then cols [nnz] using rowptr [n_eq+1]. */
+int sc_csr_pattern(int n_nodes, int dim, const int* eqmap, const int64_t* adj_ptr, const int* adj,
+                   const int64_t* rowptr, int64_t* rowlen, int* cols, void* stream);
+
+/* Step 4: values.  Ke/Me as from sc_element_matrices; K, M [nnz] are overwritten. */
+int sc_assemble_values(int n_nodes, int n_en, int dim, const int* elem, const int* eqmap, const int* inc_ptr,
+                       const int* inc, const int64_t* adj_ptr, const int* adj, const int64_t* rowptr,
+                       const int* cols, const double* Ke, const double* Me, double* K, double* M, void* stream);
+
+/* ------------------------------------------------------------------ Lysmer + Rayleigh
+ * Replaces the scatter of GenerateMatrix.absorbing_boundaries (scatter/system_matrix.py:355-376).
+ * For face f with sorted equation numbers eqs[f][a] (a < nf), face matrix Fm[f][a][b] and
+ * per-column factors fct[f][b] (dashpot rho*v) and fct2[f][b] (spring Ec or G):
+ *   C_abs[eqs[a], eqs[b]] += Fm[a][b] * fct[b];  K_abs[..] += |Fm[a][b]| * fct2[b]
+ * accumulated per entry in face order.  Contributions are grouped by row with
+ * sc_group_rows (row_ptr [n_eq+1], order [n_face*nf*nf]); work [n_eq] int32 scratch. */
+int sc_group_rows(int n_face, int nf, const int* eqs, int n_eq, int* row_ptr, int* order, int* work, void* stream);
+int sc_lysmer_values(int n_face, int nf, const int* eqs, const double* Fm, const double* fct, const double* fct2,
+                     int n_eq, const int* row_ptr, const int* order, const int64_t* rowptr, const int* cols,
+                     double* C_abs, double* K_abs, void* stream);
+
+/* out[i] = c0*x[i] + (c1*y[i] + c2*z[i]) for i < n (x, y or z may be NULL = 0).
+ * Rayleigh: C = C_abs + (alpha M + beta K) (scatter/system_matrix.py:189-198);
+ * Lysmer spring: K = K0 + K_abs / k_div (system_matrix.py:376). */
+int sc_combine(int64_t n, double c0, const double* x, double c1, const double* y, double c2, const double* z,
+               double* out, void* stream);
+
+/* ------------------------------------------------------------------ Newmark time loop
+ * Replaces the PuggleSolvers NewmarkExplicit loop the reference drives from
+ * scatter/scatter.py:133-159 (average acceleration, beta = 1/4, gamma = 1/2, consistent
+ * mass, constant effective matrix).  Each step solves, for the new acceleration x,
+ *     A x = f(t) - C vp - K up,   A = M + dt/2 C + dt^2/4 K,
+ *     vp = v + dt/2 a,  up = u + dt v + dt^2/4 a,
+ * then u = up + dt^2/4 x, v = vp + dt/2 x, a = x -- the same update as the reference's
+ * K^ u = rhs form.  The solve is Jacobi-preconditioned CG on A, warm-started from the
+ * previous acceleration, to ||r|| <= rtol ||rhs|| (FP64 dot products, deterministic
+ * reductions).  One step is one CUDA graph launch with a device-side conditional loop.
+ *
+ * The caller owns every buffer.  sc_newmark_workspace_doubles() gives the scratch size.
+ * Force table (CSR over time): f_ptr [n_t+1], f_eq [f_ptr[n_t]], f_val [..]: the force at
+ * step t is sum over k in [f_ptr[t], f_ptr[t+1]) of f_val[k] e_{f_eq[k]}
+ * (Force.update_load_at_t, scatter/force_external.py:55-74).
+ * Output: every out_interval steps (step 0 included) the solver writes u, v, a at the
+ * n_rec equations rec_eq into out_u/out_v/out_a [n_out][n_rec] (any may be NULL).
+ */
+typedef struct sc_newmark sc_newmark;
+
+int64_t sc_newmark_workspace_doubles(int64_t n_eq, int64_t n_blocks_hint);
+int sc_newmark_create(sc_newmark** h, int64_t n_eq, const int64_t* rowptr, const int* cols, const double* M,
+                      const double* C, const double* K, double* A, double dt, double rtol, int max_iter,
+                      double* u, double* v, double* a, double* workspace, int64_t workspace_doubles, void* stream);
+int sc_newmark_set_force(sc_newmark* h, int n_t, const int64_t* f_ptr, const int* f_eq, const double* f_val);
+int sc_newmark_set_output(sc_newmark* h, int out_interval, int n_rec, const int* rec_eq, double* out_u,
+                          double* out_v, double* out_a, int64_t n_out);
+/* a0 = M^-1 (f(0) - C v - K u) by CG on M (scatter/scatter.py:158 numerical.update(0)) and
+ * writes the step-0 output row.  Synchronous. */
+int sc_newmark_initial_acceleration(sc_newmark* h);
+/* run steps t = t_begin .. t_end-1 -> states t+1; asynchronous (graph launches) */
+int sc_newmark_run(sc_newmark* h, int t_begin, int t_end);
+/* synchronous: CG status of the run so far (SC_OK / SC_NOT_CONVERGED / SC_BREAKDOWN),
+ * total and maximum CG iterations per step */
+int sc_newmark_status(sc_newmark* h, int64_t* total_iters, int* max_iters_per_step);
+/* Timing aid: launches the step loop's SpMV kernel (w = A p, with its p.w partials) `reps`
+ * times on the solver's stream between CUDA events, outside any graph; returns the mean
+ * device time per launch and the algorithmic bytes of one launch (12 B per stored entry +
+ * row pointers + one read of p + the write of w).  Touches only scratch vectors. */
+int sc_newmark_time_spmv(sc_newmark* h, int reps, float* ms_per_launch, int64_t* bytes_per_launch);
+int sc_newmark_destroy(sc_newmark* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

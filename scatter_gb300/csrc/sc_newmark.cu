@@ -1,0 +1,634 @@
+// Newmark (beta = 1/4, gamma = 1/2) time loop with a device-side PCG per step.
+//
+// Replaces the PuggleSolvers NewmarkExplicit loop driven by scatter/scatter.py:133-159.
+// Per step t -> t+1 (acceleration form of the same update):
+//   vp = v + dt/2 a,  up = u + dt v + dt^2/4 a
+//   A x = f(t+1) - C vp - K up,          A = M + dt/2 C + dt^2/4 K
+//   u = up + dt^2/4 x,  v = vp + dt/2 x,  a = x
+// x is found by Jacobi-PCG warm-started from a, stopped at ||r|| <= rtol ||rhs||.
+//
+// Execution: one CUDA graph per step: [force, predict, residual] -> WHILE{spmv, update,
+// direction} -> [finalize].  The WHILE node is a graph conditional whose value the residual
+// and update kernels set on the device (converged / iteration cap / breakdown), so a step
+// costs exactly the iterations it needs with no host round trip.  Reductions are per-block
+// partials summed by the last block to finish (ticket counter, no spin-waits), in a fixed
+// order, so every run is bitwise reproducible.  Matrices are CSR over the reference's
+// equation numbering with a shared element-graph pattern.
+#include <vector>
+
+#include "sc_common.cuh"
+
+namespace sc {
+
+constexpr int kRowThreads = 256;  // 8 warps, one row per warp
+
+struct NmScalars {
+  double rz, pw, rr, bb, alpha, beta, tol2, pad0;
+  long long total_iters;
+  int it, max_it, max_seen, status, t, pad1;
+  unsigned int ticket;
+  unsigned int pad2[3];
+};
+
+struct NmArgs {
+  int64_t n;
+  const int64_t* rowptr;
+  const int* cols;
+  const double *M, *C, *K, *A;
+  double *u, *v, *a;
+  double *vp, *up, *x, *r, *z, *p, *w, *dinv, *f;
+  double* part;  // [nblocks][4]
+  NmScalars* s;
+  double dt;
+  // force table
+  int n_t;
+  const int64_t* f_ptr;
+  const int* f_eq;
+  const double* f_val;
+  // output
+  int out_interval, n_rec;
+  const int* rec_eq;
+  double *out_u, *out_v, *out_a;
+  int64_t n_out;
+};
+
+// returns true in every thread of the last block to arrive
+__device__ inline bool last_block(unsigned int* ticket) {
+  __shared__ bool am_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) am_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  return am_last;
+}
+
+// sum column k of part[nb][4] in the last block, fixed order; result in thread 0
+__device__ inline double reduce_parts(const double* part, int k, double* sh) {
+  double s = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(part + b * 4 + k);
+  return block_sum(s, sh);
+}
+
+__global__ void k_force(NmArgs g) {
+  // clear the entries of step t, write those of step t+1 (dense f)
+  const int t = g.s->t;
+  if (g.f_ptr == nullptr) return;
+  if (t >= 0 && t < g.n_t)
+    for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f[g.f_eq[k]] = 0.0;
+  __syncthreads();
+  const int t1 = t + 1;
+  if (t1 >= 0 && t1 < g.n_t)
+    for (int64_t k = g.f_ptr[t1] + threadIdx.x; k < g.f_ptr[t1 + 1]; k += blockDim.x) g.f[g.f_eq[k]] += g.f_val[k];
+}
+
+__global__ void k_predict(NmArgs g) {
+  const double dt = g.dt, h = 0.5 * dt, q = 0.25 * dt * dt;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double ai = g.a[i], vi = g.v[i];
+    g.vp[i] = vi + h * ai;
+    g.up[i] = g.u[i] + dt * vi + q * ai;
+  }
+}
+
+// rhs = f - C vp - K up ; r = rhs - Op x0 ; z = dinv r ; p = z.  mode 0: x0 = a (step),
+// mode 1: x0 = 0 (initial acceleration, Op = M, vp/up point at v/u).
+__global__ void __launch_bounds__(kRowThreads) k_residual(NmArgs g, const double* __restrict__ Op, int mode,
+                                                          cudaGraphConditionalHandle hc) {
+  __shared__ double sh[32];
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const double* __restrict__ vp = mode == 0 ? g.vp : g.v;
+  const double* __restrict__ up = mode == 0 ? g.up : g.u;
+  double prz = 0, prr = 0, pbb = 0;
+  for (int64_t row = gw; row < g.n; row += nw) {
+    const int64_t k0 = g.rowptr[row], k1 = g.rowptr[row + 1];
+    double sr = 0.0, sa = 0.0;
+    for (int64_t k = k0 + lane; k < k1; k += 32) {
+      const int c = g.cols[k];
+      sr = fma(g.C[k], vp[c], sr);
+      sr = fma(g.K[k], up[c], sr);
+      if (mode == 0) sa = fma(Op[k], g.a[c], sa);
+    }
+    sr = warp_sum(sr);
+    sa = warp_sum(sa);
+    if (lane == 0) {
+      const double rhs = g.f[row] - sr;
+      const double r = rhs - sa;
+      const double z = g.dinv[row] * r;
+      g.x[row] = mode == 0 ? g.a[row] : 0.0;
+      g.r[row] = r;
+      g.z[row] = z;
+      g.p[row] = z;
+      prz += r * z;
+      prr += r * r;
+      pbb += rhs * rhs;
+    }
+  }
+  double t = block_sum(prz, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 0] = t;
+  t = block_sum(prr, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 1] = t;
+  t = block_sum(pbb, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 2] = t;
+  if (last_block(&g.s->ticket)) {
+    const double rz = reduce_parts(g.part, 0, sh);
+    const double rr = reduce_parts(g.part, 1, sh);
+    const double bb = reduce_parts(g.part, 2, sh);
+    if (threadIdx.x == 0) {
+      NmScalars* s = g.s;
+      s->rz = rz;
+      s->rr = rr;
+      s->bb = bb;
+      s->it = 0;
+      s->ticket = 0;
+      const bool done = rr <= s->tol2 * bb;
+      cudaGraphSetConditional(hc, done ? 0u : 1u);
+    }
+  }
+}
+
+// w = Op p ; partial p.w ; last block: alpha = rz / pw.  kInGraph = false is the same
+// kernel for standalone timing (it does not touch the graph conditional).
+template <bool kInGraph>
+__global__ void __launch_bounds__(kRowThreads) k_spmv(NmArgs g, const double* __restrict__ Op,
+                                                      cudaGraphConditionalHandle hc) {
+  __shared__ double sh[32];
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double ppw = 0.0;
+  for (int64_t row = gw; row < g.n; row += nw) {
+    const int64_t k0 = g.rowptr[row], k1 = g.rowptr[row + 1];
+    double s = 0.0;
+    for (int64_t k = k0 + lane; k < k1; k += 32) s = fma(__ldcs(Op + k), g.p[__ldcs(g.cols + k)], s);
+    s = warp_sum(s);
+    if (lane == 0) {
+      g.w[row] = s;
+      ppw += g.p[row] * s;
+    }
+  }
+  const double t = block_sum(ppw, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 3] = t;
+  if (last_block(&g.s->ticket)) {
+    const double pw = reduce_parts(g.part, 3, sh);
+    if (threadIdx.x == 0) {
+      NmScalars* s = g.s;
+      s->ticket = 0;
+      s->pw = pw;
+      if (!kInGraph) {
+        // standalone timing launch: leave the solver's scalars untouched
+      } else if (!(pw > 0.0)) {  // not SPD along p (or NaN): stop this solve, keep x
+        s->alpha = 0.0;
+        s->status = SC_BREAKDOWN;
+        cudaGraphSetConditional(hc, 0u);
+      } else {
+        s->alpha = s->rz / pw;
+      }
+    }
+  }
+}
+
+// x += alpha p ; r -= alpha w ; z = dinv r ; partial r.z, r.r ; last block: beta, test
+__global__ void k_update(NmArgs g, cudaGraphConditionalHandle hc) {
+  __shared__ double sh[32];
+  const double alpha = g.s->alpha;
+  double prz = 0.0, prr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double pi = g.p[i];
+    g.x[i] = fma(alpha, pi, g.x[i]);
+    const double r = fma(-alpha, g.w[i], g.r[i]);
+    g.r[i] = r;
+    const double z = g.dinv[i] * r;
+    g.z[i] = z;
+    prz += r * z;
+    prr += r * r;
+  }
+  double t = block_sum(prz, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 0] = t;
+  t = block_sum(prr, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 1] = t;
+  if (last_block(&g.s->ticket)) {
+    const double rz = reduce_parts(g.part, 0, sh);
+    const double rr = reduce_parts(g.part, 1, sh);
+    if (threadIdx.x == 0) {
+      NmScalars* s = g.s;
+      s->ticket = 0;
+      s->beta = s->rz != 0.0 ? rz / s->rz : 0.0;
+      s->rz = rz;
+      s->rr = rr;
+      s->it += 1;
+      bool done = rr <= s->tol2 * s->bb;
+      if (!done && s->it >= s->max_it) {
+        s->status = s->status ? s->status : SC_NOT_CONVERGED;
+        done = true;
+      }
+      if (s->status == SC_BREAKDOWN) done = true;
+      if (done) cudaGraphSetConditional(hc, 0u);
+    }
+  }
+}
+
+__global__ void k_direction(NmArgs g) {
+  const double beta = g.s->beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x)
+    g.p[i] = fma(beta, g.p[i], g.z[i]);
+}
+
+__device__ inline void record(const NmArgs& g, int step) {
+  if (g.n_rec <= 0 || g.out_interval <= 0 || step % g.out_interval) return;
+  const int64_t row = step / g.out_interval;
+  if (row >= g.n_out) return;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.n_rec; j += (int64_t)gridDim.x * blockDim.x) {
+    const int e = g.rec_eq[j];
+    if (g.out_u) g.out_u[row * g.n_rec + j] = g.u[e];
+    if (g.out_v) g.out_v[row * g.n_rec + j] = g.v[e];
+    if (g.out_a) g.out_a[row * g.n_rec + j] = g.a[e];
+  }
+}
+
+// u = up + dt^2/4 x ; v = vp + dt/2 x ; a = x ; t += 1
+__global__ void k_finalize(NmArgs g) {
+  const double h = 0.5 * g.dt, q = 0.25 * g.dt * g.dt;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = g.x[i];
+    g.u[i] = fma(q, x, g.up[i]);
+    g.v[i] = fma(h, x, g.vp[i]);
+    g.a[i] = x;
+  }
+}
+
+__global__ void k_record(NmArgs g, int bump) {
+  // runs after k_finalize: step index t+1 is the state just computed
+  const int step = g.s->t + bump;
+  record(g, step);
+  __syncthreads();
+  if (bump && blockIdx.x == 0 && threadIdx.x == 0) {
+    NmScalars* s = g.s;
+    s->total_iters += s->it;
+    if (s->it > s->max_seen) s->max_seen = s->it;
+  }
+}
+
+__global__ void k_advance(NmScalars* s) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) s->t += 1;
+}
+
+// initial acceleration: a = x after CG on M
+__global__ void k_copy_x_to_a(NmArgs g) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x)
+    g.a[i] = g.x[i];
+}
+
+__global__ void k_dinv(int64_t n, const int64_t* __restrict__ rowptr, const int* __restrict__ cols,
+                       const double* __restrict__ Op, double* __restrict__ dinv, int* __restrict__ bad) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double d = 0.0;
+    for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+      if (cols[k] == i) d = Op[k];
+    if (!(d > 0.0)) {
+      atomicExch(bad, 1);
+      d = 1.0;
+    }
+    dinv[i] = 1.0 / d;
+  }
+}
+
+__global__ void k_init_scalars(NmScalars* s, double tol2, int max_it) {
+  s->rz = s->pw = s->rr = s->bb = s->alpha = s->beta = 0.0;
+  s->tol2 = tol2;
+  s->total_iters = 0;
+  s->it = 0;
+  s->max_it = max_it;
+  s->max_seen = 0;
+  s->status = SC_OK;
+  s->t = 0;
+  s->ticket = 0;
+}
+
+__global__ void k_set_t(NmScalars* s, int t) { s->t = t; }
+
+}  // namespace sc
+
+using namespace sc;
+
+struct sc_newmark {
+  NmArgs g;
+  cudaStream_t user = nullptr, cap = nullptr, cap2 = nullptr;
+  unsigned row_blocks = 1, vec_blocks = 1;
+  cudaGraphExec_t step_exec = nullptr, init_exec = nullptr;
+  cudaGraph_t step_graph = nullptr, init_graph = nullptr;
+  double rtol = 1e-12;
+};
+
+namespace {
+
+// Build [pre] -> WHILE{spmv, update, direction} -> [post] for operator Op.
+int build_pcg_graph(sc_newmark* h, const double* Op, int mode, cudaGraph_t* graph_out, cudaGraphExec_t* exec_out) {
+  cudaGraph_t graph = nullptr;
+  int rc = check(cudaGraphCreate(&graph, 0), "cudaGraphCreate");
+  if (rc) return rc;
+  cudaGraphConditionalHandle hc;
+  if ((rc = check(cudaGraphConditionalHandleCreate(&hc, graph, 1, cudaGraphCondAssignDefault), "handle"))) {
+    cudaGraphDestroy(graph);
+    return rc;
+  }
+  NmArgs g = h->g;
+  cudaStream_t cs = h->cap;
+  do {
+    if ((rc = check(cudaStreamBeginCaptureToGraph(cs, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+                    "capture pre")))
+      break;
+    if (mode == 0) {
+      k_force<<<1, 256, 0, cs>>>(g);
+      k_predict<<<h->vec_blocks, 256, 0, cs>>>(g);
+    }
+    k_residual<<<h->row_blocks, kRowThreads, 0, cs>>>(g, Op, mode, hc);
+    cudaStreamCaptureStatus stt;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    if ((rc = check(cudaStreamGetCaptureInfo(cs, &stt, nullptr, nullptr, &deps, nullptr, &ndeps), "capture info")))
+      break;
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = hc;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    if ((rc = check(cudaGraphAddNode(&cnode, graph, deps, nullptr, ndeps, &cp), "add conditional"))) break;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if ((rc = check(cudaStreamUpdateCaptureDependencies(cs, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies),
+                    "update deps")))
+      break;
+    // body, captured on a second stream
+    if ((rc = check(cudaStreamBeginCaptureToGraph(h->cap2, body, nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal),
+                    "capture body")))
+      break;
+    k_spmv<true><<<h->row_blocks, kRowThreads, 0, h->cap2>>>(g, Op, hc);
+    k_update<<<h->vec_blocks, 256, 0, h->cap2>>>(g, hc);
+    k_direction<<<h->vec_blocks, 256, 0, h->cap2>>>(g);
+    cudaGraph_t body_out = nullptr;
+    if ((rc = check(cudaStreamEndCapture(h->cap2, &body_out), "end body"))) break;
+    // post
+    if (mode == 0) {
+      k_finalize<<<h->vec_blocks, 256, 0, cs>>>(g);
+      k_record<<<h->vec_blocks, 256, 0, cs>>>(g, 1);
+      k_advance<<<1, 32, 0, cs>>>(g.s);
+    } else {
+      k_copy_x_to_a<<<h->vec_blocks, 256, 0, cs>>>(g);
+      k_record<<<h->vec_blocks, 256, 0, cs>>>(g, 0);
+    }
+    cudaGraph_t out = nullptr;
+    if ((rc = check(cudaStreamEndCapture(cs, &out), "end capture"))) break;
+    if ((rc = check(cudaGraphInstantiate(exec_out, graph, 0), "instantiate"))) break;
+  } while (0);
+  if (rc) {
+    cudaStreamCaptureStatus st;
+    if (cudaStreamIsCapturing(cs, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
+      cudaGraph_t tmp;
+      cudaStreamEndCapture(cs, &tmp);
+    }
+    if (cudaStreamIsCapturing(h->cap2, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
+      cudaGraph_t tmp;
+      cudaStreamEndCapture(h->cap2, &tmp);
+    }
+    cudaGetLastError();
+    cudaGraphDestroy(graph);
+    return rc;
+  }
+  *graph_out = graph;
+  return SC_OK;
+}
+
+unsigned row_blocks_for(int64_t n) {
+  // one row per warp, 8 warps per block, grid-stride; 16 blocks of 256 per SM
+  int64_t b = (n + 7) / 8;
+  const int64_t cap = 152 * 16;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+}  // namespace
+
+extern "C" int64_t sc_newmark_workspace_doubles(int64_t n_eq, int64_t) {
+  // vp up x r z p w dinv f  +  part[blocks][4]  +  scalars
+  return 9 * n_eq + 4 * (int64_t)row_blocks_for(n_eq) + 4 * 152 * 16 + 64;
+}
+
+extern "C" int sc_newmark_create(sc_newmark** out, int64_t n_eq, const int64_t* rowptr, const int* cols,
+                                 const double* M, const double* C, const double* K, double* A, double dt, double rtol,
+                                 int max_iter, double* u, double* v, double* a, double* ws, int64_t ws_doubles,
+                                 void* stream) {
+  if (!out || n_eq <= 0 || !rowptr || !cols || !M || !C || !K || !A || !u || !v || !a || !ws) return SC_BAD_ARG;
+  if (!(dt > 0.0) || !(rtol > 0.0) || max_iter <= 0) return SC_BAD_ARG;
+  if (ws_doubles < sc_newmark_workspace_doubles(n_eq, 0)) return SC_BAD_ARG;
+  if ((((uintptr_t)ws) & 15) != 0) return SC_BAD_ARG;
+  sc_newmark* h = new sc_newmark();
+  h->user = (cudaStream_t)stream;
+  h->rtol = rtol;
+  NmArgs& g = h->g;
+  g = NmArgs{};
+  g.n = n_eq;
+  g.rowptr = rowptr;
+  g.cols = cols;
+  g.M = M;
+  g.C = C;
+  g.K = K;
+  g.A = A;
+  g.u = u;
+  g.v = v;
+  g.a = a;
+  double* p = ws;
+  g.vp = p; p += n_eq;
+  g.up = p; p += n_eq;
+  g.x = p; p += n_eq;
+  g.r = p; p += n_eq;
+  g.z = p; p += n_eq;
+  g.p = p; p += n_eq;
+  g.w = p; p += n_eq;
+  g.dinv = p; p += n_eq;
+  g.f = p; p += n_eq;
+  h->row_blocks = row_blocks_for(n_eq);
+  h->vec_blocks = grid_for(n_eq, 256, 152 * 16);
+  g.part = p; p += 4 * (int64_t)(h->row_blocks > h->vec_blocks ? h->row_blocks : h->vec_blocks);
+  // scalars on a 64-byte boundary
+  uintptr_t sp = ((uintptr_t)p + 63) & ~(uintptr_t)63;
+  g.s = (NmScalars*)sp;
+  g.dt = dt;
+  cudaStream_t st = h->user;
+  int rc = SC_OK;
+  int* bad = nullptr;
+  do {
+    if ((rc = check(cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking), "stream"))) break;
+    if ((rc = check(cudaStreamCreateWithFlags(&h->cap2, cudaStreamNonBlocking), "stream"))) break;
+    // A = M + dt/2 C + dt^2/4 K on the shared pattern
+    const int64_t nnz_dummy = 0;
+    (void)nnz_dummy;
+    int64_t nnz = 0;
+    if ((rc = check(cudaMemcpyAsync(&nnz, rowptr + n_eq, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "nnz"))) break;
+    if ((rc = check(cudaStreamSynchronize(st), "sync"))) break;
+    if ((rc = sc_combine(nnz, 1.0, M, 0.5 * dt, C, 0.25 * dt * dt, K, A, st))) break;
+    if ((rc = check(cudaMemsetAsync(g.f, 0, sizeof(double) * n_eq, st), "memset f"))) break;
+    if ((rc = check(cudaMallocAsync((void**)&bad, sizeof(int), st), "malloc"))) break;
+    if ((rc = check(cudaMemsetAsync(bad, 0, sizeof(int), st), "memset"))) break;
+    k_dinv<<<h->vec_blocks, 256, 0, st>>>(n_eq, rowptr, cols, A, g.dinv, bad);
+    k_init_scalars<<<1, 1, 0, st>>>(g.s, rtol * rtol, max_iter);
+    if ((rc = check_launch("newmark init"))) break;
+    int hb = 0;
+    if ((rc = check(cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, st), "memcpy"))) break;
+    if ((rc = check(cudaStreamSynchronize(st), "sync"))) break;
+    if (hb) {
+      rc = SC_BAD_ARG;  // effective matrix has a non-positive diagonal
+      break;
+    }
+  } while (0);
+  if (bad) {
+    cudaFreeAsync(bad, st);
+    cudaStreamSynchronize(st);
+  }
+  if (rc) {
+    sc_newmark_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return SC_OK;
+}
+
+extern "C" int sc_newmark_set_force(sc_newmark* h, int n_t, const int64_t* f_ptr, const int* f_eq,
+                                    const double* f_val) {
+  if (!h || n_t < 0 || (n_t > 0 && (!f_ptr || !f_eq || !f_val))) return SC_BAD_ARG;
+  h->g.n_t = n_t;
+  h->g.f_ptr = n_t > 0 ? f_ptr : nullptr;
+  h->g.f_eq = f_eq;
+  h->g.f_val = f_val;
+  // graphs bake in the arguments: rebuild lazily
+  if (h->step_exec) cudaGraphExecDestroy(h->step_exec), h->step_exec = nullptr;
+  if (h->step_graph) cudaGraphDestroy(h->step_graph), h->step_graph = nullptr;
+  if (h->init_exec) cudaGraphExecDestroy(h->init_exec), h->init_exec = nullptr;
+  if (h->init_graph) cudaGraphDestroy(h->init_graph), h->init_graph = nullptr;
+  return SC_OK;
+}
+
+extern "C" int sc_newmark_set_output(sc_newmark* h, int out_interval, int n_rec, const int* rec_eq, double* out_u,
+                                     double* out_v, double* out_a, int64_t n_out) {
+  if (!h || n_rec < 0 || (n_rec > 0 && (!rec_eq || out_interval <= 0 || n_out <= 0))) return SC_BAD_ARG;
+  h->g.out_interval = out_interval;
+  h->g.n_rec = n_rec;
+  h->g.rec_eq = rec_eq;
+  h->g.out_u = out_u;
+  h->g.out_v = out_v;
+  h->g.out_a = out_a;
+  h->g.n_out = n_out;
+  if (h->step_exec) cudaGraphExecDestroy(h->step_exec), h->step_exec = nullptr;
+  if (h->step_graph) cudaGraphDestroy(h->step_graph), h->step_graph = nullptr;
+  if (h->init_exec) cudaGraphExecDestroy(h->init_exec), h->init_exec = nullptr;
+  if (h->init_graph) cudaGraphDestroy(h->init_graph), h->init_graph = nullptr;
+  return SC_OK;
+}
+
+extern "C" int sc_newmark_initial_acceleration(sc_newmark* h) {
+  if (!h) return SC_BAD_ARG;
+  cudaStream_t st = h->user;
+  NmArgs& g = h->g;
+  int rc;
+  // f = force(0); the dinv of M for this solve
+  if ((rc = check(cudaMemsetAsync(g.f, 0, sizeof(double) * g.n, st), "memset f"))) return rc;
+  k_set_t<<<1, 1, 0, st>>>(g.s, -1);
+  k_force<<<1, 256, 0, st>>>(g);  // writes step 0 entries (t+1 = 0)
+  k_set_t<<<1, 1, 0, st>>>(g.s, 0);
+  if ((rc = check_launch("initial force"))) return rc;
+  // CG on M with its own Jacobi scaling: swap dinv temporarily
+  int* bad = nullptr;
+  if ((rc = check(cudaMallocAsync((void**)&bad, sizeof(int), st), "malloc"))) return rc;
+  cudaMemsetAsync(bad, 0, sizeof(int), st);
+  k_dinv<<<h->vec_blocks, 256, 0, st>>>(g.n, g.rowptr, g.cols, g.M, g.dinv, bad);
+  if (!h->init_exec) {
+    if ((rc = build_pcg_graph(h, g.M, 1, &h->init_graph, &h->init_exec))) {
+      cudaFreeAsync(bad, st);
+      return rc;
+    }
+  }
+  rc = check(cudaGraphLaunch(h->init_exec, st), "launch init");
+  // restore A's Jacobi scaling
+  cudaMemsetAsync(bad, 0, sizeof(int), st);
+  k_dinv<<<h->vec_blocks, 256, 0, st>>>(g.n, g.rowptr, g.cols, g.A, g.dinv, bad);
+  int hb = 0;
+  cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(bad, st);
+  int rc2 = check(cudaStreamSynchronize(st), "sync init");
+  if (rc) return rc;
+  if (rc2) return rc2;
+  if (hb) return SC_BAD_ARG;
+  NmScalars s;
+  if ((rc = check(cudaMemcpy(&s, g.s, sizeof(s), cudaMemcpyDeviceToHost), "read scalars"))) return rc;
+  return s.status;
+}
+
+extern "C" int sc_newmark_run(sc_newmark* h, int t_begin, int t_end) {
+  if (!h || t_begin < 0 || t_end < t_begin) return SC_BAD_ARG;
+  int rc;
+  if (!h->step_exec) {
+    if ((rc = build_pcg_graph(h, h->g.A, 0, &h->step_graph, &h->step_exec))) return rc;
+  }
+  k_set_t<<<1, 1, 0, h->user>>>(h->g.s, t_begin);
+  if ((rc = check_launch("set t"))) return rc;
+  for (int t = t_begin; t < t_end; ++t)
+    if ((rc = check(cudaGraphLaunch(h->step_exec, h->user), "launch step"))) return rc;
+  return SC_OK;
+}
+
+extern "C" int sc_newmark_status(sc_newmark* h, int64_t* total_iters, int* max_iters) {
+  if (!h) return SC_BAD_ARG;
+  int rc = check(cudaStreamSynchronize(h->user), "sync status");
+  if (rc) return rc;
+  NmScalars s;
+  if ((rc = check(cudaMemcpy(&s, h->g.s, sizeof(s), cudaMemcpyDeviceToHost), "read scalars"))) return rc;
+  if (total_iters) *total_iters = s.total_iters;
+  if (max_iters) *max_iters = s.max_seen;
+  return s.status;
+}
+
+extern "C" int sc_newmark_time_spmv(sc_newmark* h, int reps, float* ms_per_launch, int64_t* bytes_per_launch) {
+  if (!h || reps <= 0 || !ms_per_launch) return SC_BAD_ARG;
+  cudaStream_t st = h->user;
+  cudaEvent_t e0, e1;
+  int rc = check(cudaEventCreate(&e0), "event");
+  if (rc) return rc;
+  if ((rc = check(cudaEventCreate(&e1), "event"))) {
+    cudaEventDestroy(e0);
+    return rc;
+  }
+  cudaGraphConditionalHandle none = 0;
+  k_spmv<false><<<h->row_blocks, kRowThreads, 0, st>>>(h->g, h->g.A, none);  // warm
+  cudaEventRecord(e0, st);
+  for (int i = 0; i < reps; ++i) k_spmv<false><<<h->row_blocks, kRowThreads, 0, st>>>(h->g, h->g.A, none);
+  cudaEventRecord(e1, st);
+  rc = check_launch("k_spmv timing");
+  if (!rc) rc = check(cudaEventSynchronize(e1), "event sync");
+  float ms = 0.f;
+  if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+  *ms_per_launch = ms / reps;
+  if (bytes_per_launch) {
+    int64_t nnz = 0;
+    cudaMemcpy(&nnz, h->g.rowptr + h->g.n, sizeof(int64_t), cudaMemcpyDeviceToHost);
+    // values + column indices + row pointers + p (one pass) + w (write)
+    *bytes_per_launch = nnz * 12 + (h->g.n + 1) * 8 + h->g.n * 16;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+extern "C" int sc_newmark_destroy(sc_newmark* h) {
+  if (!h) return SC_OK;
+  if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
+  if (h->step_graph) cudaGraphDestroy(h->step_graph);
+  if (h->init_exec) cudaGraphExecDestroy(h->init_exec);
+  if (h->init_graph) cudaGraphDestroy(h->init_graph);
+  if (h->cap) cudaStreamDestroy(h->cap);
+  if (h->cap2) cudaStreamDestroy(h->cap2);
+  delete h;
+  return SC_OK;
+}

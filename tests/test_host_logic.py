@@ -1,0 +1,119 @@
+"""Host-side logic of the GPU path (no GPU): mesh reading and numbering, Lysmer face
+ordering, force tables -- each against the reference's golden vectors."""
+import os
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from helpers import case, golden_csr, golden_load_table, npz
+from scatter_gb300 import meshgen
+from scatter_gb300.mesher import ReadMesh
+
+CASES = ["column_hexa8_pulse", "column_hexa8_abs", "column_hexa20_abs", "quad4_2d", "tri3_bench2", "tri6_bench2",
+         "tetra4_bench2", "tetra10_bench2", "tetra10_abs", "cube_abs5", "cube_moving"]
+
+
+def _read_back(name, tmp_path):
+    model, spec = case(name)
+    dim = int(model["dimension"])
+    src = SimpleNamespace(nodes=model["nodes"], elem=model["elem"], element_type=model["element_type"],
+                          materials=[[dim, int(i), str(n)] for i, n in zip(model["material_ids"], model["material_names"])],
+                          materials_index=model["materials_index"])
+    path = os.path.join(tmp_path, f"{name}.msh")
+    meshgen.write_gmsh(path, src)
+    m = ReadMesh(path)
+    m.read_gmsh()
+    m.read_bc(spec["boundaries"])
+    m.mapping()
+    m.connectivities()
+    m.get_mesh_edges()
+    return m, model, spec
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_mesher_numbering(name, tmp_path):
+    m, model, spec = _read_back(name, tmp_path)
+    assert m.element_type == model["element_type"] and m.dimension == model["dimension"]
+    np.testing.assert_array_equal(m.BC, model["BC"])
+    np.testing.assert_array_equal(m.BC_dir, model["BC_dir"])
+    np.testing.assert_array_equal(m.eq_nb_dof, model["eq_nb_dof"])
+    np.testing.assert_array_equal(m.eq_nb_elem, model["eq_nb_elem"])
+    assert m.number_eq == model["number_eq"]
+    if "boundary_elem" in model:
+        np.testing.assert_array_equal(m.boundary_elem, model["boundary_elem"])
+
+
+@pytest.mark.parametrize("name", ["column_hexa8_abs", "column_hexa20_abs", "tetra4_abs", "tetra10_abs", "cube_abs5"])
+def test_lysmer_face_ordering(name):
+    """Host face ordering + oracle face integrals reproduce the reference's absorbing matrices."""
+    from helpers import element_props
+    from oracle import elements as el
+    from scatter_gb300.lysmer import boundary_faces
+    from scatter_gb300.system_matrix import FACE_TYPES
+
+    model, spec = case(name)
+    ns = SimpleNamespace(**{k: model[k] for k in ("nodes", "elem", "BC", "BC_dir", "eq_nb_dof")},
+                         element_type=model["element_type"])
+    props = element_props(model, spec["materials"])
+    faces = boundary_faces(ns, props, spec["absorbing"])
+    F = el.face_matrix(FACE_TYPES[model["element_type"]], faces["xy"], 2)
+    n = model["number_eq"]
+    nf = faces["eqs"].shape[1]
+    r = np.repeat(faces["eqs"], nf, axis=1).ravel()
+    c = np.tile(faces["eqs"], (1, nf)).ravel()
+    Cv = (F * faces["fct"][:, None, :]).ravel()
+    Kv = (np.abs(F) * faces["fct2"][:, None, :]).ravel()
+    C = sp.csr_matrix((Cv, (r, c)), shape=(n, n))
+    K = sp.csr_matrix((Kv, (r, c)), shape=(n, n)) / spec["k_div"]
+    g = npz(f"mat_{name}.npz")
+    gC, gK = golden_csr(g, "Cabs"), golden_csr(g, "Kabs")
+    assert gC.nnz > 0
+    assert abs(C - gC).max() <= 1e-14 * abs(gC).max()
+    assert abs(K - gK).max() <= 1e-14 * abs(gK).max()
+
+
+@pytest.mark.parametrize("name", ["column_hexa8_pulse", "column_hexa8_abs", "quad4_2d", "tri3_bench2",
+                                  "tetra10_bench2", "cube_moving", "cube_plane"])
+def test_force_tables(name, tmp_path):
+    from scatter_gb300.force_external import Force
+    from scatter_gb300.validator import ValidateLoad
+
+    m, model, spec = _read_back(name, tmp_path)
+    load = dict(spec["load"])
+    ValidateLoad.validate(load)
+    time = np.linspace(0, load["time"], int(np.ceil(load["time"] / spec["dt"]) + 1))
+    top = m.get_top_surface() if load["type"] == "moving_at_plane" else []
+    F = Force()
+    F.initialise_load(load, time, m, None, top_surface_elements=top)
+    Fg, tg = golden_load_table(name)
+    dense = np.stack([F.table.dense(t) for t in range(len(time))])
+    assert np.abs(dense - Fg).max() <= 1e-12 * max(np.abs(Fg).max(), 1.0)
+    np.testing.assert_array_equal(F.update_load_at_t(3), Fg[3])
+
+
+def test_structured_box_numbering_and_jacobian():
+    from oracle import elements as el
+
+    m = meshgen.box_model(3, 4, 2, 0.5, bottom="020", x_faces="200", z_faces="002")
+    assert m.number_eq == 3 * len(m.nodes)
+    X = m.nodes[:, 1:][m.elem - 1]
+    _, _, detJ, _ = el.geometry("hexa8", X, 2)
+    assert (detJ > 0).all()
+    t = meshgen.box_model(2, 2, 2, 0.5, element="tetra10")
+    X = t.nodes[:, 1:][t.elem - 1]
+    _, _, detJ, _ = el.geometry("tetra10", X, 2)
+    assert (detJ > 0).all()
+    # conforming: every mid-side node is shared by all tets around its edge
+    assert len(t.nodes) == (5 * 5 * 5)  # (2*2+1)^3 vertices + mid-sides on the refined lattice
+
+
+def test_validator_defaults():
+    from scatter_gb300.validator import ValidateLoad
+
+    load = {"type": "heaviside"}
+    ValidateLoad.validate(load)
+    assert load["ini_steps"] == 5
+    with pytest.raises(Exception):
+        ValidateLoad.validate({"type": "unknown"})
