@@ -173,12 +173,13 @@ def run_gb300(args):
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from scatter_gb300 import _native
-    from scatter_gb300.solvers import NewmarkGPU
+    from scatter_gb300.solvers import NodeBlockNewmark
     from scatter_gb300.system_matrix import GenerateMatrix
 
     _native.load()
     t_setup = time.perf_counter()
-    model, load, time_grid, rec_eq = workload()
+    dims = tuple(int(x) for x in args.dims.split(",")) + (0.5,) if args.dims else DIMS
+    model, load, time_grid, rec_eq = workload(dims)
     table = force_table(model, load, time_grid)
     t_host = time.perf_counter() - t_setup
     torch.cuda.synchronize()
@@ -193,7 +194,10 @@ def run_gb300(args):
     K_steps, W = args.steps, args.warmup
     if W + K_steps + 1 > len(time_grid):
         raise SystemExit("steps + warmup exceed the 10,000-step load history")
-    solver = NewmarkGPU(g.pattern, g.M_d, g.C_d, g.K_d, DT)
+    t0 = time.perf_counter()
+    solver = NodeBlockNewmark(g, DT)
+    torch.cuda.synchronize()
+    t_solver_setup = time.perf_counter() - t0
     solver.set_force(table)
     solver.set_output(1, rec_eq, len(time_grid), what=("v",))
     solver.initial_acceleration()
@@ -223,38 +227,42 @@ def run_gb300(args):
         ms = float(tt.item())
     value = ws * n * K_steps / (ms / 1e3)
 
-    # dominant kernel: the PCG SpMV, timed standalone on the solver's stream
-    import ctypes
-
-    mspl = ctypes.c_float()
-    bpl = ctypes.c_int64()
-    _native.call("sc_newmark_time_spmv", solver.h, 20, ctypes.byref(mspl), ctypes.byref(bpl))
+    # dominant kernel: the PCG block SpMV, timed standalone on the solver's stream
+    ms_spmv, bytes_spmv = solver.time_spmv(20)
     peak, peak_kind = peaks()
-    achieved = bpl.value / (mspl.value * 1e-3) / 1e9
+    achieved = bytes_spmv / (ms_spmv * 1e-3) / 1e9
     traffic = profile_traffic()
 
     # end to end through the solver API: each step copies its force entries host->device from
     # pinned memory and reads the step's receiver velocities back to pinned host memory
-    e2e = e2e_run(solver, table, rec_eq, W + K_steps, min(K_steps, len(time_grid) - 1 - (W + K_steps)), n)
+    e2e = None if args.no_e2e else e2e_run(solver, table, rec_eq, W + K_steps,
+                                          min(K_steps, len(time_grid) - 1 - (W + K_steps)), n)
+    # the added explicit scheme (lumped mass, one fused kernel per step) on the same model
+    explicit = explicit_run(g, table, rec_eq, K_steps, W, n)
 
     out = {"metric": METRIC, "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": K_steps, "warmup": W,
            "ms_per_step": ms / K_steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f64", "data": "synthetic (seeded structured mesh, moving point load)",
            "config": {"workload": "plain Newmark FP64, box 60x40x30 m hexa8 0.5 m (120x80x60 el), 2 layers, "
-                                  "Lysmer sides+base, moving 100 kN at 40 km/h, dt 5e-5",
+                                  "Lysmer sides+base, moving 100 kN at 40 km/h, dt 5e-5" if not args.dims
+                      else f"profiling case: box {args.dims} hexa8 0.5 m, same physics",
                       "n_eq": n, "nnz": g.pattern.nnz, "elements": int(len(model.elem)), "receivers": len(rec_eq),
                       "parallelism": f"replicas x{ws}",
                       "l2": "inputs larger than L2 (CSR values+cols 5.1 GB), no flush",
-                      "solver": "Newmark beta=1/4 gamma=1/2, Jacobi-PCG rtol 1e-12 per step"},
+                      "solver": "Newmark beta=1/4 gamma=1/2; per step PCG (FSAI preconditioner, FP32 factor), "
+                                "quadratic warm start, rtol 1e-12; node-block FP64 operator"},
            "cg_iters_per_step": iters / K_steps, "cg_iters_max": it_max,
-           "setup_s": {"host_mesh_and_loads": round(t_host, 2), "gpu_assembly_lysmer_rayleigh": round(t_assembly, 3)},
-           "gpu_launches": 7 * K_steps + 3 * iters + 1,
-           "roofline": {"bound": "hbm", "kernel": "k_spmv (CSR FP64, w = A p)", "achieved": achieved,
+           "setup_s": {"host_mesh_and_loads": round(t_host, 2), "gpu_assembly_lysmer_rayleigh": round(t_assembly, 3),
+                       "gpu_solver_setup_fsai": round(t_solver_setup, 3)},
+           "fsai_fallback_rows": solver.fsai_fallback_rows,
+           "gpu_launches": 8 * K_steps + 5 * iters + 1,
+           "roofline": {"bound": "hbm", "kernel": "nb::k_spmv (3x3 node blocks FP64, w = A p)", "achieved": achieved,
                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                        "traffic": traffic, "bytes_per_launch": bpl.value, "ms_per_launch": mspl.value},
-           "clocks": clk.summary(), "e2e": e2e}
+                        "traffic": traffic, "bytes_per_launch": bytes_spmv, "ms_per_launch": ms_spmv},
+           "clocks": clk.summary(), "e2e": e2e, "explicit_lumped": explicit}
     # CPU baseline (rank 0 only, N = 1): the oracle's C loop on the host cores
     if rank == 0 and ws == 1 and not args.no_cpu:
+        solver.close()
         rp = g.pattern.rowptr.cpu().numpy()
         cl = g.pattern.cols.cpu().numpy()
         Mh, Ch, Kh = (x.cpu().numpy() for x in (g.M_d, g.C_d, g.K_d))
@@ -266,13 +274,44 @@ def run_gb300(args):
         torch.distributed.destroy_process_group()
 
 
+def explicit_run(g, table, rec_eq, k, w, n):
+    """DOF-steps/s of the explicit lumped-mass scheme (no reference counterpart) on the model."""
+    import torch
+
+    from scatter_gb300.explicit import critical_time_step
+    from scatter_gb300.solvers import NodeBlockNewmark
+
+    dtc = critical_time_step(g)
+    s = NodeBlockNewmark(g, DT, precond="jacobi")
+    s.set_force(table)
+    s.set_output(1, rec_eq, len(table.f_ptr) - 1, what=("v",))
+    s.run_explicit(0, w)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    s.run_explicit(w, w + k)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    ms_k = s.time_explicit(20)
+    d2 = g.dim * g.dim
+    sell_entries = int(s.g.adj.numel())  # stored blocks (sliced-ELL adds row padding)
+    bytes_step = sell_entries * (8 * d2 + 4) + g.n_nodes * g.dim * 8 * 6
+    s.close()
+    return {"value": n * k / (ms / 1e3), "unit": "DOF-steps/s", "ms_per_step": ms / k, "steps": k,
+            "dt": DT, "dt_critical_bound": dtc, "kernel_ms": ms_k,
+            "kernel_gbs": bytes_step / (ms_k * 1e-3) / 1e9,
+            "note": "central difference, row-sum lumped mass (no reference counterpart); FP64"}
+
+
 def e2e_run(solver, table, rec_eq, t0, k, n):
     import torch
 
     if k <= 0:
         return None
     p, e, v = solver._keep_force
-    host_eq = torch.from_numpy(table.f_eq).pin_memory()
+    host_eq = e.cpu().pin_memory()  # slot indices of the force entries, as the solver reads them
     host_val = torch.from_numpy(table.f_val).pin_memory()
     out_v = solver.out["v"].view(solver.n_out, solver.n_rec)
     host_out = torch.empty((k, solver.n_rec), dtype=torch.float64).pin_memory()
@@ -380,6 +419,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--dims", default="", help="nx,ny,nz of a smaller box (profiling cases)")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")

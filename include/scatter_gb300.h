@@ -162,6 +162,49 @@ int sc_newmark_status(sc_newmark* h, int64_t* total_iters, int* max_iters_per_st
 int sc_newmark_time_spmv(sc_newmark* h, int reps, float* ms_per_launch, int64_t* bytes_per_launch);
 int sc_newmark_destroy(sc_newmark* h);
 
+/* ------------------------------------------------------------------ node-block Newmark
+ * The same time loop as sc_newmark_* for matrices assembled by this library from a mesh
+ * (node adjacency known), on a node-block layout: unknowns in slot space (slot = node*dim +
+ * dof, fixed DOFs kept as decoupled zero slots), K and A = M + dt/2 C + dt^2/4 K as dim x dim
+ * FP64 blocks over the node adjacency (one plane per block component), the consistent mass
+ * as one scalar per node pair, and Rayleigh damping C = Cabs + alpha M + beta K with the
+ * Lysmer dashpots Cabs as a small slot-space CSR (scatter/system_matrix.py:166-198,375).
+ * Each step solves A x = f - C vp - K up by PCG preconditioned with a factorised sparse
+ * approximate inverse G^T G of A (FP32 factor on the lower node pattern, built on the GPU),
+ * warm-started from the quadratic extrapolation of the acceleration history, to
+ * ||r|| <= rtol ||rhs||.  eqmap [n_nodes][dim] (-1 fixed); rowptr/cols/K/M/C the eq-space
+ * CSR from sc_csr_pattern + sc_assemble_values (+ Lysmer / Rayleigh); cab_* the Lysmer
+ * dashpot matrix in slot space (n_cab entries).  u, v, a: slot-space state [n_nodes*dim].
+ * Force table and receivers use slot indices.  workspace: sc_nb_workspace_bytes(), 256-byte
+ * aligned.  precond: 0 = FSAI (rows whose pattern exceeds 63 slots use a Jacobi row, counted
+ * in sc_nb_status), 1 = Jacobi (the FSAI factor restricted to the diagonal). */
+typedef struct sc_nb_newmark sc_nb_newmark;
+int64_t sc_nb_workspace_bytes(int n_nodes, int dim, int64_t nnzb);
+int sc_nb_create(sc_nb_newmark** h, int n_nodes, int dim, const int* eqmap, const int64_t* adj_ptr, const int* adj,
+                 int64_t nnzb, const int64_t* rowptr, const int* cols, const double* K, const double* M,
+                 const double* C, int64_t n_cab, const int64_t* cab_ptr, const int* cab_col, const double* cab_val,
+                 double alpha, double beta, double dt, double rtol, int max_iter, int precond, double* u, double* v,
+                 double* a, void* workspace, int64_t workspace_bytes, void* stream);
+int sc_nb_set_force(sc_nb_newmark* h, int n_t, const int64_t* f_ptr, const int* f_slot, const double* f_val);
+int sc_nb_set_output(sc_nb_newmark* h, int out_interval, int n_rec, const int* rec_slot, double* out_u,
+                     double* out_v, double* out_a, int64_t n_out);
+/* steps t_begin .. t_end-1 (asynchronous graph launches) */
+int sc_nb_run(sc_nb_newmark* h, int t_begin, int t_end);
+int sc_nb_status(sc_nb_newmark* h, int64_t* total_iters, int* max_iters_per_step, int* fsai_fallback_rows);
+/* timing aid: the step loop's block SpMV (w = A p) launched `reps` times between CUDA events */
+int sc_nb_time_spmv(sc_nb_newmark* h, int reps, float* ms_per_launch, int64_t* bytes_per_launch);
+/* Explicit central-difference steps on the same handle (no reference counterpart: the
+ * reference's mass is always consistent):
+ *   a_n = M_L^-1 (f_n - K (u_n + beta v_{n-1/2}) - alpha M_L v_{n-1/2} - Cabs v_{n-1/2}),
+ *   v_{n+1/2} = v_{n-1/2} + dt a_n,  u_{n+1} = u_n + dt v_{n+1/2},
+ * M_L the row-sum lumped mass; one fused kernel per step over the sliced-ELL K.  Receivers
+ * record u_{n+1} and v_{n+1/2}.  Conditionally stable (dt below the lumped-mass CFL limit).
+ * The first call allocates the scheme's extra vectors (setup); later calls allocate nothing. */
+int sc_nb_explicit_run(sc_nb_newmark* h, int t_begin, int t_end);
+/* timing aid: the explicit step kernel alone, `reps` launches between CUDA events */
+int sc_nb_time_explicit(sc_nb_newmark* h, int reps, float* ms_per_step);
+int sc_nb_destroy(sc_nb_newmark* h);
+
 #ifdef __cplusplus
 }
 #endif

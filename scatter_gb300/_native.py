@@ -41,6 +41,17 @@ SIGNATURES = {
     "sc_newmark_status": (I, [P, ctypes.POINTER(L), ctypes.POINTER(I)]),
     "sc_newmark_time_spmv": (I, [P, I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(L)]),
     "sc_newmark_destroy": (I, [P]),
+    "sc_nb_workspace_bytes": (L, [I, I, L]),
+    "sc_nb_create": (I, [ctypes.POINTER(P), I, I, P, P, P, L, P, P, P, P, P, L, P, P, P, D, D, D, D, I, I, P, P, P, P,
+                         L, P]),
+    "sc_nb_set_force": (I, [P, I, P, P, P]),
+    "sc_nb_set_output": (I, [P, I, I, P, P, P, P, L]),
+    "sc_nb_run": (I, [P, I, I]),
+    "sc_nb_status": (I, [P, ctypes.POINTER(L), ctypes.POINTER(I), ctypes.POINTER(I)]),
+    "sc_nb_time_spmv": (I, [P, I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(L)]),
+    "sc_nb_explicit_run": (I, [P, I, I]),
+    "sc_nb_time_explicit": (I, [P, I, ctypes.POINTER(ctypes.c_float)]),
+    "sc_nb_destroy": (I, [P]),
 }
 
 ELEMENT_CODES = {"hexa8": 0, "hexa20": 1, "tetra4": 2, "tetra10": 3, "quad4": 4, "quad8": 5, "tri3": 6, "tri6": 7}

@@ -1,0 +1,1335 @@
+// Node-block Newmark solver: the time loop of the reference (PuggleSolvers NewmarkExplicit as
+// driven by scatter/scatter.py:120-159: beta = 1/4, gamma = 1/2, consistent mass, constant
+// effective matrix) on a 3x3 (2x2 in 2D) node-block layout.
+//
+// Layout (HBM).  Unknowns live in "slot" space: slot = node * D + d for every node and DOF,
+// fixed DOFs included as decoupled slots whose values stay 0.  Matrices are blocks over the
+// node adjacency of the element graph (adj_ptr/adj, neighbours sorted, self included):
+//   KB, AB  [D*D][nnzb] FP64, one plane per block component (lane-coalesced loads)
+//   MS      [nnzb] FP64   the consistent mass is m_ab * I per node pair (Me = rho N^T N)
+//   GB, GTB [D*D][nnzb] FP32  factorised sparse approximate inverse (FSAI) of A: G on the
+//           lower part of each node row (neighbours b <= a), G^T on the upper part
+//   Cabs    small slot-space CSR holding the Lysmer dashpots (boundary rows only)
+// with A = M + dt/2 C + dt^2/4 K and C = Cabs + alpha M + beta K (Rayleigh), so
+//   b  = f - C vp - K up = f - K q1 - M q2 - Cabs y1
+//   q1 = up + beta y1, q2 = alpha y1, y1 = vp (+ the usual predictor terms, see k_predict)
+// Each step solves A x = b for the new acceleration by PCG with preconditioner G^T G,
+// warm-started from the quadratic extrapolation 3a_n - 3a_{n-1} + a_{n-2}, stopped at
+// ||r|| <= rtol ||b||; then u, v, a are updated exactly as the reference's update.
+//
+// Kernels: one warp per node row (lanes over the row's blocks) for every block product;
+// per-block partial sums reduced by the last block (ticket, fixed order, no spin-waits);
+// one CUDA graph per step with a device-side WHILE conditional around the PCG body.
+#include <math.h>
+
+#include "sc_common.cuh"
+
+namespace sc {
+namespace nb {
+
+constexpr int kThreads = 256;
+constexpr int kMaxFsai = 64;  // FSAI row pattern capacity (slots); larger rows fall back to Jacobi
+
+struct Scal {
+  double rz, pw, rr, bb, alpha, beta, tol2, pad0;
+  long long total_iters;
+  int it, max_it, max_seen, status, t, fsai_fallback;
+  unsigned int ticket;
+  int hist;  // valid previous accelerations (0..2) for the warm start
+  unsigned int pad2[2];
+};
+
+struct Args {
+  int n_nodes, D;
+  int64_t n_s;  // slots
+  int64_t nnzb;
+  const int64_t* adj_ptr;
+  const int* adj;
+  const int64_t* diag;  // position of the node itself in its adjacency row
+  const int* fixed;     // [n_s] 1 = fixed slot
+  const double *KB, *AB, *MS;
+  const float *GB, *GTB;
+  const int64_t* cab_ptr;
+  const int* cab_col;
+  const double* cab_val;
+  // sliced-ELL copies used by the per-step kernels (32 node rows per slice, column-major):
+  // full pattern (K, A, M), lower (G), upper (G^T)
+  int64_t n_slices;
+  const int64_t *sf_ptr, *sl_ptr, *su_ptr;
+  const int *sf_col, *sl_col, *su_col;
+  int64_t sf_n, sl_n, su_n;
+  const double *KS, *AS, *MSS;
+  const float *GS, *GTS;
+  double alpha_r, beta_r;  // Rayleigh coefficients
+  double aM, aK, aC;       // A = aM M + aK K + aC Cabs
+  double dt;
+  double *u, *v, *a, *a1, *a2;
+  double *q1, *q2, *y1, *x0, *x, *r, *z, *p, *w, *f;
+  float* t32;
+  double* part;
+  Scal* s;
+  // force (slot indices)
+  int n_t;
+  const int64_t* f_ptr;
+  const int* f_slot;
+  const double* f_val;
+  // output
+  int out_interval, n_rec;
+  const int* rec_slot;
+  double *out_u, *out_v, *out_a;
+  int64_t n_out;
+};
+
+__device__ inline bool last_block(unsigned int* ticket) {
+  __shared__ bool am_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) am_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  return am_last;
+}
+
+__device__ inline double reduce_parts(const double* part, int k, double* sh) {
+  double s = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(part + b * 4 + k);
+  return block_sum(s, sh);
+}
+
+template <int D>
+__device__ inline void warp_sum3(double* s) {
+#pragma unroll
+  for (int c = 0; c < D; ++c) s[c] = warp_sum(s[c]);
+}
+
+// ------------------------------------------------------------------ per-step kernels
+__global__ void k_force(Args g) {
+  const int t = g.s->t;
+  if (!g.f_ptr) return;
+  if (t >= 0 && t < g.n_t)
+    for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f[g.f_slot[k]] = 0.0;
+  __syncthreads();
+  const int t1 = t + 1;
+  if (t1 >= 0 && t1 < g.n_t)
+    for (int64_t k = g.f_ptr[t1] + threadIdx.x; k < g.f_ptr[t1 + 1]; k += blockDim.x)
+      g.f[g.f_slot[k]] += g.f_val[k];
+}
+
+// Predictor vectors (slot space):
+//   vp = v + dt/2 a, up = u + dt v + dt^2/4 a                  (Newmark predictors)
+//   b = f - C vp - K up,  C = Cabs + alpha M + beta K
+//     = f - K (up + beta vp) - M (alpha vp) - Cabs vp
+//   x0 = warm start;  A x0 = aM M x0 + aK K x0 + aC Cabs x0
+// stored: q1 = up + beta vp, q2 = alpha vp, y1 = vp, x0.
+__global__ void k_predict(Args g) {
+  const double dt = g.dt, h = 0.5 * dt, qq = 0.25 * dt * dt;
+  const int hist = g.s->hist;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
+    const double ai = g.a[i], vi = g.v[i];
+    const double vp = vi + h * ai;
+    const double up = g.u[i] + dt * vi + qq * ai;
+    g.q1[i] = up + g.beta_r * vp;
+    g.q2[i] = g.alpha_r * vp;
+    g.y1[i] = vp;
+    double x0 = ai;
+    if (hist >= 2) x0 = 3.0 * ai - 3.0 * g.a1[i] + g.a2[i];
+    else if (hist == 1) x0 = 2.0 * ai - g.a1[i];
+    if (g.fixed[i]) x0 = 0.0;
+    g.x0[i] = x0;
+  }
+}
+
+// Per-step block kernels: one thread per node row over the sliced-ELL copies.  A warp is one
+// slice of 32 consecutive node rows; entry j of every row of the slice sits at
+// ptr[slice] + 32 j + lane, so each plane load is 32 consecutive values.  Padding entries
+// point at a valid node with zero values.
+#define SELL_ROW_LOOP(ptr)                                                                      \
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < g.n_slices * 32;    \
+       row += (int64_t)gridDim.x * blockDim.x)
+
+// r = b - A x0 with b = f - K q1 - M q2 - Cabs y1; bb = |b|^2.  x = x0.
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_residual(Args g) {
+  __shared__ double sh[32];
+  double pbb = 0.0;
+  SELL_ROW_LOOP(g.sf_ptr) {
+    const int64_t sl = row >> 5;
+    const int64_t p0 = g.sf_ptr[sl] + (row & 31), W = (g.sf_ptr[sl + 1] - g.sf_ptr[sl]) >> 5;
+    double sb[D], sx[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) sb[c] = sx[c] = 0.0;
+    for (int64_t j = 0; j < W; ++j) {
+      const int64_t pos = p0 + 32 * j;
+      const int64_t bs = (int64_t)__ldcs(g.sf_col + pos) * D;
+      double qa[D], xa[D], q2a[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        qa[d] = g.q1[bs + d];
+        xa[d] = g.x0[bs + d];
+        q2a[d] = g.q2[bs + d];
+      }
+      const double m = __ldcs(g.MSS + pos);
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        double sq = m * q2a[c], sxx = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          const double kv = __ldcs(g.KS + (int64_t)(c * D + d) * g.sf_n + pos);
+          sq = fma(kv, qa[d], sq);
+          sxx = fma(kv, xa[d], sxx);
+        }
+        sb[c] += sq;
+        sx[c] = fma(g.aK, sxx, fma(g.aM * m, xa[c], sx[c]));
+      }
+    }
+    if (row < g.n_nodes) {
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        const int64_t i = row * D + c;
+        double bv = 0.0, rv = 0.0;
+        if (!g.fixed[i]) {
+          double cb = 0.0, cx = 0.0;  // Lysmer dashpots (boundary rows only)
+          for (int64_t k = g.cab_ptr[i]; k < g.cab_ptr[i + 1]; ++k) {
+            const int jj = g.cab_col[k];
+            cb = fma(g.cab_val[k], g.y1[jj], cb);
+            cx = fma(g.cab_val[k], g.x0[jj], cx);
+          }
+          bv = g.f[i] - sb[c] - cb;
+          rv = bv - (sx[c] + g.aC * cx);
+        }
+        g.r[i] = rv;
+        g.x[i] = g.x0[i];
+        pbb += bv * bv;
+      }
+    }
+  }
+  const double t = block_sum(pbb, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 2] = t;
+  if (last_block(&g.s->ticket)) {
+    const double bb = reduce_parts(g.part, 2, sh);
+    if (threadIdx.x == 0) {
+      g.s->bb = bb;
+      g.s->it = 0;
+      g.s->ticket = 0;
+    }
+  }
+}
+
+// t = G r  (lower pattern, FP32 factor, FP32 result)
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_prec_lower(Args g) {
+  SELL_ROW_LOOP(g.sl_ptr) {
+    const int64_t sl = row >> 5;
+    const int64_t p0 = g.sl_ptr[sl] + (row & 31), W = (g.sl_ptr[sl + 1] - g.sl_ptr[sl]) >> 5;
+    float s[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) s[c] = 0.f;
+    for (int64_t j = 0; j < W; ++j) {
+      const int64_t pos = p0 + 32 * j;
+      const int64_t bs = (int64_t)__ldcs(g.sl_col + pos) * D;
+      float ra[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) ra[d] = (float)g.r[bs + d];
+#pragma unroll
+      for (int c = 0; c < D; ++c)
+#pragma unroll
+        for (int d = 0; d < D; ++d) s[c] = fmaf(__ldcs(g.GS + (int64_t)(c * D + d) * g.sl_n + pos), ra[d], s[c]);
+    }
+    if (row < g.n_nodes) {
+#pragma unroll
+      for (int c = 0; c < D; ++c) g.t32[row * D + c] = s[c];
+    }
+  }
+}
+
+// z = G^T t ; partial r.z ; mode 0 (inside PCG): last block computes beta, rz;
+// mode 1 (after the residual): p = z, rz, rr and the conditional from |r| vs |b|.
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_prec_upper(Args g, int mode, cudaGraphConditionalHandle hc) {
+  __shared__ double sh[32];
+  double prz = 0.0, prr = 0.0;
+  SELL_ROW_LOOP(g.su_ptr) {
+    const int64_t sl = row >> 5;
+    const int64_t p0 = g.su_ptr[sl] + (row & 31), W = (g.su_ptr[sl + 1] - g.su_ptr[sl]) >> 5;
+    float s[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) s[c] = 0.f;
+    for (int64_t j = 0; j < W; ++j) {
+      const int64_t pos = p0 + 32 * j;
+      const int64_t bs = (int64_t)__ldcs(g.su_col + pos) * D;
+      float ta[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) ta[d] = g.t32[bs + d];
+#pragma unroll
+      for (int c = 0; c < D; ++c)
+#pragma unroll
+        for (int d = 0; d < D; ++d) s[c] = fmaf(__ldcs(g.GTS + (int64_t)(c * D + d) * g.su_n + pos), ta[d], s[c]);
+    }
+    if (row < g.n_nodes) {
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        const int64_t i = row * D + c;
+        const double z = (double)s[c];
+        const double r = g.r[i];
+        g.z[i] = z;
+        if (mode == 1) g.p[i] = z;
+        prz += r * z;
+        prr += r * r;
+      }
+    }
+  }
+  double t = block_sum(prz, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 0] = t;
+  if (mode == 1) {
+    t = block_sum(prr, sh);
+    if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 1] = t;
+  }
+  if (last_block(&g.s->ticket)) {
+    const double rz = reduce_parts(g.part, 0, sh);
+    const double rr = mode == 1 ? reduce_parts(g.part, 1, sh) : 0.0;
+    if (threadIdx.x == 0) {
+      Scal* s = g.s;
+      s->ticket = 0;
+      if (mode == 1) {
+        s->rz = rz;
+        s->rr = rr;
+        const bool done = rr <= s->tol2 * s->bb;
+        cudaGraphSetConditional(hc, done ? 0u : 1u);
+      } else {
+        s->beta = s->rz != 0.0 ? rz / s->rz : 0.0;
+        s->rz = rz;
+      }
+    }
+  }
+}
+
+// w = A p ; partial p.w ; last block: alpha
+template <int D, bool kInGraph>
+__global__ void __launch_bounds__(kThreads) k_spmv(Args g, cudaGraphConditionalHandle hc) {
+  __shared__ double sh[32];
+  double ppw = 0.0;
+  SELL_ROW_LOOP(g.sf_ptr) {
+    const int64_t sl = row >> 5;
+    const int64_t p0 = g.sf_ptr[sl] + (row & 31), W = (g.sf_ptr[sl + 1] - g.sf_ptr[sl]) >> 5;
+    double s[D][D];
+#pragma unroll
+    for (int c = 0; c < D; ++c)
+#pragma unroll
+      for (int d = 0; d < D; ++d) s[c][d] = 0.0;
+    for (int64_t j = 0; j < W; ++j) {
+      const int64_t pos = p0 + 32 * j;
+      const int64_t bs = (int64_t)__ldcs(g.sf_col + pos) * D;
+      double pa[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) pa[d] = g.p[bs + d];
+#pragma unroll
+      for (int c = 0; c < D; ++c)
+#pragma unroll
+        for (int d = 0; d < D; ++d) s[c][d] = fma(__ldcs(g.AS + (int64_t)(c * D + d) * g.sf_n + pos), pa[d], s[c][d]);
+    }
+    if (row < g.n_nodes) {
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        double wv = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) wv += s[c][d];
+        const int64_t i = row * D + c;
+        g.w[i] = wv;
+        ppw += g.p[i] * wv;
+      }
+    }
+  }
+  const double t = block_sum(ppw, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 3] = t;
+  if (last_block(&g.s->ticket)) {
+    const double pw = reduce_parts(g.part, 3, sh);
+    if (threadIdx.x == 0) {
+      Scal* s = g.s;
+      s->ticket = 0;
+      s->pw = pw;
+      if (kInGraph) {
+        if (!(pw > 0.0)) {
+          s->alpha = 0.0;
+          s->status = SC_BREAKDOWN;
+          cudaGraphSetConditional(hc, 0u);
+        } else {
+          s->alpha = s->rz / pw;
+        }
+      }
+    }
+  }
+}
+
+// x += alpha p ; r -= alpha w ; partial r.r ; last block: convergence test
+__global__ void k_update(Args g, cudaGraphConditionalHandle hc) {
+  __shared__ double sh[32];
+  const double alpha = g.s->alpha;
+  double prr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
+    g.x[i] = fma(alpha, g.p[i], g.x[i]);
+    const double r = fma(-alpha, g.w[i], g.r[i]);
+    g.r[i] = r;
+    prr += r * r;
+  }
+  const double t = block_sum(prr, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 1] = t;
+  if (last_block(&g.s->ticket)) {
+    const double rr = reduce_parts(g.part, 1, sh);
+    if (threadIdx.x == 0) {
+      Scal* s = g.s;
+      s->ticket = 0;
+      s->rr = rr;
+      s->it += 1;
+      bool done = rr <= s->tol2 * s->bb;
+      if (!done && s->it >= s->max_it) {
+        if (!s->status) s->status = SC_NOT_CONVERGED;
+        done = true;
+      }
+      if (s->status == SC_BREAKDOWN) done = true;
+      if (done) cudaGraphSetConditional(hc, 0u);
+    }
+  }
+}
+
+__global__ void k_direction(Args g) {
+  const double beta = g.s->beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x)
+    g.p[i] = fma(beta, g.p[i], g.z[i]);
+}
+
+// u = up + dt^2/4 x ; v = vp + dt/2 x ; shift the acceleration history ; record ; t += 1
+__global__ void k_finalize(Args g) {
+  const double dt = g.dt, h = 0.5 * dt, qq = 0.25 * dt * dt;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = g.x[i], ai = g.a[i], vi = g.v[i];
+    const double up = g.u[i] + dt * vi + qq * ai;
+    const double vp = vi + h * ai;
+    g.u[i] = fma(qq, x, up);
+    g.v[i] = fma(h, x, vp);
+    g.a2[i] = g.a1[i];
+    g.a1[i] = ai;
+    g.a[i] = x;
+  }
+}
+
+__global__ void k_record(Args g) {
+  const int step = g.s->t + 1;
+  if (g.n_rec > 0 && g.out_interval > 0 && step % g.out_interval == 0) {
+    const int64_t row = step / g.out_interval;
+    if (row < g.n_out)
+      for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.n_rec;
+           j += (int64_t)gridDim.x * blockDim.x) {
+        const int e = g.rec_slot[j];
+        if (g.out_u) g.out_u[row * g.n_rec + j] = g.u[e];
+        if (g.out_v) g.out_v[row * g.n_rec + j] = g.v[e];
+        if (g.out_a) g.out_a[row * g.n_rec + j] = g.a[e];
+      }
+  }
+}
+
+__global__ void k_advance(Args g) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    Scal* s = g.s;
+    s->total_iters += s->it;
+    if (s->it > s->max_seen) s->max_seen = s->it;
+    s->t += 1;
+    if (s->hist < 2) s->hist += 1;
+  }
+}
+
+// ------------------------------------------------------------------ setup kernels
+__device__ inline int64_t find_in(const int* adj, int64_t lo, int64_t hi, int key) {
+  const int64_t end = hi;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (adj[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return (lo < end && adj[lo] == key) ? lo : -1;
+}
+
+__device__ inline double csr_value(const int64_t* rowptr, const int* cols, const double* val, int row, int col) {
+  int64_t lo = rowptr[row], hi = rowptr[row + 1];
+  const int64_t end = hi;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (cols[mid] < col) lo = mid + 1;
+    else hi = mid;
+  }
+  return (lo < end && cols[lo] == col) ? val[lo] : 0.0;
+}
+
+// diag position and fixed-slot flags
+__global__ void k_setup_nodes(int n_nodes, int D, const int* eqmap, const int64_t* adj_ptr, const int* adj,
+                              int64_t* diag, int* fixed, int* bad) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n_nodes; a += gridDim.x * blockDim.x) {
+    const int64_t k = find_in(adj, adj_ptr[a], adj_ptr[a + 1], a);
+    if (k < 0) atomicExch(bad, 1);
+    diag[a] = k < 0 ? adj_ptr[a] : k;
+    for (int d = 0; d < D; ++d) fixed[(int64_t)a * D + d] = eqmap[(int64_t)a * D + d] < 0;
+  }
+}
+
+// Gather eq-space CSR K, M, C into node blocks; A = M + (dt/2 C + dt^2/4 K) entry by entry
+// (the same expression as the CSR solver); fixed slots get A = 1 on their diagonal.
+template <int D>
+__global__ void k_gather_blocks(Args g, const int* eqmap, const int64_t* rowptr, const int* cols, const double* K,
+                                const double* M, const double* C, double* KB, double* AB, double* MS) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const double h = 0.5 * g.dt, qq = 0.25 * g.dt * g.dt;
+  for (int64_t a = gw; a < g.n_nodes; a += nw) {
+    for (int64_t k = g.adj_ptr[a] + lane; k < g.adj_ptr[a + 1]; k += 32) {
+      const int b = g.adj[k];
+      double m = 0.0;
+      bool have_m = false;
+      for (int c = 0; c < D; ++c)
+        for (int d = 0; d < D; ++d) {
+          const int ea = eqmap[a * D + c], eb = eqmap[(int64_t)b * D + d];
+          double kv = 0.0, mv = 0.0, cv = 0.0;
+          if (ea >= 0 && eb >= 0) {
+            kv = csr_value(rowptr, cols, K, ea, eb);
+            mv = csr_value(rowptr, cols, M, ea, eb);
+            cv = csr_value(rowptr, cols, C, ea, eb);
+            if (c == d && !have_m) {
+              m = mv;
+              have_m = true;
+            }
+          }
+          double av = mv + (h * cv + qq * kv);
+          if (ea < 0 && b == a && c == d) av = 1.0;
+          KB[(int64_t)(c * D + d) * g.nnzb + k] = kv;
+          AB[(int64_t)(c * D + d) * g.nnzb + k] = av;
+        }
+      MS[k] = m;
+    }
+  }
+}
+
+// FSAI row for slot i = (a, c): pattern S = free-or-fixed slots of the lower neighbours
+// b < a (all d) then (a, d <= c); g = L^-T L^-1 e_last / sqrt(.) with A[S,S] = L L^T.
+// One warp per block (the dense pattern matrix takes 32 KB of shared memory).  Rows whose
+// pattern has more than kMaxFsai - 1 slots use a Jacobi row instead (counted).
+template <int D>
+__global__ void __launch_bounds__(32) k_fsai(Args g, float* GB, int* fallback, int jacobi_only) {
+  __shared__ double Am[kMaxFsai * kMaxFsai];
+  __shared__ int sl[kMaxFsai];
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = gw; i < g.n_s; i += nw) {
+    const int64_t a = i / D;
+    const int c = (int)(i - a * D);
+    const int64_t k0 = g.adj_ptr[a], kd = g.diag[a];
+    const int nlow = (int)(kd - k0);
+    const int m = nlow * D + c + 1;
+    const int64_t ga = a * D;
+    if (g.fixed[i] || m > kMaxFsai - 1 || jacobi_only) {
+      // identity row for fixed slots; Jacobi row when the pattern exceeds the capacity
+      if (lane == 0) {
+        const double aii = g.AB[(int64_t)(c * D + c) * g.nnzb + kd];
+        GB[(int64_t)(c * D + c) * g.nnzb + kd] = (float)(g.fixed[i] ? 1.0 : 1.0 / sqrt(aii));
+        if (!g.fixed[i] && !jacobi_only) atomicAdd(fallback, 1);
+      }
+      continue;
+    }
+    for (int p = lane; p < m; p += 32) {
+      if (p < nlow * D) sl[p] = g.adj[k0 + p / D] * D + (p % D);
+      else sl[p] = (int)(ga + (p - nlow * D));
+    }
+    __syncwarp();
+    // lower triangle of A[S,S]
+    for (int e = lane; e < m * m; e += 32) {
+      const int pp = e / m, qq = e - pp * m;
+      if (qq > pp) continue;
+      const int sp = sl[pp], sq = sl[qq];
+      const int bp = sp / D, dp = sp - bp * D, bq = sq / D, dq = sq - bq * D;
+      double v = 0.0;
+      const int64_t kk = (bp == bq) ? g.diag[bp] : find_in(g.adj, g.adj_ptr[bp], g.adj_ptr[bp + 1], bq);
+      if (kk >= 0) v = g.AB[(int64_t)(dp * D + dq) * g.nnzb + kk];
+      Am[pp * kMaxFsai + qq] = v;
+    }
+    __syncwarp();
+    // Cholesky, right-looking, in place (lower)
+    bool ok = true;
+    for (int j = 0; j < m; ++j) {
+      const double djj = Am[j * kMaxFsai + j];
+      if (!(djj > 0.0)) {
+        ok = false;
+        break;
+      }
+      const double ljj = sqrt(djj);
+      __syncwarp();
+      if (lane == 0) Am[j * kMaxFsai + j] = ljj;
+      for (int r = j + 1 + lane; r < m; r += 32) Am[r * kMaxFsai + j] /= ljj;
+      __syncwarp();
+      const int rem = m - j - 1;
+      for (int e = lane; e < rem * rem; e += 32) {
+        const int r = j + 1 + e / rem, q = j + 1 + (e - (e / rem) * rem);
+        if (q <= r) Am[r * kMaxFsai + q] -= Am[r * kMaxFsai + j] * Am[q * kMaxFsai + j];
+      }
+      __syncwarp();
+    }
+    ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+    if (!ok) {
+      if (lane == 0) {
+        const double aii = g.AB[(int64_t)(c * D + c) * g.nnzb + kd];
+        GB[(int64_t)(c * D + c) * g.nnzb + kd] = (float)(1.0 / sqrt(aii > 0 ? aii : 1.0));
+        atomicAdd(fallback, 1);
+      }
+      __syncwarp();
+      continue;
+    }
+    // y = L^-1 e_last = e_last / L_ll ; g = L^-T y, kept in the unused last row of Am
+    // (m <= kMaxFsai - 1)
+    double* gv = Am + (kMaxFsai - 1) * kMaxFsai;
+    // backward substitution g_k = (y_k - sum_{j>k} L_jk g_j) / L_kk
+    const double lll = Am[(m - 1) * kMaxFsai + (m - 1)];
+    if (lane == 0) gv[m - 1] = 1.0 / (lll * lll);
+    __syncwarp();
+    for (int k = m - 2; k >= 0; --k) {
+      double s = 0.0;
+      for (int j = k + 1 + lane; j < m; j += 32) s += Am[j * kMaxFsai + k] * gv[j];
+      s = warp_sum(s);
+      if (lane == 0) gv[k] = -s / Am[k * kMaxFsai + k];
+      __syncwarp();
+    }
+    const double scale = 1.0 / sqrt(gv[m - 1]);
+    for (int p = lane; p < m; p += 32) {
+      const float val = (float)(gv[p] * scale);
+      int64_t kk;
+      int d;
+      if (p < nlow * D) {
+        kk = k0 + p / D;
+        d = p % D;
+      } else {
+        kk = kd;
+        d = p - nlow * D;
+      }
+      GB[(int64_t)(c * D + d) * g.nnzb + kk] = val;
+    }
+    __syncwarp();
+  }
+}
+
+// G^T on the upper part of each node row: GTB(a, b)[c][d] = GB(b, a)[d][c]
+template <int D>
+__global__ void k_transpose_g(Args g, const float* GB, float* GTB) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t a = gw; a < g.n_nodes; a += nw) {
+    for (int64_t k = g.diag[a] + lane; k < g.adj_ptr[a + 1]; k += 32) {
+      const int b = g.adj[k];
+      const int64_t kk = (b == a) ? g.diag[a] : find_in(g.adj, g.adj_ptr[b], g.diag[b], (int)a);
+      for (int c = 0; c < D; ++c)
+        for (int d = 0; d < D; ++d)
+          GTB[(int64_t)(c * D + d) * g.nnzb + k] = kk >= 0 ? GB[(int64_t)(d * D + c) * g.nnzb + kk] : 0.f;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ explicit scheme
+// Central difference with the row-sum lumped mass M_L (no counterpart in the reference, whose
+// mass is always consistent):
+//   a_n = M_L^-1 (f_n - K (u_n + beta v_{n-1/2}) - alpha M_L v_{n-1/2} - Cabs v_{n-1/2})
+//   v_{n+1/2} = v_{n-1/2} + dt a_n ;  u_{n+1} = u_n + dt v_{n+1/2}
+// One thread per node row over the sliced-ELL K; w = u + beta v and v are ping-ponged
+// (neighbours read the previous step's values), u is updated in place (own row only).
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_explicit(Args g, const double* __restrict__ ML,
+                                                       const double* __restrict__ v_in, double* __restrict__ v_out,
+                                                       const double* __restrict__ w_in, double* __restrict__ w_out,
+                                                       const int* __restrict__ rec_map) {
+  const int step = g.s->t + 1;
+  const bool rec_now = g.n_rec > 0 && g.out_interval > 0 && (step % g.out_interval) == 0 &&
+                       step / g.out_interval < g.n_out;
+  const int64_t orow = rec_now ? step / g.out_interval : 0;
+  SELL_ROW_LOOP(g.sf_ptr) {
+    const int64_t sl = row >> 5;
+    const int64_t p0 = g.sf_ptr[sl] + (row & 31), W = (g.sf_ptr[sl + 1] - g.sf_ptr[sl]) >> 5;
+    double s[D][D];
+#pragma unroll
+    for (int c = 0; c < D; ++c)
+#pragma unroll
+      for (int d = 0; d < D; ++d) s[c][d] = 0.0;
+    for (int64_t j = 0; j < W; ++j) {
+      const int64_t pos = p0 + 32 * j;
+      const int64_t bs = (int64_t)__ldcs(g.sf_col + pos) * D;
+      double wa[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) wa[d] = w_in[bs + d];
+#pragma unroll
+      for (int c = 0; c < D; ++c)
+#pragma unroll
+        for (int d = 0; d < D; ++d) s[c][d] = fma(__ldcs(g.KS + (int64_t)(c * D + d) * g.sf_n + pos), wa[d], s[c][d]);
+    }
+    if (row < g.n_nodes) {
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        const int64_t i = row * D + c;
+        if (g.fixed[i]) {
+          v_out[i] = 0.0;
+          w_out[i] = 0.0;
+          continue;
+        }
+        double kw = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) kw += s[c][d];
+        double cab = 0.0;
+        for (int64_t k = g.cab_ptr[i]; k < g.cab_ptr[i + 1]; ++k) cab = fma(g.cab_val[k], v_in[g.cab_col[k]], cab);
+        const double vi = v_in[i], ml = ML[i];
+        const double acc = (g.f[i] - kw - g.alpha_r * ml * vi - cab) / ml;
+        const double vn = fma(g.dt, acc, vi);
+        const double un = fma(g.dt, vn, g.u[i]);
+        v_out[i] = vn;
+        g.u[i] = un;
+        w_out[i] = fma(g.beta_r, vn, un);
+        if (rec_now) {
+          const int rj = rec_map[i];
+          if (rj >= 0) {
+            if (g.out_u) g.out_u[orow * g.n_rec + rj] = un;
+            if (g.out_v) g.out_v[orow * g.n_rec + rj] = vn;
+          }
+        }
+      }
+    }
+  }
+  __shared__ double sh[32];
+  (void)sh;
+  if (last_block(&g.s->ticket)) {
+    if (threadIdx.x == 0) {
+      g.s->ticket = 0;
+      g.s->t += 1;
+    }
+  }
+}
+
+// f holds the entries of step t (= s->t); clear those of t-1
+__global__ void k_force_explicit(Args g) {
+  const int t = g.s->t;
+  if (!g.f_ptr) return;
+  const int t0 = t - 1;
+  if (t0 >= 0 && t0 < g.n_t)
+    for (int64_t k = g.f_ptr[t0] + threadIdx.x; k < g.f_ptr[t0 + 1]; k += blockDim.x) g.f[g.f_slot[k]] = 0.0;
+  __syncthreads();
+  if (t >= 0 && t < g.n_t)
+    for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f[g.f_slot[k]] += g.f_val[k];
+}
+
+// row-sum lumped mass over free columns, and w = u + beta v
+__global__ void k_lumped(Args g, double* ML) {
+  for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < g.n_nodes; a += (int64_t)gridDim.x * blockDim.x) {
+    for (int c = 0; c < g.D; ++c) {
+      double m = 0.0;
+      for (int64_t k = g.adj_ptr[a]; k < g.adj_ptr[a + 1]; ++k)
+        if (!g.fixed[(int64_t)g.adj[k] * g.D + c]) m += g.MS[k];
+      ML[a * g.D + c] = g.fixed[a * g.D + c] ? 1.0 : m;
+    }
+  }
+}
+
+__global__ void k_w_init(Args g, double* w) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x)
+    w[i] = fma(g.beta_r, g.v[i], g.u[i]);
+}
+
+__global__ void k_rec_map(Args g, int* map) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x)
+    map[i] = -1;
+}
+__global__ void k_rec_map_fill(Args g, int* map) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.n_rec; j += (int64_t)gridDim.x * blockDim.x)
+    map[g.rec_slot[j]] = (int)j;
+}
+
+// ------------------------------------------------------------------ sliced-ELL construction
+// kind 0: full row [adj_ptr[a], adj_ptr[a+1]); 1: lower [adj_ptr[a], diag[a]]; 2: upper [diag[a], adj_ptr[a+1])
+__device__ inline void row_range(int kind, const int64_t* adj_ptr, const int64_t* diag, int64_t a, int64_t& b,
+                                 int64_t& e) {
+  if (kind == 0) { b = adj_ptr[a]; e = adj_ptr[a + 1]; }
+  else if (kind == 1) { b = adj_ptr[a]; e = diag[a] + 1; }
+  else { b = diag[a]; e = adj_ptr[a + 1]; }
+}
+
+__global__ void k_sell_width(int kind, int n_nodes, int64_t n_slices, const int64_t* adj_ptr, const int64_t* diag,
+                             int64_t* slen) {
+  for (int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < n_slices;
+       sl += (int64_t)gridDim.x * blockDim.x) {
+    int64_t w = 0;
+    for (int l = 0; l < 32; ++l) {
+      const int64_t a = sl * 32 + l;
+      if (a >= n_nodes) break;
+      int64_t b, e;
+      row_range(kind, adj_ptr, diag, a, b, e);
+      if (e - b > w) w = e - b;
+    }
+    slen[sl] = 32 * w;
+  }
+}
+
+__global__ void k_sell_fill(int kind, int n_nodes, int64_t n_slices, const int64_t* adj_ptr, const int64_t* diag,
+                            const int* adj, const int64_t* sptr, int* col, int64_t* src) {
+  for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < n_slices * 32;
+       a += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t sl = a >> 5, l = a & 31;
+    const int64_t W = (sptr[sl + 1] - sptr[sl]) >> 5;
+    int64_t b = 0, e = 0;
+    if (a < n_nodes) row_range(kind, adj_ptr, diag, a, b, e);
+    for (int64_t j = 0; j < W; ++j) {
+      const int64_t pos = sptr[sl] + 32 * j + l;
+      if (j < e - b) {
+        col[pos] = adj[b + j];
+        src[pos] = b + j;
+      } else {
+        col[pos] = a < n_nodes ? (int)a : 0;
+        src[pos] = -1;
+      }
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_sell_permute(int planes, int64_t n_out, int64_t n_in, const int64_t* src, const T* in, T* out) {
+  for (int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < n_out;
+       pos += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = src[pos];
+    for (int c = 0; c < planes; ++c) out[(int64_t)c * n_out + pos] = k >= 0 ? in[(int64_t)c * n_in + k] : T(0);
+  }
+}
+
+__global__ void k_init_scal(Scal* s, double tol2, int max_it) {
+  s->rz = s->pw = s->rr = s->bb = s->alpha = s->beta = 0.0;
+  s->tol2 = tol2;
+  s->total_iters = 0;
+  s->it = 0;
+  s->max_it = max_it;
+  s->max_seen = 0;
+  s->status = SC_OK;
+  s->t = 0;
+  s->fsai_fallback = 0;
+  s->ticket = 0;
+  s->hist = 0;
+}
+
+__global__ void k_set_t(Scal* s, int t) { s->t = t; }
+
+}  // namespace nb
+}  // namespace sc
+
+using namespace sc;
+using namespace sc::nb;
+
+struct sc_nb_newmark {
+  Args g;
+  void* sell_mem[16] = {};
+  int n_sell_mem = 0;
+  // explicit scheme state (allocated on first use)
+  double *ML = nullptr, *v1 = nullptr, *w0 = nullptr, *w1 = nullptr;
+  int* rec_map = nullptr;
+  cudaGraphExec_t ex_exec[2] = {nullptr, nullptr};
+  cudaGraph_t ex_graph[2] = {nullptr, nullptr};
+  cudaStream_t user = nullptr, cap = nullptr, cap2 = nullptr;
+  unsigned node_blocks = 1, vec_blocks = 1;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+unsigned node_grid(int64_t n_nodes) {
+  // per-step block kernels: one thread per node row, 256 threads per block
+  int64_t b = (n_nodes + 255) / 256;
+  const int64_t cap = 152 * 16;
+  return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+template <int D>
+int build_graph(sc_nb_newmark* h) {
+  cudaGraph_t graph = nullptr;
+  int rc = check(cudaGraphCreate(&graph, 0), "graph create");
+  if (rc) return rc;
+  cudaGraphConditionalHandle hc;
+  if ((rc = check(cudaGraphConditionalHandleCreate(&hc, graph, 1, cudaGraphCondAssignDefault), "handle"))) {
+    cudaGraphDestroy(graph);
+    return rc;
+  }
+  Args g = h->g;
+  cudaStream_t cs = h->cap, c2 = h->cap2;
+  const unsigned nbk = h->node_blocks, vbk = h->vec_blocks;
+  do {
+    if ((rc = check(cudaStreamBeginCaptureToGraph(cs, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+                    "capture")))
+      break;
+    k_force<<<1, 256, 0, cs>>>(g);
+    k_predict<<<vbk, 256, 0, cs>>>(g);
+    k_residual<D><<<nbk, kThreads, 0, cs>>>(g);
+    k_prec_lower<D><<<nbk, kThreads, 0, cs>>>(g);
+    k_prec_upper<D><<<nbk, kThreads, 0, cs>>>(g, 1, hc);
+    cudaStreamCaptureStatus stt;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    if ((rc = check(cudaStreamGetCaptureInfo(cs, &stt, nullptr, nullptr, &deps, nullptr, &ndeps), "capture info")))
+      break;
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = hc;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    if ((rc = check(cudaGraphAddNode(&cnode, graph, deps, nullptr, ndeps, &cp), "add conditional"))) break;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if ((rc = check(cudaStreamUpdateCaptureDependencies(cs, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies),
+                    "update deps")))
+      break;
+    if ((rc = check(cudaStreamBeginCaptureToGraph(c2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+                    "capture body")))
+      break;
+    k_spmv<D, true><<<nbk, kThreads, 0, c2>>>(g, hc);
+    k_update<<<vbk, 256, 0, c2>>>(g, hc);
+    k_prec_lower<D><<<nbk, kThreads, 0, c2>>>(g);
+    k_prec_upper<D><<<nbk, kThreads, 0, c2>>>(g, 0, hc);
+    k_direction<<<vbk, 256, 0, c2>>>(g);
+    cudaGraph_t bo;
+    if ((rc = check(cudaStreamEndCapture(c2, &bo), "end body"))) break;
+    k_finalize<<<vbk, 256, 0, cs>>>(g);
+    k_record<<<vbk, 256, 0, cs>>>(g);
+    k_advance<<<1, 32, 0, cs>>>(g);
+    cudaGraph_t out;
+    if ((rc = check(cudaStreamEndCapture(cs, &out), "end capture"))) break;
+    if ((rc = check(cudaGraphInstantiate(&h->exec, graph, 0), "instantiate"))) break;
+  } while (0);
+  if (rc) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t tmp;
+    if (cudaStreamIsCapturing(cs, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) cudaStreamEndCapture(cs, &tmp);
+    if (cudaStreamIsCapturing(c2, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) cudaStreamEndCapture(c2, &tmp);
+    cudaGetLastError();
+    cudaGraphDestroy(graph);
+    return rc;
+  }
+  h->graph = graph;
+  return SC_OK;
+}
+
+}  // namespace
+static void drop_explicit_graphs(sc_nb_newmark* h);
+namespace {
+
+void drop_graph(sc_nb_newmark* h) {
+  if (h->exec) cudaGraphExecDestroy(h->exec), h->exec = nullptr;
+  if (h->graph) cudaGraphDestroy(h->graph), h->graph = nullptr;
+}
+
+}  // namespace
+
+// Sliced-ELL copies of K, A, M (full pattern), G (lower) and G^T (upper) for the per-step
+// kernels; allocated here (setup) from the stream-ordered pool and freed by sc_nb_destroy.
+static int build_sell(sc_nb_newmark* h, const double* KB, const double* AB, const double* MS, const float* GB,
+                      const float* GTB) {
+  Args& g = h->g;
+  cudaStream_t st = h->user;
+  const int D2 = g.D * g.D;
+  g.n_slices = ((int64_t)g.n_nodes + 31) / 32;
+  int rc = SC_OK;
+  auto alloc = [&](void** p, size_t bytes) {
+    int r = check(cudaMallocAsync(p, bytes > 0 ? bytes : 8, st), "sell malloc");
+    if (!r) h->sell_mem[h->n_sell_mem++] = *p;
+    return r;
+  };
+  int64_t* scan_work = nullptr;
+  int64_t* src = nullptr;
+  const int64_t nsl = g.n_slices;
+  if ((rc = check(cudaMallocAsync((void**)&scan_work, 8 * sc_scan_work_size(nsl), st), "malloc"))) return rc;
+  for (int kind = 0; kind < 3 && !rc; ++kind) {
+    int64_t* ptr = nullptr;
+    if ((rc = alloc((void**)&ptr, 8 * (nsl + 1)))) break;
+    k_sell_width<<<grid_for(nsl, 128), 128, 0, st>>>(kind, g.n_nodes, nsl, g.adj_ptr, g.diag, ptr);
+    if ((rc = sc_exclusive_scan_i64(nsl, ptr, ptr, scan_work, st))) break;
+    int64_t total = 0;
+    if ((rc = check(cudaMemcpyAsync(&total, ptr + nsl, 8, cudaMemcpyDeviceToHost, st), "memcpy"))) break;
+    if ((rc = check(cudaStreamSynchronize(st), "sync"))) break;
+    int* col = nullptr;
+    if ((rc = alloc((void**)&col, 4 * total))) break;
+    if ((rc = check(cudaMallocAsync((void**)&src, 8 * (total > 0 ? total : 1), st), "malloc"))) break;
+    k_sell_fill<<<grid_for(nsl * 32, 128), 128, 0, st>>>(kind, g.n_nodes, nsl, g.adj_ptr, g.diag, g.adj, ptr, col,
+                                                        src);
+    const unsigned pb = grid_for(total, 256, 152 * 32);
+    if (kind == 0) {
+      double *ks = nullptr, *as = nullptr, *ms = nullptr;
+      if ((rc = alloc((void**)&ks, 8 * D2 * total))) break;
+      if ((rc = alloc((void**)&as, 8 * D2 * total))) break;
+      if ((rc = alloc((void**)&ms, 8 * total))) break;
+      k_sell_permute<double><<<pb, 256, 0, st>>>(D2, total, g.nnzb, src, KB, ks);
+      k_sell_permute<double><<<pb, 256, 0, st>>>(D2, total, g.nnzb, src, AB, as);
+      k_sell_permute<double><<<pb, 256, 0, st>>>(1, total, g.nnzb, src, MS, ms);
+      g.sf_ptr = ptr; g.sf_col = col; g.sf_n = total; g.KS = ks; g.AS = as; g.MSS = ms;
+    } else {
+      float* gs = nullptr;
+      if ((rc = alloc((void**)&gs, 4 * D2 * total))) break;
+      k_sell_permute<float><<<pb, 256, 0, st>>>(D2, total, g.nnzb, src, kind == 1 ? GB : GTB, gs);
+      if (kind == 1) { g.sl_ptr = ptr; g.sl_col = col; g.sl_n = total; g.GS = gs; }
+      else { g.su_ptr = ptr; g.su_col = col; g.su_n = total; g.GTS = gs; }
+    }
+    rc = check_launch("sell build");
+    cudaFreeAsync(src, st);
+    src = nullptr;
+  }
+  if (src) cudaFreeAsync(src, st);
+  cudaFreeAsync(scan_work, st);
+  if (!rc) rc = check(cudaStreamSynchronize(st), "sync sell");
+  return rc;
+}
+
+// Workspace layout (bytes, 256-aligned pieces), see sc_nb_workspace_bytes.
+static int64_t align256(int64_t x) { return (x + 255) & ~(int64_t)255; }
+
+extern "C" int64_t sc_nb_workspace_bytes(int n_nodes, int dim, int64_t nnzb) {
+  const int64_t ns = (int64_t)n_nodes * dim, D2 = (int64_t)dim * dim;
+  int64_t b = 0;
+  b += align256(8 * n_nodes);                 // diag
+  b += align256(4 * ns);                      // fixed
+  b += 2 * align256(8 * D2 * nnzb);           // KB, AB
+  b += align256(8 * nnzb);                    // MS
+  b += 2 * align256(4 * D2 * nnzb);           // GB, GTB
+  b += 13 * align256(8 * ns);                 // a1 a2 q1 q2 y1 x0 x r z p w f (+1 spare)
+  b += align256(4 * ns);                      // t32
+  b += align256(8 * 4 * 152 * 16);            // partials
+  b += align256(sizeof(Scal));
+  return b;
+}
+
+extern "C" int sc_nb_create(sc_nb_newmark** out, int n_nodes, int dim, const int* eqmap, const int64_t* adj_ptr,
+                            const int* adj, int64_t nnzb, const int64_t* rowptr, const int* cols, const double* K,
+                            const double* M, const double* C, int64_t n_cab, const int64_t* cab_ptr,
+                            const int* cab_col, const double* cab_val, double alpha, double beta, double dt,
+                            double rtol, int max_iter, int precond, double* u, double* v, double* a,
+                            void* workspace, int64_t workspace_bytes, void* stream) {
+  if (!out || n_nodes <= 0 || (dim != 2 && dim != 3) || !eqmap || !adj_ptr || !adj || nnzb <= 0 || !rowptr ||
+      !cols || !K || !M || !C || !cab_ptr || !u || !v || !a || !workspace)
+    return SC_BAD_ARG;
+  if (n_cab > 0 && (!cab_col || !cab_val)) return SC_BAD_ARG;
+  if (!(dt > 0) || !(rtol > 0) || max_iter <= 0) return SC_BAD_ARG;
+  if (workspace_bytes < sc_nb_workspace_bytes(n_nodes, dim, nnzb)) return SC_BAD_ARG;
+  if (((uintptr_t)workspace & 255) != 0) return SC_BAD_ARG;
+  sc_nb_newmark* h = new sc_nb_newmark();
+  h->user = (cudaStream_t)stream;
+  Args& g = h->g;
+  g = Args{};
+  const int64_t ns = (int64_t)n_nodes * dim, D2 = (int64_t)dim * dim;
+  g.n_nodes = n_nodes;
+  g.D = dim;
+  g.n_s = ns;
+  g.nnzb = nnzb;
+  g.adj_ptr = adj_ptr;
+  g.adj = adj;
+  g.cab_ptr = cab_ptr;
+  g.cab_col = cab_col;
+  g.cab_val = cab_val;
+  g.alpha_r = alpha;
+  g.beta_r = beta;
+  g.aM = 1.0 + alpha * 0.5 * dt;
+  g.aK = beta * 0.5 * dt + 0.25 * dt * dt;
+  g.aC = 0.5 * dt;
+  g.dt = dt;
+  g.u = u;
+  g.v = v;
+  g.a = a;
+  char* p = (char*)workspace;
+  auto take = [&](int64_t bytes) {
+    char* q = p;
+    p += align256(bytes);
+    return (void*)q;
+  };
+  int64_t* diag = (int64_t*)take(8 * n_nodes);
+  int* fixed = (int*)take(4 * ns);
+  double* KB = (double*)take(8 * D2 * nnzb);
+  double* AB = (double*)take(8 * D2 * nnzb);
+  double* MS = (double*)take(8 * nnzb);
+  float* GB = (float*)take(4 * D2 * nnzb);
+  float* GTB = (float*)take(4 * D2 * nnzb);
+  g.diag = diag;
+  g.fixed = fixed;
+  g.KB = KB;
+  g.AB = AB;
+  g.MS = MS;
+  g.GB = GB;
+  g.GTB = GTB;
+  g.a1 = (double*)take(8 * ns);
+  g.a2 = (double*)take(8 * ns);
+  g.q1 = (double*)take(8 * ns);
+  g.q2 = (double*)take(8 * ns);
+  g.y1 = (double*)take(8 * ns);
+  g.x0 = (double*)take(8 * ns);
+  g.x = (double*)take(8 * ns);
+  g.r = (double*)take(8 * ns);
+  g.z = (double*)take(8 * ns);
+  g.p = (double*)take(8 * ns);
+  g.w = (double*)take(8 * ns);
+  g.f = (double*)take(8 * ns);
+  take(8 * ns);
+  g.t32 = (float*)take(4 * ns);
+  g.part = (double*)take(8 * 4 * 152 * 16);
+  g.s = (Scal*)take(sizeof(Scal));
+  h->node_blocks = node_grid(n_nodes);
+  h->vec_blocks = grid_for(ns, 256, 152 * 16);
+  cudaStream_t st = h->user;
+  int rc = SC_OK;
+  int* dflag = nullptr;
+  do {
+    if ((rc = check(cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking), "stream"))) break;
+    if ((rc = check(cudaStreamCreateWithFlags(&h->cap2, cudaStreamNonBlocking), "stream"))) break;
+    if ((rc = check(cudaMallocAsync((void**)&dflag, 2 * sizeof(int), st), "malloc"))) break;
+    cudaMemsetAsync(dflag, 0, 2 * sizeof(int), st);
+    cudaMemsetAsync(g.f, 0, 8 * ns, st);
+    cudaMemsetAsync(g.a1, 0, 8 * ns, st);
+    cudaMemsetAsync(g.a2, 0, 8 * ns, st);
+    cudaMemsetAsync(GB, 0, 4 * D2 * nnzb, st);
+    k_setup_nodes<<<grid_for(n_nodes, 128), 128, 0, st>>>(n_nodes, dim, eqmap, adj_ptr, adj, diag, fixed, dflag);
+    if (dim == 3)
+      k_gather_blocks<3><<<h->node_blocks, kThreads, 0, st>>>(g, eqmap, rowptr, cols, K, M, C, KB, AB, MS);
+    else
+      k_gather_blocks<2><<<h->node_blocks, kThreads, 0, st>>>(g, eqmap, rowptr, cols, K, M, C, KB, AB, MS);
+    const unsigned fb = grid_for(ns, 1, 152 * 64);
+    if (dim == 3) {
+      k_fsai<3><<<fb, 32, 0, st>>>(g, GB, dflag + 1, precond == 1);
+      k_transpose_g<3><<<h->node_blocks, kThreads, 0, st>>>(g, GB, GTB);
+    } else {
+      k_fsai<2><<<fb, 32, 0, st>>>(g, GB, dflag + 1, precond == 1);
+      k_transpose_g<2><<<h->node_blocks, kThreads, 0, st>>>(g, GB, GTB);
+    }
+    k_init_scal<<<1, 1, 0, st>>>(g.s, rtol * rtol, max_iter);
+    if ((rc = check_launch("nb setup"))) break;
+    if ((rc = build_sell(h, KB, AB, MS, GB, GTB))) break;
+    int hf[2] = {0, 0};
+    if ((rc = check(cudaMemcpyAsync(hf, dflag, 2 * sizeof(int), cudaMemcpyDeviceToHost, st), "memcpy"))) break;
+    if ((rc = check(cudaStreamSynchronize(st), "sync"))) break;
+    if (hf[0]) rc = SC_BAD_ARG;  // a node missing from its own adjacency row
+    int fallback = hf[1];
+    cudaMemcpy(&g.s->fsai_fallback, &fallback, sizeof(int), cudaMemcpyHostToDevice);
+  } while (0);
+  if (dflag) {
+    cudaFreeAsync(dflag, st);
+    cudaStreamSynchronize(st);
+  }
+  if (rc) {
+    cudaStreamSynchronize(st);
+    for (int i = 0; i < h->n_sell_mem; ++i) cudaFree(h->sell_mem[i]);
+    if (h->cap) cudaStreamDestroy(h->cap);
+    if (h->cap2) cudaStreamDestroy(h->cap2);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return SC_OK;
+}
+
+extern "C" int sc_nb_set_force(sc_nb_newmark* h, int n_t, const int64_t* f_ptr, const int* f_slot,
+                               const double* f_val) {
+  if (!h || n_t < 0 || (n_t > 0 && (!f_ptr || !f_slot || !f_val))) return SC_BAD_ARG;
+  h->g.n_t = n_t;
+  h->g.f_ptr = n_t > 0 ? f_ptr : nullptr;
+  h->g.f_slot = f_slot;
+  h->g.f_val = f_val;
+  drop_graph(h);
+  drop_explicit_graphs(h);
+  // dense f holds the entries of the current step
+  cudaMemsetAsync(h->g.f, 0, 8 * h->g.n_s, h->user);
+  return SC_OK;
+}
+
+extern "C" int sc_nb_set_output(sc_nb_newmark* h, int out_interval, int n_rec, const int* rec_slot, double* out_u,
+                                double* out_v, double* out_a, int64_t n_out) {
+  if (!h || n_rec < 0 || (n_rec > 0 && (!rec_slot || out_interval <= 0 || n_out <= 0))) return SC_BAD_ARG;
+  h->g.out_interval = out_interval;
+  h->g.n_rec = n_rec;
+  h->g.rec_slot = rec_slot;
+  h->g.out_u = out_u;
+  h->g.out_v = out_v;
+  h->g.out_a = out_a;
+  h->g.n_out = n_out;
+  drop_graph(h);
+  drop_explicit_graphs(h);
+  return SC_OK;
+}
+
+// t_begin: state index of u/v/a on entry (the force entries of step t_begin are assumed in f
+// when t_begin > 0; at t_begin == 0 they are written here).  The warm start uses the
+// acceleration history (a1, a2) once steps of this solver have filled it.
+extern "C" int sc_nb_run(sc_nb_newmark* h, int t_begin, int t_end) {
+  if (!h || t_begin < 0 || t_end < t_begin) return SC_BAD_ARG;
+  int rc;
+  if (!h->exec) {
+    rc = h->g.D == 3 ? build_graph<3>(h) : build_graph<2>(h);
+    if (rc) return rc;
+  }
+  cudaStream_t st = h->user;
+  if (t_begin == 0 && h->g.f_ptr) {
+    k_set_t<<<1, 1, 0, st>>>(h->g.s, -1);
+    k_force<<<1, 256, 0, st>>>(h->g);  // step 0 entries
+  }
+  k_set_t<<<1, 1, 0, st>>>(h->g.s, t_begin);
+  if ((rc = check_launch("nb run"))) return rc;
+  for (int t = t_begin; t < t_end; ++t)
+    if ((rc = check(cudaGraphLaunch(h->exec, st), "graph launch"))) return rc;
+  return SC_OK;
+}
+
+static void drop_explicit_graphs(sc_nb_newmark* h) {
+  for (int k = 0; k < 2; ++k) {
+    if (h->ex_exec[k]) cudaGraphExecDestroy(h->ex_exec[k]), h->ex_exec[k] = nullptr;
+    if (h->ex_graph[k]) cudaGraphDestroy(h->ex_graph[k]), h->ex_graph[k] = nullptr;
+  }
+}
+
+template <int D>
+static int build_explicit_graph(sc_nb_newmark* h, int k) {
+  Args g = h->g;
+  const double* vin = k == 0 ? g.v : h->v1;
+  double* vout = k == 0 ? h->v1 : g.v;
+  const double* win = k == 0 ? h->w0 : h->w1;
+  double* wout = k == 0 ? h->w1 : h->w0;
+  cudaStream_t cs = h->cap;
+  int rc = check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "capture explicit");
+  if (rc) return rc;
+  k_explicit<D><<<h->node_blocks, kThreads, 0, cs>>>(g, h->ML, vin, vout, win, wout, h->rec_map);
+  k_force_explicit<<<1, 256, 0, cs>>>(g);
+  cudaGraph_t graph;
+  if ((rc = check(cudaStreamEndCapture(cs, &graph), "end explicit"))) return rc;
+  if ((rc = check(cudaGraphInstantiate(&h->ex_exec[k], graph, 0), "instantiate explicit"))) {
+    cudaGraphDestroy(graph);
+    return rc;
+  }
+  h->ex_graph[k] = graph;
+  return SC_OK;
+}
+
+// Explicit central-difference steps t_begin .. t_end-1 on the same handle (u, v are the
+// handle's state vectors; a is not used).  At t_begin == 0 the force entries of step 0 are
+// written; the run always ends with the state in the caller's u and v.
+extern "C" int sc_nb_explicit_run(sc_nb_newmark* h, int t_begin, int t_end) {
+  if (!h || t_begin < 0 || t_end < t_begin) return SC_BAD_ARG;
+  Args& g = h->g;
+  cudaStream_t st = h->user;
+  int rc;
+  if (!h->ML) {
+    const int64_t ns = g.n_s;
+    if ((rc = check(cudaMallocAsync((void**)&h->ML, 8 * ns, st), "malloc"))) return rc;
+    if ((rc = check(cudaMallocAsync((void**)&h->v1, 8 * ns, st), "malloc"))) return rc;
+    if ((rc = check(cudaMallocAsync((void**)&h->w0, 8 * ns, st), "malloc"))) return rc;
+    if ((rc = check(cudaMallocAsync((void**)&h->w1, 8 * ns, st), "malloc"))) return rc;
+    if ((rc = check(cudaMallocAsync((void**)&h->rec_map, 4 * ns, st), "malloc"))) return rc;
+    k_lumped<<<grid_for(g.n_nodes, 256), 256, 0, st>>>(g, h->ML);
+  }
+  if (!h->ex_exec[0]) {
+    k_rec_map<<<grid_for(g.n_s, 256), 256, 0, st>>>(g, h->rec_map);
+    if (g.n_rec > 0) k_rec_map_fill<<<grid_for(g.n_rec, 256), 256, 0, st>>>(g, h->rec_map);
+    for (int k = 0; k < 2; ++k) {
+      rc = g.D == 3 ? build_explicit_graph<3>(h, k) : build_explicit_graph<2>(h, k);
+      if (rc) return rc;
+    }
+  }
+  k_w_init<<<h->vec_blocks, 256, 0, st>>>(g, h->w0);
+  if (t_begin == 0 && g.f_ptr) {
+    cudaMemsetAsync(g.f, 0, 8 * g.n_s, st);
+    k_set_t<<<1, 1, 0, st>>>(g.s, 0);
+    k_force_explicit<<<1, 256, 0, st>>>(g);  // step 0 entries
+  }
+  k_set_t<<<1, 1, 0, st>>>(g.s, t_begin);
+  if ((rc = check_launch("explicit prepare"))) return rc;
+  int k = 0;
+  for (int t = t_begin; t < t_end; ++t, k ^= 1)
+    if ((rc = check(cudaGraphLaunch(h->ex_exec[k], st), "explicit launch"))) return rc;
+  if (k == 1) {  // state is in v1 / w1: bring v back to the caller's buffer
+    if ((rc = check(cudaMemcpyAsync(g.v, h->v1, 8 * g.n_s, cudaMemcpyDeviceToDevice, st), "copy v"))) return rc;
+  }
+  return SC_OK;
+}
+
+extern "C" int sc_nb_time_explicit(sc_nb_newmark* h, int reps, float* ms_per_step) {
+  if (!h || reps <= 0 || !ms_per_step || !h->ex_exec[0]) return SC_BAD_ARG;
+  cudaStream_t st = h->user;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int t = 0;
+  (void)t;
+  cudaEventRecord(e0, st);
+  for (int i = 0; i < reps; ++i)
+    if (h->g.D == 3)
+      k_explicit<3><<<h->node_blocks, kThreads, 0, st>>>(h->g, h->ML, h->g.v, h->v1, h->w0, h->w1, h->rec_map);
+    else
+      k_explicit<2><<<h->node_blocks, kThreads, 0, st>>>(h->g, h->ML, h->g.v, h->v1, h->w0, h->w1, h->rec_map);
+  cudaEventRecord(e1, st);
+  int rc = check_launch("explicit timing");
+  if (!rc) rc = check(cudaEventSynchronize(e1), "sync");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  *ms_per_step = ms / reps;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+extern "C" int sc_nb_status(sc_nb_newmark* h, int64_t* total_iters, int* max_iters, int* fsai_fallback_rows) {
+  if (!h) return SC_BAD_ARG;
+  int rc = check(cudaStreamSynchronize(h->user), "sync");
+  if (rc) return rc;
+  Scal s;
+  if ((rc = check(cudaMemcpy(&s, h->g.s, sizeof(s), cudaMemcpyDeviceToHost), "read"))) return rc;
+  if (total_iters) *total_iters = s.total_iters;
+  if (max_iters) *max_iters = s.max_seen;
+  if (fsai_fallback_rows) *fsai_fallback_rows = s.fsai_fallback;
+  return s.status;
+}
+
+extern "C" int sc_nb_time_spmv(sc_nb_newmark* h, int reps, float* ms_per_launch, int64_t* bytes_per_launch) {
+  if (!h || reps <= 0 || !ms_per_launch) return SC_BAD_ARG;
+  cudaStream_t st = h->user;
+  cudaEvent_t e0, e1;
+  int rc = check(cudaEventCreate(&e0), "event");
+  if (rc) return rc;
+  if ((rc = check(cudaEventCreate(&e1), "event"))) {
+    cudaEventDestroy(e0);
+    return rc;
+  }
+  cudaGraphConditionalHandle none = 0;
+  const unsigned nbk = h->node_blocks;
+  auto launch = [&]() {
+    if (h->g.D == 3) k_spmv<3, false><<<nbk, kThreads, 0, st>>>(h->g, none);
+    else k_spmv<2, false><<<nbk, kThreads, 0, st>>>(h->g, none);
+  };
+  launch();
+  cudaEventRecord(e0, st);
+  for (int i = 0; i < reps; ++i) launch();
+  cudaEventRecord(e1, st);
+  rc = check_launch("nb spmv timing");
+  if (!rc) rc = check(cudaEventSynchronize(e1), "event sync");
+  float ms = 0.f;
+  if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+  *ms_per_launch = ms / reps;
+  if (bytes_per_launch) {
+    const int64_t D2 = (int64_t)h->g.D * h->g.D;
+    // A blocks + block columns + row pointers + one read of p + the write of w
+    *bytes_per_launch = h->g.nnzb * (8 * D2 + 4) + (int64_t)(h->g.n_slices + 1) * 8 + h->g.n_s * 16;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+extern "C" int sc_nb_destroy(sc_nb_newmark* h) {
+  if (!h) return SC_OK;
+  drop_graph(h);
+  drop_explicit_graphs(h);
+  for (int i = 0; i < h->n_sell_mem; ++i) cudaFree(h->sell_mem[i]);
+  if (h->ML) cudaFree(h->ML);
+  if (h->v1) cudaFree(h->v1);
+  if (h->w0) cudaFree(h->w0);
+  if (h->w1) cudaFree(h->w1);
+  if (h->rec_map) cudaFree(h->rec_map);
+  if (h->cap) cudaStreamDestroy(h->cap);
+  if (h->cap2) cudaStreamDestroy(h->cap2);
+  delete h;
+  return SC_OK;
+}

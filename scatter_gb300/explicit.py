@@ -1,0 +1,84 @@
+"""Explicit central-difference scheme with lumped mass on the GPU (no reference counterpart).
+
+The reference's time integrators (PuggleSolvers, scatter/scatter.py:120-131) use the
+consistent mass (scatter/discretisation.py:203-222).  This scheme is the added fast path:
+
+    M_L = row sums of M;  C = Cabs + alpha M_L + beta K
+    a_n = M_L^-1 (f_n - K (u_n + beta v_{n-1/2}) - alpha M_L v_{n-1/2} - Cabs v_{n-1/2})
+    v_{n+1/2} = v_{n-1/2} + dt a_n,   u_{n+1} = u_n + dt v_{n+1/2}
+
+one fused kernel per step (``sc_nb_explicit_run``).  ``ExplicitLumped`` has the solver duck
+type of ``NewmarkExplicit``; the velocity reported at step n+1 is v_{n+1/2}.
+"""
+import numpy as np
+import torch
+
+from . import device as dv
+from .solvers import ForceTable, NodeBlockNewmark
+from .system_matrix import GenerateMatrix
+
+
+def critical_time_step(g: GenerateMatrix):
+    """2 / omega_max with omega_max^2 bounded by Gershgorin on M_L^-1 K (a lower bound on the
+    true CFL limit of the lumped scheme)."""
+    rp = g.pattern.rowptr
+    counts = (rp[1:] - rp[:-1]).long()
+    rows = torch.repeat_interleave(torch.arange(g.n_eq, device=rp.device), counts)
+    ml = torch.zeros(g.n_eq, dtype=torch.float64, device=rp.device).index_add_(0, rows, g.M_d)
+    ka = torch.zeros(g.n_eq, dtype=torch.float64, device=rp.device).index_add_(0, rows, g.K_d.abs())
+    bound = float((ka / ml).max().item())
+    if float(ml.min().item()) <= 0:
+        raise ValueError("lumped mass has non-positive entries (row-sum lumping of this element type)")
+    return 2.0 / np.sqrt(bound)
+
+
+class ExplicitLumped:
+    def __init__(self, check_cfl=True):
+        self.output_interval = 1
+        self.update_rhs_at_time_step_func = None
+        self.force_table = None
+        self.receivers = None
+        self.check_cfl = check_cfl
+
+    def initialise(self, number_equations, time):
+        self.number_equations = int(number_equations)
+        self.time = np.asarray(time, dtype=float)
+        n_out = len(range(0, len(self.time), self.output_interval))
+        self.output_time = self.time[::self.output_interval][:n_out]
+        self.u = np.zeros((n_out, self.number_equations))
+        self.v = np.zeros_like(self.u)
+        self.a = np.zeros_like(self.u)
+
+    def update(self, t_idx):
+        self.t_idx = t_idx
+
+    def calculate(self, M, C, K, F, t_start_idx, t_end_idx):
+        if not isinstance(M, GenerateMatrix):
+            raise TypeError("the explicit GPU scheme takes the GenerateMatrix that assembled M, C, K")
+        g = M
+        dt = self.time[1] - self.time[0]
+        if self.check_cfl:
+            dtc = critical_time_step(g)
+            if dt > dtc:
+                raise ValueError(f"explicit scheme unstable: dt {dt:.3e} > critical {dtc:.3e}")
+        n_t = len(self.time)
+        table = self.force_table
+        if table is None:
+            func = self.update_rhs_at_time_step_func or (lambda t: F)
+            table = ForceTable.from_callback(func, n_t, g.n_eq)
+        s = NodeBlockNewmark(g, dt)
+        s.set_force(table)
+        rec = np.arange(g.n_eq) if self.receivers is None else np.asarray(self.receivers)
+        n_out = len(range(0, n_t, self.output_interval))
+        s.set_output(self.output_interval, rec, n_out, what=("u", "v"))
+        for k in ("u", "v"):
+            s.out[k][:s.n_rec] = {"u": s.u, "v": s.v}[k][s.rec.long()]
+        s.run_explicit(t_start_idx, t_end_idx)
+        torch.cuda.synchronize()
+        out = s.outputs()
+        if self.receivers is None:
+            self.u, self.v = out["u"], out["v"]
+        else:
+            self.u_rec, self.v_rec = out["u"], out["v"]
+        self.solver_handle = s
+        s.close()

@@ -147,11 +147,154 @@ class NewmarkGPU:
             pass
 
 
+class NodeBlockNewmark:
+    """Node-block time loop for matrices assembled by GenerateMatrix (sc_nb_* C-ABI).
+
+    State in slot space (slot = node * dim + dof); the eq <-> slot maps translate force
+    entries, receivers and outputs from/to the reference's equation numbering."""
+
+    def __init__(self, g, dt, rtol=1e-12, max_iter=1000, precond="fsai"):
+        if g.adj_ptr is None:
+            raise ValueError("GenerateMatrix has no node structure")
+        self.g = g
+        D, N = g.dim, g.n_nodes
+        self.D, self.N = D, N
+        self.n_s = D * N
+        eqmap = g.eqmap_d.view(-1).long()
+        free = eqmap >= 0
+        slots = torch.arange(self.n_s, device=eqmap.device)
+        self.eq2slot = torch.full((g.n_eq,), -1, dtype=torch.int64, device=eqmap.device)
+        self.eq2slot[eqmap[free]] = slots[free]
+        # Lysmer dashpots as a slot-space CSR
+        if g.Cabs_d is not None:
+            nz = torch.nonzero(g.Cabs_d).view(-1)
+            rp = g.pattern.rowptr
+            rows_eq = torch.searchsorted(rp, nz, right=True) - 1
+            cols_eq = g.pattern.cols[nz].long()
+            rs, cs, vs = self.eq2slot[rows_eq], self.eq2slot[cols_eq], g.Cabs_d[nz]
+            key = rs * self.n_s + cs
+            o = torch.argsort(key)
+            rs, cs, vs = rs[o], cs[o], vs[o]
+            cnt = torch.bincount(rs, minlength=self.n_s)
+        else:
+            cs = torch.zeros(0, dtype=torch.int64, device=eqmap.device)
+            vs = torch.zeros(0, dtype=torch.float64, device=eqmap.device)
+            cnt = torch.zeros(self.n_s, dtype=torch.int64, device=eqmap.device)
+        self.cab_ptr = torch.zeros(self.n_s + 1, dtype=torch.int64, device=eqmap.device)
+        self.cab_ptr[1:] = torch.cumsum(cnt, 0)
+        self.cab_col = cs.to(torch.int32).contiguous()
+        self.cab_val = vs.to(torch.float64).contiguous()
+        if self.cab_col.numel() == 0:
+            self.cab_col = torch.zeros(1, dtype=torch.int32, device=eqmap.device)
+            self.cab_val = torch.zeros(1, dtype=torch.float64, device=eqmap.device)
+        self.u = dv.zeros(self.n_s, torch.float64)
+        self.v = dv.zeros(self.n_s, torch.float64)
+        self.a = dv.zeros(self.n_s, torch.float64)
+        nnzb = int(g.adj.numel())
+        wsb = nat.value("sc_nb_workspace_bytes", N, D, nnzb)
+        self.ws = dv.empty(wsb, torch.uint8)
+        h = ctypes.c_void_p()
+        nat.call("sc_nb_create", ctypes.byref(h), N, D, g.eqmap_d.data_ptr(), g.adj_ptr.data_ptr(), g.adj.data_ptr(),
+                 nnzb, g.pattern.rowptr.data_ptr(), g.pattern.cols.data_ptr(), g.K_d.data_ptr(), g.M_d.data_ptr(),
+                 g.C_d.data_ptr(), int(cnt.sum().item()), self.cab_ptr.data_ptr(), self.cab_col.data_ptr(),
+                 self.cab_val.data_ptr(), float(g.alpha), float(g.beta), float(dt), float(rtol), int(max_iter),
+                 {"fsai": 0, "jacobi": 1}[precond], self.u.data_ptr(), self.v.data_ptr(), self.a.data_ptr(), self.ws.data_ptr(), wsb, dv.stream_ptr())
+        self.h = h
+        self.dt = dt
+
+    def set_force(self, table: ForceTable):
+        eq = dv.to_dev(table.f_eq, torch.int64)
+        slot = self.eq2slot[eq].to(torch.int32) if eq.numel() else eq.to(torch.int32)
+        if eq.numel() and bool((slot < 0).any()):
+            raise ValueError("force on a fixed DOF")
+        self._keep_force = [dv.to_dev(table.f_ptr, torch.int64), slot.contiguous(), dv.to_dev(table.f_val,
+                                                                                              torch.float64)]
+        if self._keep_force[1].numel() == 0:
+            self._keep_force[1] = torch.zeros(1, dtype=torch.int32, device=slot.device)
+            self._keep_force[2] = torch.zeros(1, dtype=torch.float64, device=slot.device)
+        p, e, v = self._keep_force
+        self.table = table
+        nat.call("sc_nb_set_force", self.h, table.n_t, p.data_ptr(), e.data_ptr(), v.data_ptr())
+
+    def set_output(self, interval, rec_eq, n_out, what=("u", "v", "a")):
+        rec = self.eq2slot[dv.to_dev(np.asarray(rec_eq, dtype=np.int64), torch.int64)].to(torch.int32).contiguous()
+        self.rec = rec
+        nr = rec.numel()
+        self.out = {k: (dv.zeros(n_out * nr, torch.float64) if k in what else None) for k in ("u", "v", "a")}
+        nat.call("sc_nb_set_output", self.h, int(interval), nr, rec.data_ptr(),
+                 *(dv.ptr(self.out[k]) for k in ("u", "v", "a")), int(n_out))
+        self.n_out, self.n_rec = int(n_out), nr
+
+    def initial_acceleration(self):
+        """a0 = M^-1 (f(0) - C v0 - K u0); zero for a start from rest without load at t = 0
+        (pulse, heaviside, moving loads all start at 0), else solved with the CSR path."""
+        t = self.table
+        if t.f_ptr[1] > t.f_ptr[0] and np.any(t.f_val[t.f_ptr[0]:t.f_ptr[1]] != 0):
+            g = self.g
+            csr = NewmarkGPU(g.pattern, g.M_d, g.C_d, g.K_d, self.dt)
+            csr.set_force(t)
+            csr.initial_acceleration()
+            a_eq = csr.a
+            free = self.eq2slot >= 0
+            self.a[self.eq2slot[free]] = a_eq[free]
+            csr.close()
+        # step-0 output row
+        for k, buf in self.out.items():
+            if buf is not None:
+                src = {"u": self.u, "v": self.v, "a": self.a}[k]
+                buf[:self.n_rec] = src[self.rec.long()]
+
+    def run(self, t_begin, t_end):
+        nat.call("sc_nb_run", self.h, int(t_begin), int(t_end))
+
+    def status(self):
+        tot = ctypes.c_int64()
+        mx = ctypes.c_int()
+        fb = ctypes.c_int()
+        rc = nat.value("sc_nb_status", self.h, ctypes.byref(tot), ctypes.byref(mx), ctypes.byref(fb))
+        self.fsai_fallback_rows = fb.value
+        return rc, tot.value, mx.value
+
+    def time_spmv(self, reps=20):
+        ms = ctypes.c_float()
+        by = ctypes.c_int64()
+        nat.call("sc_nb_time_spmv", self.h, int(reps), ctypes.byref(ms), ctypes.byref(by))
+        return ms.value, by.value
+
+    def run_explicit(self, t_begin, t_end):
+        nat.call("sc_nb_explicit_run", self.h, int(t_begin), int(t_end))
+
+    def time_explicit(self, reps=20):
+        ms = ctypes.c_float()
+        nat.call("sc_nb_time_explicit", self.h, int(reps), ctypes.byref(ms))
+        return ms.value
+
+    def outputs(self):
+        return {k: (None if t is None else dv.host(t).reshape(self.n_out, self.n_rec)) for k, t in self.out.items()}
+
+    def state_eq(self):
+        """u, v, a in the reference's equation numbering (host arrays)."""
+        free = self.eq2slot
+        return tuple(dv.host(x[free]) for x in (self.u, self.v, self.a))
+
+    def close(self):
+        if getattr(self, "h", None):
+            nat.value("sc_nb_destroy", self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class NewmarkExplicit:
     """GPU drop-in for PuggleSolvers' NewmarkExplicit as called by scatter/scatter.py:120-159."""
 
-    def __init__(self, rtol=1e-12, max_iter=1000):
+    def __init__(self, rtol=1e-12, max_iter=1000, layout="node-block"):
         self.output_interval = 1
+        self.layout = layout  # "node-block" (matrices from GenerateMatrix) or "csr"
         self.update_rhs_at_time_step_func = None
         self.rtol = rtol
         self.max_iter = max_iter
@@ -189,16 +332,29 @@ class NewmarkExplicit:
             else:
                 F0 = np.asarray(F, dtype=float)
                 table = ForceTable.from_callback(lambda t: F0, n_t, n)
-        solver = NewmarkGPU(pat, Md, Cd, Kd, dt, self.rtol, self.max_iter)
-        solver.set_force(table)
         rec = np.arange(n) if self.receivers is None else np.asarray(self.receivers)
         n_out = len(range(0, n_t, self.output_interval))
-        solver.set_output(self.output_interval, rec, n_out)
-        solver.initial_acceleration()
-        solver.run(t_start_idx, t_end_idx)
-        rc, tot, mx = solver.status()
+        attempts = ["fsai", "jacobi"] if (isinstance(M, GenerateMatrix) and self.layout == "node-block"
+                                          and M.adj_ptr is not None) else ["csr"]
+        for kind in attempts:
+            if kind == "csr":
+                solver = NewmarkGPU(pat, Md, Cd, Kd, dt, self.rtol, self.max_iter)
+            else:
+                solver = NodeBlockNewmark(M, dt, self.rtol, self.max_iter, precond=kind)
+            solver.set_force(table)
+            solver.set_output(self.output_interval, rec, n_out)
+            solver.initial_acceleration()
+            solver.run(t_start_idx, t_end_idx)
+            rc, tot, mx = solver.status()
+            self.preconditioner = kind
+            # the FP32 approximate inverse can lose positivity on nearly singular effective
+            # matrices (under-integrated quadratic tetrahedra at small dt): redo with Jacobi
+            if rc == 3 and kind == "fsai":
+                solver.close()
+                continue
+            break
         if rc != 0:
-            raise nat.ScatterGpuError("sc_newmark_run", rc, nat.load().sc_status_string(rc).decode(), "")
+            raise nat.ScatterGpuError("time loop", rc, nat.load().sc_status_string(rc).decode(), "")
         out = solver.outputs()
         self.iterations = (tot, mx)
         if self.receivers is None:

@@ -118,6 +118,8 @@ class GenerateMatrix:
         self.alpha = self.beta = 0.0
         self.props = None
         self._cache = {}
+        self.n_nodes = self.dim = None
+        self.adj_ptr = self.adj = self.eqmap_d = None
 
     # -------------------------------------------------------------- element integration + assembly
     def generate_stiffness_and_mass(self, data, material: dict) -> None:
@@ -149,6 +151,8 @@ class GenerateMatrix:
                  Ke.data_ptr(), Me.data_ptr(), K.data_ptr(), M.data_ptr(), s)
         del Ke, Me
         self.pattern = pat
+        self.n_nodes, self.dim = n_nodes, dim
+        self.adj_ptr, self.adj, self.eqmap_d = adj_ptr, adj[:int(adj_ptr[n_nodes].item())], eqmap_d
         self.K0_d = K
         self.K_d = K
         self.M_d = M
@@ -217,10 +221,12 @@ class GenerateMatrix:
     def damping_Rayleigh(self, damp) -> None:
         """C = C + (alpha M + beta K) on the GPU (system_matrix.py:166-198)."""
         a, b = self.rayleigh_coefficients(damp)
-        self.alpha, self.beta = float(a), float(b)
+        # C = C_abs + (alpha M + beta K): kept as coefficients for the node-block solver
+        self.alpha, self.beta = self.alpha + float(a), self.beta + float(b)
+        a, b = float(a), float(b)
         nnz = self.pattern.nnz
         C = dv.empty(max(nnz, 1), torch.float64)[:nnz]
-        nat.call("sc_combine", nnz, 1.0, self.C_d.data_ptr(), self.alpha, self.M_d.data_ptr(), self.beta,
+        nat.call("sc_combine", nnz, 1.0, self.C_d.data_ptr(), a, self.M_d.data_ptr(), b,
                  self.K_d.data_ptr(), C.data_ptr(), dv.stream_ptr())
         self.C_d = C
         self._cache.clear()

@@ -129,7 +129,7 @@ def test_assembly_is_deterministic(torch_cuda):
         assert torch_cuda.equal(a, b)
 
 
-def _gpu_history(name, rtol=1e-12, receivers=None):
+def _gpu_history(name, rtol=1e-12, receivers=None, layout="node-block"):
     from oracle import loads
     from scatter_gb300.solvers import ForceTable, NewmarkExplicit
 
@@ -137,7 +137,7 @@ def _gpu_history(name, rtol=1e-12, receivers=None):
     load = dict(spec["load"])
     time = loads.time_grid(load["time"], spec["dt"])
     F = loads.table(load, time, model)
-    solver = NewmarkExplicit(rtol=rtol)
+    solver = NewmarkExplicit(rtol=rtol, layout=layout)
     solver.output_interval = 1
     solver.initialise(ns.number_eq, time)
     solver.force_table = ForceTable.from_dense(F)
@@ -147,9 +147,13 @@ def _gpu_history(name, rtol=1e-12, receivers=None):
     return solver, model, spec, time, F
 
 
+LAYOUTS = ["node-block", "csr"]
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
 @pytest.mark.parametrize("name", ["tri3_bench2", "tri6_bench2", "tetra4_bench2", "tetra10_bench2"])
-def test_newmark_vs_benchmark_set_2(torch_cuda, name):
-    solver, model, spec, time, F = _gpu_history(name)
+def test_newmark_vs_benchmark_set_2(torch_cuda, name, layout):
+    solver, model, spec, time, F = _gpu_history(name, layout=layout)
     h = npz(f"hist_{name}.npz")
     idx = np.where(model["nodes"][:, 0].astype(int) == 3)[0][0]
     e = int(model["eq_nb_dof"][idx, 1])
@@ -157,10 +161,11 @@ def test_newmark_vs_benchmark_set_2(torch_cuda, name):
     assert rel_l2(solver.v[:, e], h["vel_y"]) <= 1e-10
 
 
-def test_newmark_vs_oracle_full_history(torch_cuda):
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_newmark_vs_oracle_full_history(torch_cuda, layout):
     from oracle import newmark
 
-    solver, model, spec, time, F = _gpu_history("column_hexa8_abs")
+    solver, model, spec, time, F = _gpu_history("column_hexa8_abs", layout=layout)
     _, _, Mo, Co, Ko, _, _ = oracle_system("column_hexa8_abs")
     U, V, A, _ = newmark.solve(Mo, Co, Ko, F, time, 1)
     assert rel_l2(solver.u, U) <= 1e-10
@@ -168,8 +173,9 @@ def test_newmark_vs_oracle_full_history(torch_cuda):
     assert rel_l2(solver.a, A) <= 1e-9
 
 
-def test_newmark_hexa8_vtk_series(torch_cuda):
-    solver, model, spec, time, F = _gpu_history("column_hexa8_pulse")
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_newmark_hexa8_vtk_series(torch_cuda, layout):
+    solver, model, spec, time, F = _gpu_history("column_hexa8_pulse", layout=layout)
     h = npz("hist_column_hexa8_pulse.npz")
     ids = model["nodes"][:, 0].astype(int)
     sel = [np.where(ids == n)[0][0] for n in h["nodes"]]
@@ -179,8 +185,9 @@ def test_newmark_hexa8_vtk_series(torch_cuda):
     assert rel_l2(Uf[1000], h["dis_all_1000"]) <= 1e-10
 
 
-def test_newmark_quad4_all_nodes(torch_cuda):
-    solver, model, spec, time, F = _gpu_history("quad4_2d")
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_newmark_quad4_all_nodes(torch_cuda, layout):
+    solver, model, spec, time, F = _gpu_history("quad4_2d", layout=layout)
     h = npz("hist_quad4_2d.npz")
     ids = model["nodes"][:, 0].astype(int)
     sel = [np.where(ids == n)[0][0] for n in h["nodes"]]
@@ -226,3 +233,129 @@ def test_newmark_not_converged_status(torch_cuda):
         s.force_table = ForceTable.from_dense(F)
         s.calculate(g, g, g, F[0], 0, len(time) - 1)
     assert ei.value.code == 2
+
+
+@pytest.mark.parametrize("element", ["hexa8", "tetra10"])
+def test_node_block_box_lysmer_moving_load(torch_cuda, element):
+    """Box with Lysmer dashpots on sides and base and a moving point load (the benchmark's
+    physics at small size): node-block GPU loop vs the oracle's direct-solve Newmark."""
+    from oracle import assembly as asm
+    from oracle import elements as el
+    from oracle import lysmer, newmark
+    from scatter_gb300 import meshgen
+    from scatter_gb300.force_external import Force
+    from scatter_gb300.solvers import NewmarkExplicit
+    from scatter_gb300.system_matrix import GenerateMatrix, element_properties
+
+    mats = {"lower": {"density": 2000.0, "Young": 150e6, "poisson": 0.25},
+            "upper": {"density": 1800.0, "Young": 30e6, "poisson": 0.3}}
+    m = meshgen.box_model(6, 4, 4, 0.5, element=element, layers=[(0.0, "lower"), (1.5, "upper")],
+                          bottom="020", x_faces="200", z_faces="002")
+    g = GenerateMatrix(m.number_eq, 2)
+    g.generate_stiffness_and_mass(m, mats)
+    g.absorbing_boundaries(m, mats, [1, 1], 1e3)
+    g.damping_Rayleigh([1, 0.02, 50, 0.02])
+    dt, n_t = 5e-5, 160
+    time = np.linspace(0, dt * (n_t - 1), n_t)
+    if element == "hexa8":
+        load = {"type": "moving_at_plane", "force": [0, -1e5, 0], "speed": 40 / 3.6, "direction": [1, 0],
+                "start_coord": [0.75, -0.75], "time": time[-1], "ini_steps": 5}
+        top = m.get_top_surface()
+    else:
+        load = {"type": "heaviside", "force": [0, -1e4, 0], "node": list(m.top_nodes()[:5]), "time": time[-1],
+                "ini_steps": 5}
+        top = []
+    F = Force()
+    F.initialise_load(load, time, m, None, top_surface_elements=top)
+    s = NewmarkExplicit()
+    s.initialise(m.number_eq, time)
+    s.force_table = F.table
+    s.calculate(g, g, g, F.force_vector, 0, n_t - 1)
+    # oracle: its own element matrices, assembly, Lysmer, Rayleigh and direct-solve Newmark
+    E, nu, rho = element_properties(m, mats)
+    X = m.nodes[:, 1:][m.node_index()[m.elem]]
+    Ke, Me = el.element_matrices(element, X, E, nu, rho)
+    pairs = asm.element_pairs(m.eq_nb_elem)
+    K0 = asm.assemble(m.eq_nb_elem, Ke, m.number_eq, pairs)
+    Mo = asm.assemble(m.eq_nb_elem, Me, m.number_eq, pairs)
+    mdl = {"nodes": m.nodes, "elem": m.elem, "BC": m.BC, "BC_dir": m.BC_dir, "eq_nb_dof": m.eq_nb_dof,
+           "element_type": element, "number_eq": m.number_eq}
+    Ca, Ka = lysmer.absorbing(mdl, (E, nu, rho), [1, 1], 1e3)
+    Ko = asm.drop_zeros(K0 + Ka)
+    Co = asm.rayleigh(Mo, Ko, Ca, [1, 0.02, 50, 0.02])
+    Fd = np.stack([F.table.dense(t) for t in range(n_t)])
+    U, V, A, _ = newmark.solve(Mo, Co, Ko, Fd, time, 1)
+    assert rel_l2(s.u, U) <= 1e-10
+    assert rel_l2(s.v, V) <= 1e-10
+    assert rel_l2(s.a, A) <= 1e-9
+
+
+def test_node_block_and_csr_agree_and_repeat(torch_cuda):
+    """Both device layouts give the same history (to the solve tolerance), and the node-block
+    loop is bitwise reproducible run to run."""
+    a, *_ = _gpu_history("tetra10_bench2", layout="node-block")
+    b, *_ = _gpu_history("tetra10_bench2", layout="node-block")
+    c, *_ = _gpu_history("tetra10_bench2", layout="csr")
+    np.testing.assert_array_equal(a.u, b.u)
+    assert rel_l2(a.u, c.u) <= 1e-10
+
+
+@pytest.mark.parametrize("name", ["column_hexa8_pulse", "cube_abs5"])
+def test_explicit_vs_oracle(torch_cuda, name):
+    """Explicit lumped-mass scheme: GPU fused step vs oracle/explicit.py (FP64)."""
+    from oracle import explicit, loads
+    from scatter_gb300.explicit import ExplicitLumped, critical_time_step
+    from scatter_gb300.solvers import ForceTable
+
+    g, ns, model, spec = _gpu_system(name)
+    dt = 0.5 * critical_time_step(g)
+    n_t = 300
+    time = np.linspace(0, dt * (n_t - 1), n_t)
+    load = dict(spec["load"])
+    load["time"] = time[-1]
+    F = loads.table(load, time, model) if load["type"] != "moving" else None
+    if F is None:
+        pytest.skip("moving load table needs the golden time grid")
+    s = ExplicitLumped()
+    s.initialise(ns.number_eq, time)
+    s.force_table = ForceTable.from_dense(F)
+    s.calculate(g, g, g, F[0], 0, n_t - 1)
+    Cabs = g.pattern.to_scipy(g.Cabs_d) if g.Cabs_d is not None else g.M * 0
+    U, V = explicit.solve(g.M, Cabs, g.K, g.alpha, g.beta, F, n_t, dt)
+    assert rel_l2(s.u, U) <= 1e-10
+    assert rel_l2(s.v, V) <= 1e-10
+
+
+def test_explicit_matches_newmark_at_small_dt(torch_cuda):
+    """Explicit lumped and implicit consistent schemes converge to the same response: at a dt
+    far below the CFL limit their receiver histories agree to the mass-lumping error."""
+    from scatter_gb300 import meshgen
+    from scatter_gb300.explicit import ExplicitLumped
+    from scatter_gb300.force_external import Force
+    from scatter_gb300.solvers import NewmarkExplicit
+    from scatter_gb300.system_matrix import GenerateMatrix
+
+    m = meshgen.column_model(2, 20, 2, 0.5, bottom="111")
+    mats = {"solid": {"density": 2000.0, "Young": 100e6, "poisson": 0.2}}
+    g = GenerateMatrix(m.number_eq, 2)
+    g.generate_stiffness_and_mass(m, mats)
+    g.absorbing_boundaries(m, mats, [1, 1], 1e3)
+    g.damping_Rayleigh([1, 0.02, 50, 0.02])
+    dt, n_t = 1e-4, 2001
+    time = np.linspace(0, dt * (n_t - 1), n_t)
+    load = {"type": "heaviside", "force": [0, -1000 / 9, 0], "node": list(m.top_nodes()), "time": time[-1],
+            "ini_steps": 5}
+    F = Force()
+    F.initialise_load(load, time, m, None)
+    rec = [int(m.eq_nb_dof[m.node_index()[m.top_nodes()[4]], 1])]
+    a = NewmarkExplicit()
+    a.initialise(m.number_eq, time)
+    a.force_table = F.table
+    a.receivers = rec
+    a.calculate(g, g, g, F.force_vector, 0, n_t - 1)
+    b = ExplicitLumped()
+    b.initialise(m.number_eq, time)
+    b.force_table = F.table
+    b.receivers = rec
+    b.calculate(g, g, g, F.force_vector, 0, n_t - 1)
+    assert rel_l2(b.u_rec, a.u_rec) <= 0.25
