@@ -239,6 +239,15 @@ def run_gb300(args):
                                           min(K_steps, len(time_grid) - 1 - (W + K_steps)), n)
     # the added explicit scheme (lumped mass, one fused kernel per step) on the same model
     explicit = explicit_run(g, table, rec_eq, K_steps, W, n)
+    host_csr = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        host_csr = (g.pattern.rowptr.cpu().numpy(), g.pattern.cols.cpu().numpy(),
+                    *(x.cpu().numpy() for x in (g.M_d, g.C_d, g.K_d)))
+    solver.close()
+    nnz = int(g.pattern.nnz)
+    del g
+    batched = None if args.no_batched else batched_run(min(K_steps, 2990), W)
+    adjoint = None if args.no_adjoint else adjoint_run()
 
     out = {"metric": METRIC, "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": K_steps, "warmup": W,
            "ms_per_step": ms / K_steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -246,7 +255,7 @@ def run_gb300(args):
            "config": {"workload": "plain Newmark FP64, box 60x40x30 m hexa8 0.5 m (120x80x60 el), 2 layers, "
                                   "Lysmer sides+base, moving 100 kN at 40 km/h, dt 5e-5" if not args.dims
                       else f"profiling case: box {args.dims} hexa8 0.5 m, same physics",
-                      "n_eq": n, "nnz": g.pattern.nnz, "elements": int(len(model.elem)), "receivers": len(rec_eq),
+                      "n_eq": n, "nnz": nnz, "elements": int(len(model.elem)), "receivers": len(rec_eq),
                       "parallelism": f"replicas x{ws}",
                       "l2": "inputs larger than L2 (CSR values+cols 5.1 GB), no flush",
                       "solver": "Newmark beta=1/4 gamma=1/2; per step PCG (FSAI preconditioner, FP32 factor), "
@@ -259,15 +268,11 @@ def run_gb300(args):
            "roofline": {"bound": "hbm", "kernel": "nb::k_spmv (3x3 node blocks FP64, w = A p)", "achieved": achieved,
                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                         "traffic": traffic, "bytes_per_launch": bytes_spmv, "ms_per_launch": ms_spmv},
-           "clocks": clk.summary(), "e2e": e2e, "explicit_lumped": explicit}
+           "clocks": clk.summary(), "e2e": e2e, "explicit_lumped": explicit, "batched": batched,
+           "adjoint": adjoint}
     # CPU baseline (rank 0 only, N = 1): the oracle's C loop on the host cores
     if rank == 0 and ws == 1 and not args.no_cpu:
-        solver.close()
-        rp = g.pattern.rowptr.cpu().numpy()
-        cl = g.pattern.cols.cpu().numpy()
-        Mh, Ch, Kh = (x.cpu().numpy() for x in (g.M_d, g.C_d, g.K_d))
-        out["cpu_baseline"] = cpu_baseline_run(n, rp, cl, Mh, Ch, Kh, table, rec_eq, target_s=args.cpu_seconds)
-    solver.close()
+        out["cpu_baseline"] = cpu_baseline_run(n, *host_csr, table, rec_eq, target_s=args.cpu_seconds)
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:
@@ -303,6 +308,172 @@ def explicit_run(g, table, rec_eq, k, w, n):
             "dt": DT, "dt_critical_bound": dtc, "kernel_ms": ms_k,
             "kernel_gbs": bytes_step / (ms_k * 1e-3) / 1e9,
             "note": "central difference, row-sum lumped mass (no reference counterpart); FP64"}
+
+
+def _top_receivers(model, n, seed):
+    top = model.top_nodes()
+    rng = np.random.default_rng(seed)
+    nodes = np.sort(rng.choice(top, size=min(n, len(top)), replace=False))
+    return model.eq_nb_dof[model.node_index()[nodes], 1].astype(np.int64)
+
+
+def _top_centre(model):
+    top = model.top_nodes()
+    X = model.nodes[model.node_index()[top], 1:]
+    c = 0.5 * (X.min(axis=0) + X.max(axis=0))
+    return int(top[np.argmin(((X[:, [0, 2]] - c[[0, 2]]) ** 2).sum(axis=1))])
+
+
+def _events():
+    import torch
+
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def batched_run(k, w, R=256):
+    """Batching workload: R = 256 seeded log-normal Young's modulus realisations (mean 50 MPa,
+    CoV 0.25, Gaussian covariance, correlation lengths 5 / 1 / 5 m in x / y (vertical) / z),
+    nu = 0.3, rho = 1900, box 40 x 20 x 10 m hexa8 at 0.5 m (80 x 40 x 20 elements), Lysmer
+    sides and base, Ricker 20 Hz at the top centre; all realisations advanced by one kernel
+    per step, against the plain FP64 explicit GPU path run once for one realisation."""
+    import torch
+
+    from scatter_gb300 import device as dv
+    from scatter_gb300 import meshgen
+    from scatter_gb300.batched import BatchedExplicit
+    from scatter_gb300.force_external import ricker_table
+    from scatter_gb300.random_fields import element_centroids, lognormal_fields
+    from scatter_gb300.solvers import NodeBlockNewmark
+    from scatter_gb300.system_matrix import GenerateMatrix
+
+    m = meshgen.box_model(80, 40, 20, 0.5, bottom="020", x_faces="200", z_faces="002")
+    n_t = 3001
+    if w + k + 1 > n_t:
+        raise SystemExit("batched steps + warmup exceed the 3000-step history")
+    tg = np.arange(n_t) * DT
+    table = ricker_table(m, _top_centre(m), -10e3, 20.0, 0.05, tg)
+    rec_eq = _top_receivers(m, N_REC, 1)
+    nu, rho = 0.3, 1900.0
+    young = lognormal_fields(element_centroids(m), seed=2024, R=R, lengths=(5.0, 1.0, 5.0), mean=50e6, sd=12.5e6)
+    n = int(m.number_eq)
+    b = BatchedExplicit(m, young, nu, rho, SETTINGS["damping"], SETTINGS["absorbing_BC"],
+                        SETTINGS["absorbing_BC_stiff"], DT)
+    b.set_force(table)
+    b.set_output(1, rec_eq, n_t)
+    b.run(0, w)
+    torch.cuda.synchronize()
+    e0, e1 = _events()
+    e0.record()
+    b.run(w, w + k)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_b = e0.elapsed_time(e1)
+    vb = b.velocities()[: w + k + 1, :, 0]
+    y0 = dv.host(young[:, 0]).astype(float)
+    b.close()
+    del b
+    n_el = len(m.elem)
+    g = GenerateMatrix(n, SETTINGS["int_order"])
+    g.generate_stiffness_and_mass(m, None, element_props=(y0, np.full(n_el, nu), np.full(n_el, rho)))
+    g.absorbing_boundaries(m, None, SETTINGS["absorbing_BC"], SETTINGS["absorbing_BC_stiff"])
+    g.damping_Rayleigh(SETTINGS["damping"])
+    s = NodeBlockNewmark(g, DT, precond="jacobi")
+    s.set_force(table)
+    s.set_output(1, rec_eq, n_t, what=("v",))
+    s.run_explicit(0, w)
+    torch.cuda.synchronize()
+    e0, e1 = _events()
+    e0.record()
+    s.run_explicit(w, w + k)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_s = e0.elapsed_time(e1)
+    vs = dv.host(s.out["v"]).reshape(n_t, len(rec_eq))[: w + k + 1]
+    s.close()
+    rel = float(np.linalg.norm(vb - vs) / max(np.linalg.norm(vs), 1e-300))
+    vb_rate = n * R * k / (ms_b / 1e3)
+    single = n * k / (ms_s / 1e3)
+    return {"value": vb_rate, "unit": "DOF-steps/s", "single_solve": single, "speedup_vs_single": vb_rate / single,
+            "realisations": R, "n_eq": n, "elements": n_el, "steps": k, "warmup": w, "ms_per_step": ms_b / k,
+            "single_ms_per_step": ms_s / k, "rel_l2_vs_fp64_realisation0": rel,
+            "workload": "256 log-normal E realisations, box 40x20x10 m hexa8 0.5 m, Lysmer, Ricker 20 Hz, dt 5e-5",
+            "single": "plain FP64 explicit GPU path (node-block graph), realisation 0, same steps"}
+
+
+def adjoint_run(n_steps=4000, checkpoint=200, n_fd=20):
+    """Differentiation workload: misfit of vertical surface velocities at 25 receivers w.r.t.
+    per-element E and rho, box 20 x 10 x 20 m (x / y vertical / z) hexa8 at 0.5 m (32,000
+    elements), target from a seeded log-normal E field (CoV 0.3, correlation 3 m), evaluated
+    at a homogeneous 60 MPa guess; 4000 steps, checkpoint every 200.  Reports the cost of one
+    gradient against one forward solve, and central differences (h = 1e-6 relative) on
+    n_fd elements (half E, half rho) drawn from those with the largest gradients."""
+    import torch
+
+    from scatter_gb300 import meshgen
+    from scatter_gb300.adjoint import ExplicitAdjoint
+    from scatter_gb300.force_external import ricker_table
+    from scatter_gb300.random_fields import element_centroids, lognormal_fields
+
+    m = meshgen.box_model(40, 20, 40, 0.5, bottom="020", x_faces="200", z_faces="002")
+    tg = np.arange(n_steps + 1) * DT
+    table = ricker_table(m, _top_centre(m), -10e3, 20.0, 0.05, tg)
+    rec_eq = _top_receivers(m, 25, 5)
+    n_el = len(m.elem)
+    nu, rho = np.full(n_el, 0.3), np.full(n_el, 1900.0)
+    from scatter_gb300 import device as dv
+
+    E_true = dv.host(lognormal_fields(element_centroids(m), seed=77, R=1, lengths=(3.0, 3.0, 3.0), mean=60e6,
+                                      sd=18e6))[:, 0].astype(float)
+    E0 = np.full(n_el, 60e6)
+    A = ExplicitAdjoint(m, nu, SETTINGS["damping"], SETTINGS["absorbing_BC"], SETTINGS["absorbing_BC_stiff"], DT,
+                        n_steps, rec_eq, table, checkpoint=checkpoint)
+    p = A.prepare(E_true, rho)
+    target = p.forward()
+    p.close()
+    p = A.prepare(E0, rho)
+    p.forward()  # builds the explicit graphs
+    s = p.solver
+    torch.cuda.synchronize()
+    e0, e1 = _events()
+    e0.record()
+    s.run_explicit(0, n_steps)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_f = e0.elapsed_time(e1)
+    p.gradient(target)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J, gE, gR = p.gradient(target)
+    ms_a = (time.perf_counter() - t0) * 1e3
+    v0 = p.forward()
+    p.close()
+
+    def misfit(E, r):
+        q = A.prepare(E, r)
+        v = q.forward()
+        q.close()
+        return 0.5 * float(((v[1:] - target[1:]) ** 2).sum())
+
+    rng = np.random.default_rng(11)
+    worst = 0.0
+    checks = []
+    for kind, grad in (("E", gE), ("rho", gR)):
+        top = np.argsort(-np.abs(grad))[: max(n_el // 20, n_fd)]
+        for e in rng.choice(top, size=n_fd // 2, replace=False):
+            base = E0 if kind == "E" else rho
+            h = 1e-6 * base[e]
+            up, dn = base.copy(), base.copy()
+            up[e] += h
+            dn[e] -= h
+            fd = ((misfit(up, rho) - misfit(dn, rho)) if kind == "E" else (misfit(E0, up) - misfit(E0, dn))) / (2 * h)
+            err = abs(fd - grad[e]) / abs(grad[e])
+            worst = max(worst, err)
+            checks.append([kind, int(e), float(grad[e]), float(fd)])
+    return {"adjoint_over_forward": ms_a / ms_f, "forward_ms": ms_f, "gradient_ms": ms_a, "misfit": J,
+            "misfit_check": 0.5 * float(((v0[1:] - target[1:]) ** 2).sum()), "n_eq": int(m.number_eq),
+            "elements": n_el, "steps": n_steps, "checkpoint": checkpoint, "fd_max_rel_err": worst, "fd_checks": len(checks),
+            "timing": "forward: CUDA events around the explicit run; gradient: host wall clock around the whole "
+                      "sc_nb_adjoint call (forward with checkpoints, recompute, backward, graph set-up, copies)"}
 
 
 def e2e_run(solver, table, rec_eq, t0, k, n):
@@ -421,6 +592,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--dims", default="", help="nx,ny,nz of a smaller box (profiling cases)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 256-realisation batched measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost and FD measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")

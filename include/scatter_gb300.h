@@ -162,6 +162,17 @@ int sc_newmark_status(sc_newmark* h, int64_t* total_iters, int* max_iters_per_st
 int sc_newmark_time_spmv(sc_newmark* h, int reps, float* ms_per_launch, int64_t* bytes_per_launch);
 int sc_newmark_destroy(sc_newmark* h);
 
+/* ------------------------------------------------------------------ random fields
+ * Input of the batched path (the reference draws per-element fields with gstools' SRF,
+ * scatter/random_fields.py:59-120, and maps them log-normally, :73-77).  Gaussian covariance
+ * exp(-(pi/4)|r/l|^2) by the randomisation (spectral) method with n_modes modes per
+ * realisation, drawn from a counter-based generator so a field depends only on (seed, r).
+ *   sc_rf_modes:     modes [R][n_modes][5] (k_x, k_y, k_z, Z1, Z2), float32
+ *   sc_rf_lognormal: out [n_pts][R] = exp(mu_ln + sigma_ln g_r(x_p)), xyz [n_pts][3] float32 */
+int sc_rf_modes(uint64_t seed, int R, int n_modes, double lx, double ly, double lz, float* modes, void* stream);
+int sc_rf_lognormal(int n_pts, const float* xyz, int R, int n_modes, const float* modes, double mu_ln,
+                    double sigma_ln, float* out, void* stream);
+
 /* ------------------------------------------------------------------ node-block Newmark
  * The same time loop as sc_newmark_* for matrices assembled by this library from a mesh
  * (node adjacency known), on a node-block layout: unknowns in slot space (slot = node*dim +
@@ -185,6 +196,10 @@ int sc_nb_create(sc_nb_newmark** h, int n_nodes, int dim, const int* eqmap, cons
                  const double* C, int64_t n_cab, const int64_t* cab_ptr, const int* cab_col, const double* cab_val,
                  double alpha, double beta, double dt, double rtol, int max_iter, int precond, double* u, double* v,
                  double* a, void* workspace, int64_t workspace_bytes, void* stream);
+/* options bit 0: run the PCG SpMV in FP64 instead of the default FP32-pair arithmetic
+ * (A as hi + lo FP32 pairs, exact TwoProd/TwoSum accumulation, ~2^-46 relative per product;
+ * the residual, dot products and state stay FP64). */
+int sc_nb_set_options(sc_nb_newmark* h, int options);
 int sc_nb_set_force(sc_nb_newmark* h, int n_t, const int64_t* f_ptr, const int* f_slot, const double* f_val);
 int sc_nb_set_output(sc_nb_newmark* h, int out_interval, int n_rec, const int* rec_slot, double* out_u,
                      double* out_v, double* out_a, int64_t n_out);
@@ -203,7 +218,50 @@ int sc_nb_time_spmv(sc_nb_newmark* h, int reps, float* ms_per_launch, int64_t* b
 int sc_nb_explicit_run(sc_nb_newmark* h, int t_begin, int t_end);
 /* timing aid: the explicit step kernel alone, `reps` launches between CUDA events */
 int sc_nb_time_explicit(sc_nb_newmark* h, int reps, float* ms_per_step);
+/* Adjoint of the explicit scheme (no reference counterpart): misfit
+ *   J = 1/2 sum_{n=1..n_steps} sum_r (v_n[rec_slot[r]] - target[n][r])^2
+ * of the receiver velocities of a run from rest (sc_nb_explicit_run semantics, the handle's
+ * force table), and dJ/dE_e, dJ/drho_e for per-element Young's modulus and density, with
+ *   K = sum_e E_e K1_e + Lysmer springs, M_L = sum_e rho_e ml1_e, Lysmer dashpots ~ sqrt(rho_e E_e)
+ * (the operators the handle was built from must be these at the given young/rho).  Forward
+ * with FP64 checkpoints every `checkpoint` steps, recompute per segment, backward recursion;
+ * one CUDA graph per recompute step and per backward step; gradients accumulated per element
+ * (deterministic).  Descriptor fields:
+ *   elem [n_elem][n_en] node indices; ke_type [n_elem] -> ke1 [types][3 n_en][3 n_en] FP32
+ *   unit-E element stiffness; young, rho [n_elem]; ml1 [n_elem][n_en][3] unit lumped mass
+ *   (free columns); l_eptr [n_elem+1], l_row, l_col (slots), l_c, l_s: the element's Lysmer
+ *   dashpot and spring entries at the current parameters.  3D only.  grad_E, grad_rho [n_elem]
+ *   device outputs; J_host may be NULL.  Allocates its checkpoint buffers (setup). */
+typedef struct sc_adj_desc sc_adj_desc;
+int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* desc, double* J_host, double* grad_E, double* grad_rho);
+/* testing aid: y = Op x in slot space; which = 0: A, 1: K, 2: consistent mass, 3: the
+ * preconditioner G^T G, 4: Lysmer dashpots.  Synchronous; call between steps. */
+int sc_nb_apply(sc_nb_newmark* h, int which, const double* x, double* y);
 int sc_nb_destroy(sc_nb_newmark* h);
+
+/* ------------------------------------------------------------------ batched realisations
+ * R realisations of the per-element Young's modulus (the reference's random-field input,
+ * scatter/random_fields.py:109-118, one material per element) advanced together with the
+ * explicit lumped-mass scheme of sc_nb_explicit_run: K_r = sum_e E_{e,r} K1_e, with K1_e the
+ * element stiffness at E = 1 (sc_element_matrices with young = 1), shared density and Poisson
+ * ratio, and per-realisation Lysmer terms (dashpot coefficients scale with sqrt(E), spring
+ * coefficients with E; scatter/system_matrix.py:362-376).  FP32 stiffness products, FP64
+ * u and v.  All per-realisation arrays are [slot or element][R] (realisation fastest).
+ *   elem [n_elem][n_en] node indices; inc_ptr/inc node -> element incidence (sc_node_incidence)
+ *   ke_type [n_elem] -> ke1 [n_types][3 n_en][3 n_en] float32; young [n_elem][R] float32
+ *   ml [3 n_nodes] lumped mass; fixed [3 n_nodes]; alpha, beta Rayleigh; dt time step
+ *   l_ptr [3 n_nodes + 1], l_col, l_elem, l_c, l_s: Lysmer entries per slot row: column slot,
+ *     element whose E scales it, unit dashpot coefficient (x sqrt(E)), unit spring (x E)
+ *   u, v [3 n_nodes][R] FP64 state.  Setup allocates the ping-pong copies; runs allocate nothing.
+ * R <= 1024; n_en in {4, 8, 10, 20}. */
+typedef struct sc_batch_desc sc_batch_desc;
+typedef struct sc_batch sc_batch;
+int sc_batch_create(sc_batch** h, const sc_batch_desc* desc, double* u, double* v, void* stream);
+int sc_batch_set_force(sc_batch* h, int n_t, const int64_t* f_ptr, const int* f_slot, const double* f_val);
+/* receivers record v [n_out][n_rec][R] every out_interval steps */
+int sc_batch_set_output(sc_batch* h, int out_interval, int n_rec, const int* rec_slot, double* out_v, int64_t n_out);
+int sc_batch_run(sc_batch* h, int t_begin, int t_end);
+int sc_batch_destroy(sc_batch* h);
 
 #ifdef __cplusplus
 }

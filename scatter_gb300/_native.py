@@ -41,9 +41,17 @@ SIGNATURES = {
     "sc_newmark_status": (I, [P, ctypes.POINTER(L), ctypes.POINTER(I)]),
     "sc_newmark_time_spmv": (I, [P, I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(L)]),
     "sc_newmark_destroy": (I, [P]),
+    "sc_rf_modes": (I, [ctypes.c_uint64, I, I, D, D, D, P, P]),
+    "sc_rf_lognormal": (I, [I, P, I, I, P, D, D, P, P]),
+    "sc_batch_create": (I, [ctypes.POINTER(P), P, P, P, P]),
+    "sc_batch_set_force": (I, [P, I, P, P, P]),
+    "sc_batch_set_output": (I, [P, I, I, P, P, L]),
+    "sc_batch_run": (I, [P, I, I]),
+    "sc_batch_destroy": (I, [P]),
     "sc_nb_workspace_bytes": (L, [I, I, L]),
     "sc_nb_create": (I, [ctypes.POINTER(P), I, I, P, P, P, L, P, P, P, P, P, L, P, P, P, D, D, D, D, I, I, P, P, P, P,
                          L, P]),
+    "sc_nb_set_options": (I, [P, I]),
     "sc_nb_set_force": (I, [P, I, P, P, P]),
     "sc_nb_set_output": (I, [P, I, I, P, P, P, P, L]),
     "sc_nb_run": (I, [P, I, I]),
@@ -51,6 +59,8 @@ SIGNATURES = {
     "sc_nb_time_spmv": (I, [P, I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(L)]),
     "sc_nb_explicit_run": (I, [P, I, I]),
     "sc_nb_time_explicit": (I, [P, I, ctypes.POINTER(ctypes.c_float)]),
+    "sc_nb_apply": (I, [P, I, P, P]),
+    "sc_nb_adjoint": (I, [P, P, ctypes.POINTER(D), P, P]),
     "sc_nb_destroy": (I, [P]),
 }
 

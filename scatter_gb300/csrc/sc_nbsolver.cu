@@ -21,6 +21,7 @@
 // per-block partial sums reduced by the last block (ticket, fixed order, no spin-waits);
 // one CUDA graph per step with a device-side WHILE conditional around the PCG body.
 #include <math.h>
+#include <stdlib.h>
 
 #include "sc_common.cuh"
 
@@ -36,7 +37,8 @@ struct Scal {
   int it, max_it, max_seen, status, t, fsai_fallback;
   unsigned int ticket;
   int hist;  // valid previous accelerations (0..2) for the warm start
-  unsigned int pad2[2];
+  int done;  // eager mode: set when the PCG loop should stop
+  unsigned int pad2[1];
 };
 
 struct Args {
@@ -60,6 +62,9 @@ struct Args {
   int64_t sf_n, sl_n, su_n;
   const double *KS, *AS, *MSS;
   const float *GS, *GTS;
+  const float2* APS;       // A as FP32 (hi, lo) pairs (hi + lo = A to 48 bits) for the pair-arithmetic SpMV
+  float2* p2;              // p as (hi, lo) FP32 pairs, written with p
+  int spmv_pair;           // 1: PCG SpMV in FP32-pair arithmetic, 0: FP64
   double alpha_r, beta_r;  // Rayleigh coefficients
   double aM, aK, aC;       // A = aM M + aK K + aC Cabs
   double dt;
@@ -89,6 +94,14 @@ __device__ inline bool last_block(unsigned int* ticket) {
   return am_last;
 }
 
+// kMode 0: inside the step graph (drives the WHILE conditional); 1: eager launches (the host
+// reads Scal::done); 2: standalone timing launch (no solver scalars touched)
+template <int kMode>
+__device__ inline void pcg_continue(cudaGraphConditionalHandle hc, Scal* s, bool go) {
+  if (kMode == 0) cudaGraphSetConditional(hc, go ? 1u : 0u);
+  else if (kMode == 1) s->done = go ? 0 : 1;
+}
+
 __device__ inline double reduce_parts(const double* part, int k, double* sh) {
   double s = 0.0;
   for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(part + b * 4 + k);
@@ -99,6 +112,12 @@ template <int D>
 __device__ inline void warp_sum3(double* s) {
 #pragma unroll
   for (int c = 0; c < D; ++c) s[c] = warp_sum(s[c]);
+}
+
+// (hi, lo) FP32 pair of a double: hi + lo reproduces x to 48 bits
+__device__ inline float2 split_pair(double x) {
+  const float hi = (float)x;
+  return make_float2(hi, (float)(x - (double)hi));
 }
 
 // ------------------------------------------------------------------ per-step kernels
@@ -135,6 +154,7 @@ __global__ void k_predict(Args g) {
     else if (hist == 1) x0 = 2.0 * ai - g.a1[i];
     if (g.fixed[i]) x0 = 0.0;
     g.x0[i] = x0;
+    if (g.spmv_pair) g.p2[i] = split_pair(x0);  // p2 is scratch until p is first written
   }
 }
 
@@ -147,7 +167,7 @@ __global__ void k_predict(Args g) {
        row += (int64_t)gridDim.x * blockDim.x)
 
 // r = b - A x0 with b = f - K q1 - M q2 - Cabs y1; bb = |b|^2.  x = x0.
-template <int D>
+template <int D, bool kPair>
 __global__ void __launch_bounds__(kThreads) k_residual(Args g) {
   __shared__ double sh[32];
   double pbb = 0.0;
@@ -155,8 +175,12 @@ __global__ void __launch_bounds__(kThreads) k_residual(Args g) {
     const int64_t sl = row >> 5;
     const int64_t p0 = g.sf_ptr[sl] + (row & 31), W = (g.sf_ptr[sl + 1] - g.sf_ptr[sl]) >> 5;
     double sb[D], sx[D];
+    float xh[D], xl[D];
 #pragma unroll
-    for (int c = 0; c < D; ++c) sb[c] = sx[c] = 0.0;
+    for (int c = 0; c < D; ++c) {
+      sb[c] = sx[c] = 0.0;
+      xh[c] = xl[c] = 0.f;
+    }
     for (int64_t j = 0; j < W; ++j) {
       const int64_t pos = p0 + 32 * j;
       const int64_t bs = (int64_t)__ldcs(g.sf_col + pos) * D;
@@ -168,18 +192,48 @@ __global__ void __launch_bounds__(kThreads) k_residual(Args g) {
         q2a[d] = g.q2[bs + d];
       }
       const double m = __ldcs(g.MSS + pos);
+      if (kPair) {
+        // b part in FP64 (elastic forces cancel); A x0 in FP32-pair arithmetic on the A planes
+        float2 xp[D];
 #pragma unroll
-      for (int c = 0; c < D; ++c) {
-        double sq = m * q2a[c], sxx = 0.0;
+        for (int d = 0; d < D; ++d) xp[d] = g.p2[bs + d];
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-          const double kv = __ldcs(g.KS + (int64_t)(c * D + d) * g.sf_n + pos);
-          sq = fma(kv, qa[d], sq);
-          sxx = fma(kv, xa[d], sxx);
+        for (int c = 0; c < D; ++c) {
+          double sq = m * q2a[c];
+#pragma unroll
+          for (int d = 0; d < D; ++d) sq = fma(__ldcs(g.KS + (int64_t)(c * D + d) * g.sf_n + pos), qa[d], sq);
+          sb[c] += sq;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            const float2 a2 = __ldcs(g.APS + (int64_t)(c * D + d) * g.sf_n + pos);
+            const float ah = a2.x, al = a2.y;
+            const float pr = __fmul_rn(ah, xp[d].x);
+            const float pe = fmaf(ah, xp[d].x, -pr);
+            const float t = __fadd_rn(xh[c], pr);
+            const float bp = __fsub_rn(t, xh[c]);
+            const float e2 = __fadd_rn(__fsub_rn(xh[c], __fsub_rn(t, bp)), __fsub_rn(pr, bp));
+            xh[c] = t;
+            xl[c] += (pe + e2) + fmaf(ah, xp[d].y, al * xp[d].x);
+          }
         }
-        sb[c] += sq;
-        sx[c] = fma(g.aK, sxx, fma(g.aM * m, xa[c], sx[c]));
+      } else {
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          double sq = m * q2a[c], sxx = 0.0;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            const double kv = __ldcs(g.KS + (int64_t)(c * D + d) * g.sf_n + pos);
+            sq = fma(kv, qa[d], sq);
+            sxx = fma(kv, xa[d], sxx);
+          }
+          sb[c] += sq;
+          sx[c] = fma(g.aK, sxx, fma(g.aM * m, xa[c], sx[c]));
+        }
       }
+    }
+    if (kPair) {
+#pragma unroll
+      for (int c = 0; c < D; ++c) sx[c] = (double)xh[c] + (double)xl[c];
     }
     if (row < g.n_nodes) {
 #pragma unroll
@@ -191,10 +245,11 @@ __global__ void __launch_bounds__(kThreads) k_residual(Args g) {
           for (int64_t k = g.cab_ptr[i]; k < g.cab_ptr[i + 1]; ++k) {
             const int jj = g.cab_col[k];
             cb = fma(g.cab_val[k], g.y1[jj], cb);
-            cx = fma(g.cab_val[k], g.x0[jj], cx);
+            if (!kPair) cx = fma(g.cab_val[k], g.x0[jj], cx);
           }
           bv = g.f[i] - sb[c] - cb;
-          rv = bv - (sx[c] + g.aC * cx);
+          // the A planes of the pair path already hold the dashpots (A = M + dt/2 C + dt^2/4 K)
+          rv = kPair ? bv - sx[c] : bv - (sx[c] + g.aC * cx);
         }
         g.r[i] = rv;
         g.x[i] = g.x0[i];
@@ -243,7 +298,7 @@ __global__ void __launch_bounds__(kThreads) k_prec_lower(Args g) {
 
 // z = G^T t ; partial r.z ; mode 0 (inside PCG): last block computes beta, rz;
 // mode 1 (after the residual): p = z, rz, rr and the conditional from |r| vs |b|.
-template <int D>
+template <int D, int kMode>
 __global__ void __launch_bounds__(kThreads) k_prec_upper(Args g, int mode, cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
   double prz = 0.0, prr = 0.0;
@@ -271,7 +326,10 @@ __global__ void __launch_bounds__(kThreads) k_prec_upper(Args g, int mode, cudaG
         const double z = (double)s[c];
         const double r = g.r[i];
         g.z[i] = z;
-        if (mode == 1) g.p[i] = z;
+        if (mode == 1) {
+          g.p[i] = z;
+          if (g.spmv_pair) g.p2[i] = split_pair(z);
+        }
         prz += r * z;
         prr += r * r;
       }
@@ -293,7 +351,7 @@ __global__ void __launch_bounds__(kThreads) k_prec_upper(Args g, int mode, cudaG
         s->rz = rz;
         s->rr = rr;
         const bool done = rr <= s->tol2 * s->bb;
-        cudaGraphSetConditional(hc, done ? 0u : 1u);
+        pcg_continue<kMode>(hc, s, !done);
       } else {
         s->beta = s->rz != 0.0 ? rz / s->rz : 0.0;
         s->rz = rz;
@@ -302,8 +360,32 @@ __global__ void __launch_bounds__(kThreads) k_prec_upper(Args g, int mode, cudaG
   }
 }
 
+// z = G^T t only (no reductions, no graph conditional): used by sc_nb_apply
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_prec_upper_nograph(Args g) {
+  SELL_ROW_LOOP(g.su_ptr) {
+    const int64_t sl = row >> 5;
+    const int64_t p0 = g.su_ptr[sl] + (row & 31), W = (g.su_ptr[sl + 1] - g.su_ptr[sl]) >> 5;
+    float s[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) s[c] = 0.f;
+    for (int64_t j = 0; j < W; ++j) {
+      const int64_t pos = p0 + 32 * j;
+      const int64_t bs = (int64_t)g.su_col[pos] * D;
+#pragma unroll
+      for (int c = 0; c < D; ++c)
+#pragma unroll
+        for (int d = 0; d < D; ++d) s[c] = fmaf(g.GTS[(int64_t)(c * D + d) * g.su_n + pos], g.t32[bs + d], s[c]);
+    }
+    if (row < g.n_nodes) {
+#pragma unroll
+      for (int c = 0; c < D; ++c) g.z[row * D + c] = (double)s[c];
+    }
+  }
+}
+
 // w = A p ; partial p.w ; last block: alpha
-template <int D, bool kInGraph>
+template <int D, int kMode>
 __global__ void __launch_bounds__(kThreads) k_spmv(Args g, cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
   double ppw = 0.0;
@@ -346,11 +428,81 @@ __global__ void __launch_bounds__(kThreads) k_spmv(Args g, cudaGraphConditionalH
       Scal* s = g.s;
       s->ticket = 0;
       s->pw = pw;
-      if (kInGraph) {
+      if (kMode != 2) {
         if (!(pw > 0.0)) {
           s->alpha = 0.0;
           s->status = SC_BREAKDOWN;
-          cudaGraphSetConditional(hc, 0u);
+          pcg_continue<kMode>(hc, s, false);
+        } else {
+          s->alpha = s->rz / pw;
+        }
+      }
+    }
+  }
+}
+
+// w = A p in FP32-pair arithmetic.  Each product A_cd p_d = (ah + al)(ph + pl) is formed as
+// the exact FP32 product ah*ph (TwoProd through fmaf) plus the cross terms ah*pl + al*ph;
+// the row sums are carried as an unevaluated (hi, lo) FP32 pair with TwoSum (Knuth) and
+// converted to FP64 once per row.  Relative accuracy ~2^-46 per product, no FP64 pipe work
+// in the block loop; same bytes as the FP64 kernel (A: 2 x 4 B per value, p: 8 B pairs).
+template <int D, int kMode>
+__global__ void __launch_bounds__(kThreads) k_spmv_pair(Args g, cudaGraphConditionalHandle hc) {
+  __shared__ double sh[32];
+  double ppw = 0.0;
+  SELL_ROW_LOOP(g.sf_ptr) {
+    const int64_t sl = row >> 5;
+    const int64_t p0 = g.sf_ptr[sl] + (row & 31), W = (g.sf_ptr[sl + 1] - g.sf_ptr[sl]) >> 5;
+    float hi[D], lo[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) hi[c] = lo[c] = 0.f;
+#pragma unroll 2
+    for (int64_t j = 0; j < W; ++j) {
+      const int64_t pos = p0 + 32 * j;
+      const int64_t bs = (int64_t)__ldcs(g.sf_col + pos) * D;
+      float2 pv[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) pv[d] = g.p2[bs + d];
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          const float2 a2 = __ldcs(g.APS + (int64_t)(c * D + d) * g.sf_n + pos);
+          const float ah = a2.x, al = a2.y;
+          // _rn intrinsics: no contraction into FMAs, which would break the error terms
+          const float pr = __fmul_rn(ah, pv[d].x);
+          const float pe = fmaf(ah, pv[d].x, -pr);
+          const float t = __fadd_rn(hi[c], pr);
+          const float bp = __fsub_rn(t, hi[c]);
+          const float e2 = __fadd_rn(__fsub_rn(hi[c], __fsub_rn(t, bp)), __fsub_rn(pr, bp));
+          hi[c] = t;
+          lo[c] += (pe + e2) + fmaf(ah, pv[d].y, al * pv[d].x);
+        }
+      }
+    }
+    if (row < g.n_nodes) {
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        const double wv = (double)hi[c] + (double)lo[c];
+        const int64_t i = row * D + c;
+        g.w[i] = wv;
+        ppw += g.p[i] * wv;
+      }
+    }
+  }
+  const double t = block_sum(ppw, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 3] = t;
+  if (last_block(&g.s->ticket)) {
+    const double pw = reduce_parts(g.part, 3, sh);
+    if (threadIdx.x == 0) {
+      Scal* s = g.s;
+      s->ticket = 0;
+      s->pw = pw;
+      if (kMode != 2) {
+        if (!(pw > 0.0)) {
+          s->alpha = 0.0;
+          s->status = SC_BREAKDOWN;
+          pcg_continue<kMode>(hc, s, false);
         } else {
           s->alpha = s->rz / pw;
         }
@@ -360,6 +512,7 @@ __global__ void __launch_bounds__(kThreads) k_spmv(Args g, cudaGraphConditionalH
 }
 
 // x += alpha p ; r -= alpha w ; partial r.r ; last block: convergence test
+template <int kMode>
 __global__ void k_update(Args g, cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
   const double alpha = g.s->alpha;
@@ -385,15 +538,18 @@ __global__ void k_update(Args g, cudaGraphConditionalHandle hc) {
         done = true;
       }
       if (s->status == SC_BREAKDOWN) done = true;
-      if (done) cudaGraphSetConditional(hc, 0u);
+      if (done) pcg_continue<kMode>(hc, s, false);
     }
   }
 }
 
 __global__ void k_direction(Args g) {
   const double beta = g.s->beta;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x)
-    g.p[i] = fma(beta, g.p[i], g.z[i]);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
+    const double pv = fma(beta, g.p[i], g.z[i]);
+    g.p[i] = pv;
+    if (g.spmv_pair) g.p2[i] = split_pair(pv);
+  }
 }
 
 // u = up + dt^2/4 x ; v = vp + dt/2 x ; shift the acceleration history ; record ; t += 1
@@ -705,6 +861,13 @@ __global__ void __launch_bounds__(kThreads) k_explicit(Args g, const double* __r
   }
 }
 
+// f = entries of step s->t (f zeroed beforehand)
+__global__ void k_force_explicit0(Args g) {
+  const int t = g.s->t;
+  if (!g.f_ptr || t < 0 || t >= g.n_t) return;
+  for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f[g.f_slot[k]] += g.f_val[k];
+}
+
 // f holds the entries of step t (= s->t); clear those of t-1
 __global__ void k_force_explicit(Args g) {
   const int t = g.s->t;
@@ -863,9 +1026,10 @@ int build_graph(sc_nb_newmark* h) {
       break;
     k_force<<<1, 256, 0, cs>>>(g);
     k_predict<<<vbk, 256, 0, cs>>>(g);
-    k_residual<D><<<nbk, kThreads, 0, cs>>>(g);
+    if (g.spmv_pair) k_residual<D, true><<<nbk, kThreads, 0, cs>>>(g);
+    else k_residual<D, false><<<nbk, kThreads, 0, cs>>>(g);
     k_prec_lower<D><<<nbk, kThreads, 0, cs>>>(g);
-    k_prec_upper<D><<<nbk, kThreads, 0, cs>>>(g, 1, hc);
+    k_prec_upper<D, 0><<<nbk, kThreads, 0, cs>>>(g, 1, hc);
     cudaStreamCaptureStatus stt;
     const cudaGraphNode_t* deps = nullptr;
     size_t ndeps = 0;
@@ -885,10 +1049,11 @@ int build_graph(sc_nb_newmark* h) {
     if ((rc = check(cudaStreamBeginCaptureToGraph(c2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
                     "capture body")))
       break;
-    k_spmv<D, true><<<nbk, kThreads, 0, c2>>>(g, hc);
-    k_update<<<vbk, 256, 0, c2>>>(g, hc);
+    if (g.spmv_pair) k_spmv_pair<D, 0><<<nbk, kThreads, 0, c2>>>(g, hc);
+    else k_spmv<D, 0><<<nbk, kThreads, 0, c2>>>(g, hc);
+    k_update<0><<<vbk, 256, 0, c2>>>(g, hc);
     k_prec_lower<D><<<nbk, kThreads, 0, c2>>>(g);
-    k_prec_upper<D><<<nbk, kThreads, 0, c2>>>(g, 0, hc);
+    k_prec_upper<D, 0><<<nbk, kThreads, 0, c2>>>(g, 0, hc);
     k_direction<<<vbk, 256, 0, c2>>>(g);
     cudaGraph_t bo;
     if ((rc = check(cudaStreamEndCapture(c2, &bo), "end body"))) break;
@@ -922,6 +1087,13 @@ void drop_graph(sc_nb_newmark* h) {
 }
 
 }  // namespace
+
+__global__ void k_split_pairs(int64_t n, const double* __restrict__ x, float2* __restrict__ hl) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float h = (float)x[i];
+    hl[i] = make_float2(h, (float)(x[i] - (double)h));
+  }
+}
 
 // Sliced-ELL copies of K, A, M (full pattern), G (lower) and G^T (upper) for the per-step
 // kernels; allocated here (setup) from the stream-ordered pool and freed by sc_nb_destroy.
@@ -963,7 +1135,11 @@ static int build_sell(sc_nb_newmark* h, const double* KB, const double* AB, cons
       k_sell_permute<double><<<pb, 256, 0, st>>>(D2, total, g.nnzb, src, KB, ks);
       k_sell_permute<double><<<pb, 256, 0, st>>>(D2, total, g.nnzb, src, AB, as);
       k_sell_permute<double><<<pb, 256, 0, st>>>(1, total, g.nnzb, src, MS, ms);
+      float2* ap = nullptr;
+      if ((rc = alloc((void**)&ap, 8 * D2 * total))) break;
+      k_split_pairs<<<pb, 256, 0, st>>>((int64_t)D2 * total, as, ap);
       g.sf_ptr = ptr; g.sf_col = col; g.sf_n = total; g.KS = ks; g.AS = as; g.MSS = ms;
+      g.APS = ap;
     } else {
       float* gs = nullptr;
       if ((rc = alloc((void**)&gs, 4 * D2 * total))) break;
@@ -1067,7 +1243,8 @@ extern "C" int sc_nb_create(sc_nb_newmark** out, int n_nodes, int dim, const int
   g.p = (double*)take(8 * ns);
   g.w = (double*)take(8 * ns);
   g.f = (double*)take(8 * ns);
-  take(8 * ns);
+  g.p2 = (float2*)take(8 * ns);
+  g.spmv_pair = 1;
   g.t32 = (float*)take(4 * ns);
   g.part = (double*)take(8 * 4 * 152 * 16);
   g.s = (Scal*)take(sizeof(Scal));
@@ -1124,6 +1301,13 @@ extern "C" int sc_nb_create(sc_nb_newmark** out, int n_nodes, int dim, const int
   return SC_OK;
 }
 
+extern "C" int sc_nb_set_options(sc_nb_newmark* h, int options) {
+  if (!h) return SC_BAD_ARG;
+  h->g.spmv_pair = (options & 1) ? 0 : 1;
+  drop_graph(h);
+  return SC_OK;
+}
+
 extern "C" int sc_nb_set_force(sc_nb_newmark* h, int n_t, const int64_t* f_ptr, const int* f_slot,
                                const double* f_val) {
   if (!h || n_t < 0 || (n_t > 0 && (!f_ptr || !f_slot || !f_val))) return SC_BAD_ARG;
@@ -1156,9 +1340,56 @@ extern "C" int sc_nb_set_output(sc_nb_newmark* h, int out_interval, int n_rec, c
 // t_begin: state index of u/v/a on entry (the force entries of step t_begin are assumed in f
 // when t_begin > 0; at t_begin == 0 they are written here).  The warm start uses the
 // acceleration history (a1, a2) once steps of this solver have filled it.
+// One step with eager launches (no graph): the same kernels, the PCG loop driven by the host
+// reading Scal::done after each iteration.  Used for profiling (kernels inside graphs with
+// conditional nodes cannot be captured by the profiler); selected by SCATTER_GB300_EAGER=1.
+template <int D>
+static int eager_step(sc_nb_newmark* h) {
+  Args g = h->g;
+  cudaStream_t st = h->user;
+  const unsigned nbk = h->node_blocks, vbk = h->vec_blocks;
+  cudaGraphConditionalHandle none = 0;
+  k_force<<<1, 256, 0, st>>>(g);
+  k_predict<<<vbk, 256, 0, st>>>(g);
+  if (g.spmv_pair) k_residual<D, true><<<nbk, kThreads, 0, st>>>(g);
+  else k_residual<D, false><<<nbk, kThreads, 0, st>>>(g);
+  k_prec_lower<D><<<nbk, kThreads, 0, st>>>(g);
+  k_prec_upper<D, 1><<<nbk, kThreads, 0, st>>>(g, 1, none);
+  int done = 0;
+  int rc;
+  for (int guard = 0; guard < 100000; ++guard) {
+    if ((rc = check(cudaMemcpyAsync(&done, &g.s->done, sizeof(int), cudaMemcpyDeviceToHost, st), "read done")))
+      return rc;
+    if ((rc = check(cudaStreamSynchronize(st), "sync eager"))) return rc;
+    if (done) break;
+    if (g.spmv_pair) k_spmv_pair<D, 1><<<nbk, kThreads, 0, st>>>(g, none);
+    else k_spmv<D, 1><<<nbk, kThreads, 0, st>>>(g, none);
+    k_update<1><<<vbk, 256, 0, st>>>(g, none);
+    k_prec_lower<D><<<nbk, kThreads, 0, st>>>(g);
+    k_prec_upper<D, 1><<<nbk, kThreads, 0, st>>>(g, 0, none);
+    k_direction<<<vbk, 256, 0, st>>>(g);
+  }
+  k_finalize<<<vbk, 256, 0, st>>>(g);
+  k_record<<<vbk, 256, 0, st>>>(g);
+  k_advance<<<1, 32, 0, st>>>(g);
+  return check_launch("eager step");
+}
+
 extern "C" int sc_nb_run(sc_nb_newmark* h, int t_begin, int t_end) {
   if (!h || t_begin < 0 || t_end < t_begin) return SC_BAD_ARG;
   int rc;
+  const char* eager = getenv("SCATTER_GB300_EAGER");
+  if (eager && eager[0] == '1') {
+    cudaStream_t st = h->user;
+    if (t_begin == 0 && h->g.f_ptr) {
+      k_set_t<<<1, 1, 0, st>>>(h->g.s, -1);
+      k_force<<<1, 256, 0, st>>>(h->g);
+    }
+    k_set_t<<<1, 1, 0, st>>>(h->g.s, t_begin);
+    for (int t = t_begin; t < t_end; ++t)
+      if ((rc = h->g.D == 3 ? eager_step<3>(h) : eager_step<2>(h))) return rc;
+    return SC_OK;
+  }
   if (!h->exec) {
     rc = h->g.D == 3 ? build_graph<3>(h) : build_graph<2>(h);
     if (rc) return rc;
@@ -1271,6 +1502,288 @@ extern "C" int sc_nb_time_explicit(sc_nb_newmark* h, int reps, float* ms_per_ste
   return rc;
 }
 
+// ------------------------------------------------------------------ adjoint of the explicit scheme
+// Discrete adjoint of sc_nb_explicit_run for the receiver-velocity misfit
+//   J = 1/2 sum_{n=1..N} |P v_n - d_n|^2
+// with respect to per-element E and rho (K = sum E_e K1_e + springs, M_L = sum rho_e ml1_e,
+// Cab = sum sqrt(rho_e E_e) C1_f).  Forward with checkpoints every C steps, then per segment
+// (last first) recompute the states and run the backward recursion (g = mu_v + dt mu_u,
+// y = M_L^-1 g, mu_u -= dt K y, mu_v = g - dt (beta K y + Cab y + alpha M_L y) + P^T(P v_n - d_n))
+// accumulating dJ/dE_e, dJ/drho_e element by element (deterministic, no atomics).
+struct sc_adj_desc {
+  int n_steps, checkpoint;
+  int n_rec;
+  const int* rec_slot;
+  const double* target;
+  int n_elem, n_en;
+  const int *elem, *ke_type;
+  const float* ke1;
+  const double *young, *rho, *ml1;
+  const int64_t* l_eptr;
+  const int *l_row, *l_col;
+  const double *l_c, *l_s;
+};
+namespace {
+
+struct AdjState {
+  double *seg_u, *seg_v, *mu_u, *mu_v, *y, *out_v, *gE, *gR;
+  int *n_dev, *seg_t0, *rec_map;
+  double* J;
+};
+
+__global__ void k_adj_store(Args g, const double* __restrict__ v_src, AdjState a) {
+  const int k = g.s->t - *a.seg_t0;  // state index inside the segment after this step
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
+    a.seg_u[(int64_t)k * g.n_s + i] = g.u[i];
+    a.seg_v[(int64_t)k * g.n_s + i] = v_src[i];
+  }
+}
+
+// y = (mu_v + dt mu_u) / M_L, 0 on fixed slots
+__global__ void k_adj_y(Args g, const double* __restrict__ ML, AdjState a) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
+    const double gg = fma(g.dt, a.mu_u[i], a.mu_v[i]);
+    a.y[i] = g.fixed[i] ? 0.0 : gg / ML[i];
+  }
+}
+
+// K y per node row (FP64), then the mu update of the row's slots
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_adj_mu(Args g, const double* __restrict__ ML, AdjState a,
+                                                     const double* __restrict__ target, int n_rec) {
+  const int n = *a.n_dev;  // the step being reversed (state n -> n+1)
+  const int k = n - *a.seg_t0;
+  SELL_ROW_LOOP(g.sf_ptr) {
+    const int64_t sl = row >> 5;
+    const int64_t p0 = g.sf_ptr[sl] + (row & 31), W = (g.sf_ptr[sl + 1] - g.sf_ptr[sl]) >> 5;
+    double s[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) s[c] = 0.0;
+    for (int64_t j = 0; j < W; ++j) {
+      const int64_t pos = p0 + 32 * j;
+      const int64_t bs = (int64_t)g.sf_col[pos] * D;
+#pragma unroll
+      for (int c = 0; c < D; ++c)
+#pragma unroll
+        for (int d = 0; d < D; ++d) s[c] = fma(g.KS[(int64_t)(c * D + d) * g.sf_n + pos], a.y[bs + d], s[c]);
+    }
+    if (row < g.n_nodes) {
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        const int64_t i = row * D + c;
+        if (g.fixed[i]) {
+          a.mu_u[i] = 0.0;
+          a.mu_v[i] = 0.0;
+          continue;
+        }
+        double cy = 0.0;
+        for (int64_t q = g.cab_ptr[i]; q < g.cab_ptr[i + 1]; ++q) cy = fma(g.cab_val[q], a.y[g.cab_col[q]], cy);
+        const double yi = a.y[i];
+        const double gg = fma(g.dt, a.mu_u[i], a.mu_v[i]);
+        a.mu_u[i] = fma(-g.dt, s[c], a.mu_u[i]);
+        double mv = gg - g.dt * (g.beta_r * s[c] + cy + g.alpha_r * ML[i] * yi);
+        const int rj = a.rec_map[i];
+        if (rj >= 0 && n >= 1) mv += a.seg_v[(int64_t)k * g.n_s + i] - target[(int64_t)n * n_rec + rj];
+        a.mu_v[i] = mv;
+      }
+    }
+  }
+}
+
+// per element: dJ/dE_e += -dt y_e^T K1 (u + beta v)_e ; dJ/drho_e += -dt sum ml1 y (a + alpha v)
+// plus the element's Lysmer entries
+__global__ void k_adj_grad(Args g, sc_adj_desc d, AdjState a) {
+  const int n = *a.n_dev;
+  const int k = n - *a.seg_t0;
+  const double* u = a.seg_u + (int64_t)k * g.n_s;
+  const double* v = a.seg_v + (int64_t)k * g.n_s;
+  const double* v1 = a.seg_v + (int64_t)(k + 1) * g.n_s;
+  const int nd = 3 * d.n_en;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d.n_elem; e += gridDim.x * blockDim.x) {
+    const int* en = d.elem + (int64_t)e * d.n_en;
+    const float* K1 = d.ke1 + (int64_t)d.ke_type[e] * nd * nd;
+    float ge = 0.f;
+    double gr = 0.0;
+    // K1 annihilates rigid translations: subtract the first node's (u + beta v) before
+    // rounding to FP32, so the FP32 products see strains, not displacements
+    double w0[3];
+    for (int c = 0; c < 3; ++c) w0[c] = fma(g.beta_r, v[(int64_t)en[0] * 3 + c], u[(int64_t)en[0] * 3 + c]);
+    for (int la = 0; la < d.n_en; ++la) {
+      const int64_t sa = (int64_t)en[la] * 3;
+      for (int c = 0; c < 3; ++c) {
+        const double ya = a.y[sa + c];
+        if (ya == 0.0) continue;
+        float row = 0.f;
+        for (int lb = 0; lb < d.n_en; ++lb) {
+          const int64_t sb = (int64_t)en[lb] * 3;
+          const float* kr = K1 + (int64_t)(la * 3 + c) * nd + lb * 3;
+          row = fmaf(kr[0], (float)(fma(g.beta_r, v[sb], u[sb]) - w0[0]), row);
+          row = fmaf(kr[1], (float)(fma(g.beta_r, v[sb + 1], u[sb + 1]) - w0[1]), row);
+          row = fmaf(kr[2], (float)(fma(g.beta_r, v[sb + 2], u[sb + 2]) - w0[2]), row);
+        }
+        ge = fmaf((float)ya, row, ge);
+        const double acc = (v1[sa + c] - v[sa + c]) / g.dt;
+        gr += d.ml1[((int64_t)e * d.n_en + la) * 3 + c] * ya * fma(g.alpha_r, v[sa + c], acc);
+      }
+    }
+    double gE = (double)ge;
+    double cR = 0.0;
+    for (int64_t q = d.l_eptr[e]; q < d.l_eptr[e + 1]; ++q) {
+      const double yr = a.y[d.l_row[q]];
+      const int cl = d.l_col[q];
+      gE += yr * (d.l_s[q] / d.young[e] * fma(g.beta_r, v[cl], u[cl]) + 0.5 * d.l_c[q] / d.young[e] * v[cl]);
+      cR += yr * 0.5 * d.l_c[q] / d.rho[e] * v[cl];
+    }
+    a.gE[e] -= g.dt * gE;
+    a.gR[e] -= g.dt * (gr + cR);
+  }
+}
+
+__global__ void k_adj_dec(AdjState a) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *a.n_dev -= 1;
+}
+
+__global__ void k_adj_init(Args g, AdjState a, const double* target, int n_rec, int N) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
+    a.mu_u[i] = 0.0;
+    const int rj = a.rec_map[i];
+    a.mu_v[i] = rj >= 0 ? a.out_v[(int64_t)N * n_rec + rj] - target[(int64_t)N * n_rec + rj] : 0.0;
+  }
+}
+
+__global__ void k_adj_misfit(const double* out_v, const double* target, int n_rec, int N, double* J) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int64_t q = (int64_t)n_rec + threadIdx.x; q < (int64_t)(N + 1) * n_rec; q += blockDim.x) {
+    const double r = out_v[q] - target[q];
+    s += r * r;
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) *J = 0.5 * s;
+}
+
+__global__ void k_rec_map2(int n_s, int n_rec, const int* rec, int* map) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_s; i += (int64_t)gridDim.x * blockDim.x) map[i] = -1;
+}
+__global__ void k_rec_map2_fill(int n_rec, const int* rec, int* map) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n_rec; j += gridDim.x * blockDim.x) map[rec[j]] = j;
+}
+
+}  // namespace
+
+extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_host, double* grad_E,
+                             double* grad_rho) {
+  if (!h || !dp || !grad_E || !grad_rho) return SC_BAD_ARG;
+  const sc_adj_desc d = *dp;
+  if (d.n_steps <= 0 || d.checkpoint <= 0 || d.n_rec <= 0 || !d.rec_slot || !d.target || d.n_elem <= 0 ||
+      !d.elem || !d.ke_type || !d.ke1 || !d.young || !d.rho || !d.ml1 || !d.l_eptr || h->g.D != 3)
+    return SC_BAD_ARG;
+  Args& g = h->g;
+  cudaStream_t st = h->user;
+  const int N = d.n_steps, C = d.checkpoint, nseg = (N + C - 1) / C;
+  const int64_t ns = g.n_s;
+  // save the caller's output configuration
+  const int o_int = g.out_interval, o_nrec = g.n_rec;
+  const int* o_rec = g.rec_slot;
+  double *o_u = g.out_u, *o_v = g.out_v, *o_a = g.out_a;
+  const int64_t o_nout = g.n_out;
+  AdjState a{};
+  double *ck_u = nullptr, *ck_v = nullptr;
+  int rc = SC_OK;
+  auto M = [&](void** p, size_t b) { return check(cudaMallocAsync(p, b, st), "adjoint malloc"); };
+  do {
+    if ((rc = M((void**)&ck_u, 8 * ns * nseg)) || (rc = M((void**)&ck_v, 8 * ns * nseg)) ||
+        (rc = M((void**)&a.seg_u, 8 * ns * (C + 1))) || (rc = M((void**)&a.seg_v, 8 * ns * (C + 1))) ||
+        (rc = M((void**)&a.mu_u, 8 * ns)) || (rc = M((void**)&a.mu_v, 8 * ns)) || (rc = M((void**)&a.y, 8 * ns)) ||
+        (rc = M((void**)&a.out_v, 8 * (int64_t)(N + 1) * d.n_rec)) || (rc = M((void**)&a.n_dev, 4)) ||
+        (rc = M((void**)&a.seg_t0, 4)) || (rc = M((void**)&a.rec_map, 4 * ns)) || (rc = M((void**)&a.J, 8)))
+      break;
+    a.gE = grad_E;
+    a.gR = grad_rho;
+    cudaMemsetAsync(grad_E, 0, 8 * (size_t)d.n_elem, st);
+    cudaMemsetAsync(grad_rho, 0, 8 * (size_t)d.n_elem, st);
+    cudaMemsetAsync(a.out_v, 0, 8 * (size_t)(N + 1) * d.n_rec, st);
+    k_rec_map2<<<grid_for(ns, 256), 256, 0, st>>>((int)ns, d.n_rec, d.rec_slot, a.rec_map);
+    k_rec_map2_fill<<<grid_for(d.n_rec, 128), 128, 0, st>>>(d.n_rec, d.rec_slot, a.rec_map);
+    // forward from rest with checkpoints; receivers recorded into a.out_v
+    cudaMemsetAsync(g.u, 0, 8 * ns, st);
+    cudaMemsetAsync(g.v, 0, 8 * ns, st);
+    if ((rc = sc_nb_set_output(h, 1, d.n_rec, d.rec_slot, nullptr, a.out_v, nullptr, N + 1))) break;
+    for (int sgi = 0; sgi < nseg && !rc; ++sgi) {
+      const int t0 = sgi * C, t1 = t0 + C < N ? t0 + C : N;
+      cudaMemcpyAsync(ck_u + sgi * ns, g.u, 8 * ns, cudaMemcpyDeviceToDevice, st);
+      cudaMemcpyAsync(ck_v + sgi * ns, g.v, 8 * ns, cudaMemcpyDeviceToDevice, st);
+      rc = sc_nb_explicit_run(h, t0, t1);
+    }
+    if (rc) break;
+    k_adj_misfit<<<1, 1024, 0, st>>>(a.out_v, d.target, d.n_rec, N, a.J);
+    // graphs: recompute step (explicit step + store), backward step
+    cudaGraphExec_t rec_exec[2] = {nullptr, nullptr}, bwd_exec = nullptr;
+    cudaGraph_t rec_graph[2] = {nullptr, nullptr}, bwd_graph = nullptr;
+    for (int k = 0; k < 2 && !rc; ++k) {
+      const double* vin = k == 0 ? g.v : h->v1;
+      double* vout = k == 0 ? h->v1 : g.v;
+      const double* win = k == 0 ? h->w0 : h->w1;
+      double* wout = k == 0 ? h->w1 : h->w0;
+      if ((rc = check(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal), "capture rec"))) break;
+      k_explicit<3><<<h->node_blocks, kThreads, 0, h->cap>>>(g, h->ML, vin, vout, win, wout, h->rec_map);
+      k_force_explicit<<<1, 256, 0, h->cap>>>(g);
+      k_adj_store<<<h->vec_blocks, 256, 0, h->cap>>>(g, vout, a);
+      if ((rc = check(cudaStreamEndCapture(h->cap, &rec_graph[k]), "end rec"))) break;
+      rc = check(cudaGraphInstantiate(&rec_exec[k], rec_graph[k], 0), "inst rec");
+    }
+    if (!rc) {
+      if (!(rc = check(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal), "capture bwd"))) {
+        k_adj_y<<<h->vec_blocks, 256, 0, h->cap>>>(g, h->ML, a);
+        k_adj_grad<<<grid_for(d.n_elem, 128, 152 * 32), 128, 0, h->cap>>>(g, d, a);
+        k_adj_mu<3><<<h->node_blocks, kThreads, 0, h->cap>>>(g, h->ML, a, d.target, d.n_rec);
+        k_adj_dec<<<1, 32, 0, h->cap>>>(a);
+        if (!(rc = check(cudaStreamEndCapture(h->cap, &bwd_graph), "end bwd")))
+          rc = check(cudaGraphInstantiate(&bwd_exec, bwd_graph, 0), "inst bwd");
+      }
+    }
+    if (!rc) {
+      k_adj_init<<<h->vec_blocks, 256, 0, st>>>(g, a, d.target, d.n_rec, N);
+      for (int sgi = nseg - 1; sgi >= 0 && !rc; --sgi) {
+        const int t0 = sgi * C, t1 = t0 + C < N ? t0 + C : N;
+        cudaMemcpyAsync(g.u, ck_u + sgi * ns, 8 * ns, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(g.v, ck_v + sgi * ns, 8 * ns, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(a.seg_u, g.u, 8 * ns, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(a.seg_v, g.v, 8 * ns, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(a.seg_t0, &t0, 4, cudaMemcpyHostToDevice, st);
+        // recompute states t0+1 .. t1 (the force of step t0 is restored by the setup kernels)
+        k_w_init<<<h->vec_blocks, 256, 0, st>>>(g, h->w0);
+        cudaMemsetAsync(g.f, 0, 8 * ns, st);
+        k_set_t<<<1, 1, 0, st>>>(g.s, t0);
+        k_force_explicit0<<<1, 256, 0, st>>>(g);
+        int kk = 0;
+        for (int t = t0; t < t1 && !rc; ++t, kk ^= 1) rc = check(cudaGraphLaunch(rec_exec[kk], st), "rec launch");
+        // backward t1-1 .. t0
+        const int nstart = t1 - 1;
+        cudaMemcpyAsync(a.n_dev, &nstart, 4, cudaMemcpyHostToDevice, st);
+        for (int t = t1 - 1; t >= t0 && !rc; --t) rc = check(cudaGraphLaunch(bwd_exec, st), "bwd launch");
+        if (!rc) rc = check(cudaStreamSynchronize(st), "sync segment");  // host copies of t0/nstart
+      }
+    }
+    for (int k = 0; k < 2; ++k) {
+      if (rec_exec[k]) cudaGraphExecDestroy(rec_exec[k]);
+      if (rec_graph[k]) cudaGraphDestroy(rec_graph[k]);
+    }
+    if (bwd_exec) cudaGraphExecDestroy(bwd_exec);
+    if (bwd_graph) cudaGraphDestroy(bwd_graph);
+    if (!rc && J_host) {
+      rc = check(cudaMemcpyAsync(J_host, a.J, 8, cudaMemcpyDeviceToHost, st), "J");
+      if (!rc) rc = check(cudaStreamSynchronize(st), "sync J");
+    }
+  } while (0);
+  cudaStreamSynchronize(st);
+  void* frees[] = {ck_u, ck_v, a.seg_u, a.seg_v, a.mu_u, a.mu_v, a.y, a.out_v, a.n_dev, a.seg_t0, a.rec_map, a.J};
+  for (void* q : frees)
+    if (q) cudaFree(q);
+  sc_nb_set_output(h, o_int, o_nrec, o_rec, o_u, o_v, o_a, o_nout);
+  return rc;
+}
+
 extern "C" int sc_nb_status(sc_nb_newmark* h, int64_t* total_iters, int* max_iters, int* fsai_fallback_rows) {
   if (!h) return SC_BAD_ARG;
   int rc = check(cudaStreamSynchronize(h->user), "sync");
@@ -1296,8 +1809,13 @@ extern "C" int sc_nb_time_spmv(sc_nb_newmark* h, int reps, float* ms_per_launch,
   cudaGraphConditionalHandle none = 0;
   const unsigned nbk = h->node_blocks;
   auto launch = [&]() {
-    if (h->g.D == 3) k_spmv<3, false><<<nbk, kThreads, 0, st>>>(h->g, none);
-    else k_spmv<2, false><<<nbk, kThreads, 0, st>>>(h->g, none);
+    if (h->g.spmv_pair) {
+      if (h->g.D == 3) k_spmv_pair<3, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
+      else k_spmv_pair<2, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
+    } else {
+      if (h->g.D == 3) k_spmv<3, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
+      else k_spmv<2, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
+    }
   };
   launch();
   cudaEventRecord(e0, st);
@@ -1315,6 +1833,75 @@ extern "C" int sc_nb_time_spmv(sc_nb_newmark* h, int reps, float* ms_per_launch,
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  return rc;
+}
+
+// Operator application for testing and profiling: y = Op x in slot space, with
+// which = 0: A (the PCG operator), 1: K, 2: consistent mass (m_ab I blocks), 3: the
+// preconditioner G^T G, 4: the Lysmer dashpot matrix.  Synchronous.  Uses the solver's
+// scratch vectors (call between steps).
+__global__ void k_apply_blocks(Args g, const double* __restrict__ planes, int scalar, const double* __restrict__ x,
+                               double* __restrict__ y) {
+  const int D = g.D;
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < g.n_nodes;
+       row += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t sl = row >> 5;
+    const int64_t p0 = g.sf_ptr[sl] + (row & 31), W = (g.sf_ptr[sl + 1] - g.sf_ptr[sl]) >> 5;
+    double s[3] = {0, 0, 0};
+    for (int64_t j = 0; j < W; ++j) {
+      const int64_t pos = p0 + 32 * j;
+      const int64_t bs = (int64_t)g.sf_col[pos] * D;
+      for (int c = 0; c < D; ++c) {
+        if (scalar) s[c] += planes[pos] * x[bs + c];
+        else
+          for (int d = 0; d < D; ++d) s[c] += planes[(int64_t)(c * D + d) * g.sf_n + pos] * x[bs + d];
+      }
+    }
+    for (int c = 0; c < D; ++c) y[row * D + c] = s[c];
+  }
+}
+
+__global__ void k_apply_cab(Args g, const double* __restrict__ x, double* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int64_t k = g.cab_ptr[i]; k < g.cab_ptr[i + 1]; ++k) s += g.cab_val[k] * x[g.cab_col[k]];
+    y[i] = s;
+  }
+}
+
+__global__ void k_copy(int64_t n, const double* __restrict__ x, double* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = x[i];
+}
+
+extern "C" int sc_nb_apply(sc_nb_newmark* h, int which, const double* x, double* y) {
+  if (!h || !x || !y || which < 0 || which > 4) return SC_BAD_ARG;
+  Args g = h->g;
+  cudaStream_t st = h->user;
+  const unsigned nb = grid_for(g.n_nodes, 128, 152 * 64);
+  switch (which) {
+    case 0: k_apply_blocks<<<nb, 128, 0, st>>>(g, g.AS, 0, x, y); break;
+    case 1: k_apply_blocks<<<nb, 128, 0, st>>>(g, g.KS, 0, x, y); break;
+    case 2: k_apply_blocks<<<nb, 128, 0, st>>>(g, g.MSS, 1, x, y); break;
+    case 4: k_apply_cab<<<grid_for(g.n_s, 256), 256, 0, st>>>(g, x, y); break;
+    case 3: {
+      // r <- x, t = G r, z = G^T t (the solver's own kernels), y <- z
+      k_copy<<<grid_for(g.n_s, 256), 256, 0, st>>>(g.n_s, x, g.r);
+      cudaGraphConditionalHandle none = 0;
+      if (g.D == 3) {
+        k_prec_lower<3><<<h->node_blocks, kThreads, 0, st>>>(g);
+        k_prec_upper_nograph<3><<<h->node_blocks, kThreads, 0, st>>>(g);
+      } else {
+        k_prec_lower<2><<<h->node_blocks, kThreads, 0, st>>>(g);
+        k_prec_upper_nograph<2><<<h->node_blocks, kThreads, 0, st>>>(g);
+      }
+      (void)none;
+      k_copy<<<grid_for(g.n_s, 256), 256, 0, st>>>(g.n_s, g.z, y);
+      break;
+    }
+  }
+  int rc = check_launch("nb apply");
+  if (!rc) rc = check(cudaStreamSynchronize(st), "sync apply");
   return rc;
 }
 

@@ -180,3 +180,20 @@ def _table_dropping_zeros(ptr, eqs, vals, n_eq):
     step = np.repeat(np.arange(len(ptr) - 1), np.diff(ptr))
     counts = np.bincount(step[keep], minlength=len(ptr) - 1)
     return ForceTable(np.r_[0, np.cumsum(counts)], eqs[keep], vals[keep], n_eq)
+
+
+def ricker_table(model, node_id, amplitude, f0, t0, time, direction=1):
+    """Point load with a Ricker wavelet, amplitude * (1 - 2 (pi f0 (t - t0))^2) exp(-(pi f0 (t - t0))^2),
+    on one node's DOF ``direction`` (a supplied load history; not one of the reference's load
+    types, which the solver accepts as a force table)."""
+    ids = np.asarray(model.nodes)[:, 0].astype(np.int64)
+    idx = int(np.where(ids == int(node_id))[0][0])
+    eq = np.asarray(model.eq_nb_dof, dtype=float)[idx, direction]
+    if np.isnan(eq):
+        raise ValueError("Ricker load on a fixed DOF")
+    a = (np.pi * f0 * (np.asarray(time) - t0)) ** 2
+    vals = amplitude * (1 - 2 * a) * np.exp(-a)
+    n_t = len(time)
+    keep = vals != 0
+    ptr = np.r_[0, np.cumsum(keep.astype(np.int64))]
+    return ForceTable(ptr, np.full(int(keep.sum()), int(eq)), vals[keep], int(model.number_eq))

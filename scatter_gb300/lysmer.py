@@ -78,7 +78,7 @@ def boundary_faces(model, props, parameters_viscous):
     fe, fd = np.nonzero(cnt == nf)  # element-major, direction-minor = the reference's order
     n_face = len(fe)
     out = {"eqs": np.zeros((n_face, nf), np.int32), "xy": np.zeros((n_face, nf, 2)),
-           "fct": np.zeros((n_face, nf)), "fct2": np.zeros((n_face, nf))}
+           "fct": np.zeros((n_face, nf)), "fct2": np.zeros((n_face, nf)), "elem": fe.astype(np.int64)}
     if n_face == 0:
         return out
     # face nodes in element order

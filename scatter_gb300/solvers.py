@@ -153,7 +153,7 @@ class NodeBlockNewmark:
     State in slot space (slot = node * dim + dof); the eq <-> slot maps translate force
     entries, receivers and outputs from/to the reference's equation numbering."""
 
-    def __init__(self, g, dt, rtol=1e-12, max_iter=1000, precond="fsai"):
+    def __init__(self, g, dt, rtol=1e-12, max_iter=1000, precond="fsai", spmv="pair"):
         if g.adj_ptr is None:
             raise ValueError("GenerateMatrix has no node structure")
         self.g = g
@@ -201,6 +201,7 @@ class NodeBlockNewmark:
                  {"fsai": 0, "jacobi": 1}[precond], self.u.data_ptr(), self.v.data_ptr(), self.a.data_ptr(), self.ws.data_ptr(), wsb, dv.stream_ptr())
         self.h = h
         self.dt = dt
+        nat.call("sc_nb_set_options", self.h, {"pair": 0, "fp64": 1}[spmv])
 
     def set_force(self, table: ForceTable):
         eq = dv.to_dev(table.f_eq, torch.int64)
@@ -261,6 +262,15 @@ class NodeBlockNewmark:
         nat.call("sc_nb_time_spmv", self.h, int(reps), ctypes.byref(ms), ctypes.byref(by))
         return ms.value, by.value
 
+    def apply(self, which, x_eq):
+        """Op x for testing: x in the reference's equation numbering (host) -> Op x (host)."""
+        ops = {"A": 0, "K": 1, "M": 2, "P": 3, "Cabs": 4}
+        x = torch.zeros(self.n_s, dtype=torch.float64, device=self.u.device)
+        x[self.eq2slot] = dv.to_dev(np.asarray(x_eq, dtype=float), torch.float64)
+        y = torch.zeros_like(x)
+        nat.call("sc_nb_apply", self.h, ops[which], x.data_ptr(), y.data_ptr())
+        return dv.host(y[self.eq2slot])
+
     def run_explicit(self, t_begin, t_end):
         nat.call("sc_nb_explicit_run", self.h, int(t_begin), int(t_end))
 
@@ -292,9 +302,10 @@ class NodeBlockNewmark:
 class NewmarkExplicit:
     """GPU drop-in for PuggleSolvers' NewmarkExplicit as called by scatter/scatter.py:120-159."""
 
-    def __init__(self, rtol=1e-12, max_iter=1000, layout="node-block"):
+    def __init__(self, rtol=1e-12, max_iter=1000, layout="node-block", spmv="pair"):
         self.output_interval = 1
         self.layout = layout  # "node-block" (matrices from GenerateMatrix) or "csr"
+        self.spmv = spmv  # node-block PCG operator arithmetic: "pair" (FP32 pairs) or "fp64"
         self.update_rhs_at_time_step_func = None
         self.rtol = rtol
         self.max_iter = max_iter
@@ -334,21 +345,23 @@ class NewmarkExplicit:
                 table = ForceTable.from_callback(lambda t: F0, n_t, n)
         rec = np.arange(n) if self.receivers is None else np.asarray(self.receivers)
         n_out = len(range(0, n_t, self.output_interval))
-        attempts = ["fsai", "jacobi"] if (isinstance(M, GenerateMatrix) and self.layout == "node-block"
-                                          and M.adj_ptr is not None) else ["csr"]
+        attempts = ["fsai", "csr"] if (isinstance(M, GenerateMatrix) and self.layout == "node-block"
+                                       and M.adj_ptr is not None) else ["csr"]
         for kind in attempts:
             if kind == "csr":
                 solver = NewmarkGPU(pat, Md, Cd, Kd, dt, self.rtol, self.max_iter)
             else:
-                solver = NodeBlockNewmark(M, dt, self.rtol, self.max_iter, precond=kind)
+                solver = NodeBlockNewmark(M, dt, self.rtol, self.max_iter, precond=kind, spmv=self.spmv)
             solver.set_force(table)
             solver.set_output(self.output_interval, rec, n_out)
             solver.initial_acceleration()
             solver.run(t_start_idx, t_end_idx)
             rc, tot, mx = solver.status()
             self.preconditioner = kind
-            # the FP32 approximate inverse can lose positivity on nearly singular effective
-            # matrices (under-integrated quadratic tetrahedra at small dt): redo with Jacobi
+            # the node-block PCG stops with a breakdown status when A is not positive definite:
+            # the reference's tetra10 operators can make it so (its 4-point rule leaves the
+            # consistent mass singular, and its tri6 Lysmer dashpot matrix is indefinite).
+            # Redo the solve with the CSR FP64 loop, which runs the reference's iteration as is
             if rc == 3 and kind == "fsai":
                 solver.close()
                 continue

@@ -48,15 +48,11 @@ def element_properties(model, materials):
     for row in model.materials:
         names[int(row[1])] = str(row[2])
     mi = np.asarray(model.materials_index, dtype=np.int64)
-    uniq = np.unique(mi)
-    E = np.empty(len(mi))
-    nu = np.empty(len(mi))
-    rho = np.empty(len(mi))
-    for u in uniq:
-        m = materials[names[int(u)]]
-        sel = mi == u
-        E[sel], nu[sel], rho[sel] = m["Young"], m["poisson"], m["density"]
-    return E, nu, rho
+    uniq, inv = np.unique(mi, return_inverse=True)
+    table = np.array([[materials[names[int(u)]][k] for k in ("Young", "poisson", "density")] for u in uniq],
+                     dtype=float).reshape(-1, 3)
+    vals = table[inv.ravel()]
+    return vals[:, 0].copy(), vals[:, 1].copy(), vals[:, 2].copy()
 
 
 class DeviceCSR:
@@ -122,14 +118,17 @@ class GenerateMatrix:
         self.adj_ptr = self.adj = self.eqmap_d = None
 
     # -------------------------------------------------------------- element integration + assembly
-    def generate_stiffness_and_mass(self, data, material: dict) -> None:
-        """Element Ke/Me on the GPU, then deterministic CSR assembly (system_matrix.py:35-121)."""
+    def generate_stiffness_and_mass(self, data, material: dict, element_props=None) -> None:
+        """Element Ke/Me on the GPU, then deterministic CSR assembly (system_matrix.py:35-121).
+        element_props: optional per-element (E, nu, rho) arrays used instead of ``material``
+        (the per-element materials the reference's random-field path creates)."""
         dv.require_cuda()
         etype = str(data.element_type)
         dim = int(data.dimension)
         n_en = ELEM_NODES[etype]
         nodes, id2idx, elem_idx, eqmap = model_arrays(data)
-        E, nu, rho = element_properties(data, material)
+        E, nu, rho = element_properties(data, material) if element_props is None else \
+            tuple(np.asarray(x, dtype=float) for x in element_props)
         self.props = (E, nu, rho)
         n_elem, n_nodes = len(elem_idx), len(nodes)
         s = dv.stream_ptr()

@@ -147,3 +147,24 @@ def test_rayleigh_closed_form():
     assert abs(b - b_ref) <= 1e-12 * abs(b_ref)
     with pytest.raises(SystemExit):
         rayleigh_coefficients([1, 0.01, 1, 0.01])
+
+
+def test_tetra10_lysmer_indefinite():
+    """The reference's tetra10 dashpot matrix (tri6 faces with its face-node ordering) is
+    indefinite, unlike the tetra4 and hexa8 ones; with the singular tetra10 consistent mass of
+    its 4-point rule, the Newmark matrix M + dt/2 C + dt^2/4 K is then indefinite and the time
+    loop diverges in the reference as well as here.  Pinned on the reference's own matrices."""
+    import scipy.linalg as la
+
+    def min_eig(name):
+        C = golden_csr(npz(f"mat_{name}.npz"), "Cabs").toarray()
+        return la.eigvalsh(0.5 * (C + C.T))[0], np.abs(C).max()
+
+    lo, scale = min_eig("tetra10_abs")
+    assert lo < -0.1 * scale
+    for name in ("tetra4_abs", "column_hexa8_abs"):
+        lo, scale = min_eig(name)
+        assert lo >= -1e-12 * scale
+    # the oracle's own tetra10 dashpot matrix is the same one
+    model, spec, M, C, K, Ca, Ka = oracle_system("tetra10_abs")
+    assert abs(Ca - golden_csr(npz("mat_tetra10_abs.npz"), "Cabs")).max() <= 1e-14 * abs(Ca).max()
