@@ -92,6 +92,23 @@ int sc_node_adjacency(int n_nodes, int n_en, const int* elem, const int* inc_ptr
 int64_t sc_scan_work_size(int64_t n);
 int sc_exclusive_scan_i64(int64_t n, const int64_t* in, int64_t* out, int64_t* work, void* stream);
 
+/* The same scan without a workspace and without allocating (no counterpart in the
+ * reference, which has no device code).  For callers that must not allocate device memory:
+ * a host that keeps every byte of HBM for the solver's resident matrices and accounts for
+ * each allocation itself, or a binding (cgo, JNI, ctypes without torch) with no device
+ * allocator of its own; cudaMalloc/cudaFree can also synchronise the device mid-loop.  The
+ * tile sums go to one fixed 8 KB device array per device instead, so
+ *   - n is at most SC_SCAN_NOALLOC_MAX_N; larger n returns SC_CAPACITY (message in
+ *     sc_last_error) before any launch;
+ *   - the first call on a device looks up that array's address (cudaGetSymbolAddress) with
+ *     the device current; make that first call before any stream capture on the device;
+ *   - every call shares the array, which keeps what the last call wrote; nothing in it needs
+ *     to start at zero.  Calls whose work overlaps on the GPU (different streams, or another
+ *     host thread, without ordering between them) race on it: order them.
+ * It calls no cudaMalloc, cudaFree or allocating library routine. */
+#define SC_SCAN_NOALLOC_MAX_N 8388608LL
+int sc_exclusive_scan_i64_noalloc(int64_t n, const int64_t* in, int64_t* out, void* stream);
+
 /* Step 3: CSR rows over free DOFs.  eqmap [n_nodes][dim] (-1 = fixed).
  *   rowlen [n_eq] (pass: cols == NULL) then cols [nnz] using rowptr [n_eq+1]. */
 int sc_csr_pattern(int n_nodes, int dim, const int* eqmap, const int64_t* adj_ptr, const int* adj,

@@ -27,6 +27,7 @@ SIGNATURES = {
     "sc_node_adjacency": (I, [I, I, P, P, P, P, P, P, P]),
     "sc_scan_work_size": (L, [L]),
     "sc_exclusive_scan_i64": (I, [L, P, P, P, P]),
+    "sc_exclusive_scan_i64_noalloc": (I, [L, P, P, P]),
     "sc_csr_pattern": (I, [I, I, P, P, P, P, P, P, P]),
     "sc_assemble_values": (I, [I, I, I, P, P, P, P, P, P, P, P, P, P, P, P, P]),
     "sc_group_rows": (I, [I, I, P, I, P, P, P, P]),

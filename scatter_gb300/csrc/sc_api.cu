@@ -8,6 +8,7 @@ static thread_local char g_last_error[256] = "";
 void set_last_error(const char* where, cudaError_t e) {
   snprintf(g_last_error, sizeof(g_last_error), "%s: %s", where, cudaGetErrorString(e));
 }
+void set_last_message(const char* text) { snprintf(g_last_error, sizeof(g_last_error), "%s", text); }
 }  // namespace sc
 
 extern "C" int sc_version(void) { return 1; }

@@ -13,6 +13,10 @@
 //   4. values: one warp per node walks the node's elements in ascending order and adds
 //      each element's entries into the rows of that node, so every entry is the
 //      element-order sum the reference forms.
+#include <stdio.h>
+
+#include <mutex>
+
 #include "sc_common.cuh"
 
 namespace sc {
@@ -582,4 +586,66 @@ extern "C" int sc_combine(int64_t n, double c0, const double* x, double c1, cons
   if (n == 0) return SC_OK;
   k_combine<<<grid_for(n, 256, 152 * 32), 256, 0, (cudaStream_t)stream>>>(n, c0, x, c1, y, c2, z, out);
   return check_launch("k_combine");
+}
+
+// ------------------------------------------------------------------ scan without allocation
+// sc_exclusive_scan_i64_noalloc is the same three-kernel scan as sc_exclusive_scan_i64, for
+// callers that must not allocate device memory and cannot hand over a workspace: a host
+// whose device memory is all taken by the solver's resident matrices and that accounts for
+// every allocation itself, or a binding (cgo, JNI, ctypes without torch) that owns no device
+// allocator.  cudaMalloc and cudaFree can also synchronise the whole device, which such a
+// caller may not afford between the launches of a running time loop.  The tile sums live in
+// this file-scope device array instead; it exists once per device that loads the library.
+namespace {
+
+constexpr int64_t kNoAllocTiles = 1024;  // 8 KB of tile sums: n <= 1024 * 8192 = 8,388,608
+static_assert(kNoAllocTiles * kScanTile == SC_SCAN_NOALLOC_MAX_N, "header maximum out of date");
+static __device__ __align__(256) int64_t g_scan_tile_sums[kNoAllocTiles];
+
+constexpr int kNoAllocDevices = 64;
+std::mutex g_tile_sums_lock;
+int64_t* g_tile_sums_ptr[kNoAllocDevices] = {};
+
+// Address of the array on the current device, looked up on the first call per device.
+int tile_sums_on_current_device(int64_t** out) {
+  int dev = -1;
+  int rc = check(cudaGetDevice(&dev), "sc_exclusive_scan_i64_noalloc: current device");
+  if (rc) return rc;
+  if (dev < 0 || dev >= kNoAllocDevices) {
+    set_last_message("sc_exclusive_scan_i64_noalloc: device ordinal beyond the 64 this entry point tracks");
+    return SC_CAPACITY;
+  }
+  std::lock_guard<std::mutex> guard(g_tile_sums_lock);
+  if (!g_tile_sums_ptr[dev]) {
+    int64_t* ptr = nullptr;
+    rc = check(cudaGetSymbolAddress((void**)&ptr, g_scan_tile_sums), "sc_exclusive_scan_i64_noalloc: scratch address");
+    if (rc) return rc;
+    g_tile_sums_ptr[dev] = ptr;
+  }
+  *out = g_tile_sums_ptr[dev];
+  return SC_OK;
+}
+
+}  // namespace
+
+extern "C" int sc_exclusive_scan_i64_noalloc(int64_t n, const int64_t* in, int64_t* out, void* stream) {
+  if (n < 0 || !in || !out) return SC_BAD_ARG;
+  if (n > SC_SCAN_NOALLOC_MAX_N) {
+    char msg[160];
+    snprintf(msg, sizeof(msg), "sc_exclusive_scan_i64_noalloc: n = %lld exceeds the maximum of %lld values",
+             (long long)n, (long long)SC_SCAN_NOALLOC_MAX_N);
+    set_last_message(msg);
+    return SC_CAPACITY;
+  }
+  int64_t* tile_sums = nullptr;
+  int rc = tile_sums_on_current_device(&tile_sums);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  // Nothing in the array has to start at zero: every tile sum read below is written earlier
+  // in the same call, and the entries past this call's tiles (left by earlier calls) are not read.
+  const int64_t tiles = (n + kScanTile - 1) / kScanTile;
+  if (tiles > 0) k_scan_tiles<<<(unsigned)tiles, kScanThreads, 0, st>>>(n, in, out, tile_sums);
+  k_scan_sums<<<1, kScanThreads, 0, st>>>(tiles, tile_sums, out + n);  // also writes out[0] = 0 when n == 0
+  if (tiles > 0) k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, out, tile_sums);
+  return check_launch("sc_exclusive_scan_i64_noalloc");
 }

@@ -11,6 +11,8 @@ constexpr int kWarp = 32;
 
 // Records the last CUDA error text for sc_last_error().
 void set_last_error(const char* where, cudaError_t e);
+// Records a message (no CUDA error) for sc_last_error().
+void set_last_message(const char* text);
 
 inline int check_launch(const char* where) {
   cudaError_t e = cudaGetLastError();
