@@ -360,6 +360,7 @@ def batched_run(k, w, R=256):
                         SETTINGS["absorbing_BC_stiff"], DT)
     b.set_force(table)
     b.set_output(1, rec_eq, n_t)
+    rpt, tpb, tuned_ms = b.config()
     b.run(0, w)
     torch.cuda.synchronize()
     e0, e1 = _events()
@@ -396,6 +397,7 @@ def batched_run(k, w, R=256):
     return {"value": vb_rate, "unit": "DOF-steps/s", "single_solve": single, "speedup_vs_single": vb_rate / single,
             "realisations": R, "n_eq": n, "elements": n_el, "steps": k, "warmup": w, "ms_per_step": ms_b / k,
             "single_ms_per_step": ms_s / k, "rel_l2_vs_fp64_realisation0": rel,
+            "tuned_shape": {"realisations_per_thread": rpt, "threads_per_block": tpb, "tuned_ms": tuned_ms},
             "workload": "256 log-normal E realisations, box 40x20x10 m hexa8 0.5 m, Lysmer, Ricker 20 Hz, dt 5e-5",
             "single": "plain FP64 explicit GPU path (node-block graph), realisation 0, same steps"}
 
@@ -433,6 +435,8 @@ def adjoint_run(n_steps=4000, checkpoint=200, n_fd=20):
     p = A.prepare(E0, rho)
     p.forward()  # builds the explicit graphs
     s = p.solver
+    s.u.zero_()
+    s.v.zero_()
     torch.cuda.synchronize()
     e0, e1 = _events()
     e0.record()
@@ -440,11 +444,13 @@ def adjoint_run(n_steps=4000, checkpoint=200, n_fd=20):
     e1.record()
     torch.cuda.synchronize()
     ms_f = e0.elapsed_time(e1)
+    kernel_ms = s.time_explicit(20)  # the step kernel alone, back-to-back launches
     p.gradient(target)  # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     J, gE, gR = p.gradient(target)
     ms_a = (time.perf_counter() - t0) * 1e3
+    phases = p.timings()
     v0 = p.forward()
     p.close()
 
@@ -469,7 +475,9 @@ def adjoint_run(n_steps=4000, checkpoint=200, n_fd=20):
             err = abs(fd - grad[e]) / abs(grad[e])
             worst = max(worst, err)
             checks.append([kind, int(e), float(grad[e]), float(fd)])
-    return {"adjoint_over_forward": ms_a / ms_f, "forward_ms": ms_f, "gradient_ms": ms_a, "misfit": J,
+    return {"adjoint_over_forward": ms_a / ms_f, "forward_ms": ms_f, "gradient_ms": ms_a,
+            "gradient_phases_ms": {"forward_with_checkpoints": phases[0], "recompute": phases[1],
+                                   "backward": phases[2]}, "explicit_kernel_ms": kernel_ms, "misfit": J,
             "misfit_check": 0.5 * float(((v0[1:] - target[1:]) ** 2).sum()), "n_eq": int(m.number_eq),
             "elements": n_el, "steps": n_steps, "checkpoint": checkpoint, "fd_max_rel_err": worst, "fd_checks": len(checks),
             "timing": "forward: CUDA events around the explicit run; gradient: host wall clock around the whole "
@@ -594,11 +602,23 @@ def main():
     ap.add_argument("--dims", default="", help="nx,ny,nz of a smaller box (profiling cases)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-realisation batched measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost and FD measurement")
+    ap.add_argument("--section", default="all", choices=["all", "batched", "adjoint"],
+                    help="run one added workload alone and print its JSON (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.section != "all":
+        import torch
+
+        torch.cuda.set_device(0)
+        from scatter_gb300 import _native
+
+        _native.load()
+        out = batched_run(min(args.steps, 2990), args.warmup) if args.section == "batched" else \
+            adjoint_run(n_steps=args.steps, checkpoint=min(200, args.steps), n_fd=0 if args.no_cpu else 20)
+        print(json.dumps({"section": args.section, **out}))
     else:
         run_gb300(args)
 

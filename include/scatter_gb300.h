@@ -134,6 +134,10 @@ int sc_lysmer_values(int n_face, int nf, const int* eqs, const double* Fm, const
 /* out[i] = c0*x[i] + (c1*y[i] + c2*z[i]) for i < n (x, y or z may be NULL = 0).
  * Rayleigh: C = C_abs + (alpha M + beta K) (scatter/system_matrix.py:189-198);
  * Lysmer spring: K = K0 + K_abs / k_div (system_matrix.py:376). */
+/* out[r] = sum of row r of a CSR matrix (|values| when absolute != 0), summed in column order
+ * (deterministic): the row-sum lumped mass of the explicit scheme (no reference counterpart;
+ * the reference keeps the consistent mass, scatter/discretisation.py:203-222). */
+int sc_csr_row_sums(int64_t n, const int64_t* rowptr, const double* vals, int absolute, double* out, void* stream);
 int sc_combine(int64_t n, double c0, const double* x, double c1, const double* y, double c2, const double* z,
                double* out, void* stream);
 
@@ -245,12 +249,15 @@ int sc_nb_time_explicit(sc_nb_newmark* h, int reps, float* ms_per_step);
  * one CUDA graph per recompute step and per backward step; gradients accumulated per element
  * (deterministic).  Descriptor fields:
  *   elem [n_elem][n_en] node indices; ke_type [n_elem] -> ke1 [types][3 n_en][3 n_en] FP32
- *   unit-E element stiffness; young, rho [n_elem]; ml1 [n_elem][n_en][3] unit lumped mass
+ *   unit-E element stiffness; young, rho [n_elem]; ml1 [n_elem][n_en][3] FP32 unit lumped mass
  *   (free columns); l_eptr [n_elem+1], l_row, l_col (slots), l_c, l_s: the element's Lysmer
  *   dashpot and spring entries at the current parameters.  3D only.  grad_E, grad_rho [n_elem]
  *   device outputs; J_host may be NULL.  Allocates its checkpoint buffers (setup). */
 typedef struct sc_adj_desc sc_adj_desc;
 int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* desc, double* J_host, double* grad_E, double* grad_rho);
+/* device time of the last sc_nb_adjoint call's phases, ms: [0] forward with checkpoints,
+ * [1] recompute, [2] backward */
+int sc_nb_adjoint_timings(sc_nb_newmark* h, float* ms3);
 /* testing aid: y = Op x in slot space; which = 0: A, 1: K, 2: consistent mass, 3: the
  * preconditioner G^T G, 4: Lysmer dashpots.  Synchronous; call between steps. */
 int sc_nb_apply(sc_nb_newmark* h, int which, const double* x, double* y);
@@ -269,11 +276,20 @@ int sc_nb_destroy(sc_nb_newmark* h);
  *   ml [3 n_nodes] lumped mass; fixed [3 n_nodes]; alpha, beta Rayleigh; dt time step
  *   l_ptr [3 n_nodes + 1], l_col, l_elem, l_c, l_s: Lysmer entries per slot row: column slot,
  *     element whose E scales it, unit dashpot coefficient (x sqrt(E)), unit spring (x E)
- *   u, v [3 n_nodes][R] FP64 state.  Setup allocates the ping-pong copies; runs allocate nothing.
- * R <= 1024; n_en in {4, 8, 10, 20}. */
+ *   u, v [3 n_nodes][R] FP64 state, read at the start and written at the end of each run (the
+ *   step kernel accumulates in FP32 (hi, lo) pairs).  Setup allocates the ping-pong copies and
+ *   the pair accumulators; runs allocate nothing.
+ * R <= 1024 (above 256: even up to 512, else divisible by 4); n_en in {4, 8, 10, 20}. */
 typedef struct sc_batch_desc sc_batch_desc;
 typedef struct sc_batch sc_batch;
 int sc_batch_create(sc_batch** h, const sc_batch_desc* desc, double* u, double* v, void* stream);
+/* The step kernel's shape (realisations per thread, threads per block) is picked at create
+ * time by timing the candidates on scratch copies of the state (no reference counterpart);
+ * this reports the choice and its per-step time. */
+int sc_batch_config(sc_batch* h, int* realisations_per_thread, int* threads_per_block, float* ms_per_step);
+/* testing aid: force a shape (realisations per thread in {1, 2, 4, 8} dividing R, by 4 for 4
+ * and 8; threads per block a multiple of R / rpt, at most 256) */
+int sc_batch_set_shape(sc_batch* h, int realisations_per_thread, int threads_per_block);
 int sc_batch_set_force(sc_batch* h, int n_t, const int64_t* f_ptr, const int* f_slot, const double* f_val);
 /* receivers record v [n_out][n_rec][R] every out_interval steps */
 int sc_batch_set_output(sc_batch* h, int out_interval, int n_rec, const int* rec_slot, double* out_v, int64_t n_out);

@@ -33,6 +33,7 @@ SIGNATURES = {
     "sc_group_rows": (I, [I, I, P, I, P, P, P, P]),
     "sc_lysmer_values": (I, [I, I, P, P, P, P, I, P, P, P, P, P, P, P]),
     "sc_combine": (I, [L, D, P, D, P, D, P, P, P]),
+    "sc_csr_row_sums": (I, [L, P, P, I, P, P]),
     "sc_newmark_workspace_doubles": (L, [L, L]),
     "sc_newmark_create": (I, [ctypes.POINTER(P), L, P, P, P, P, P, P, D, D, I, P, P, P, P, L, P]),
     "sc_newmark_set_force": (I, [P, I, P, P, P]),
@@ -45,6 +46,8 @@ SIGNATURES = {
     "sc_rf_modes": (I, [ctypes.c_uint64, I, I, D, D, D, P, P]),
     "sc_rf_lognormal": (I, [I, P, I, I, P, D, D, P, P]),
     "sc_batch_create": (I, [ctypes.POINTER(P), P, P, P, P]),
+    "sc_batch_config": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(ctypes.c_float)]),
+    "sc_batch_set_shape": (I, [P, I, I]),
     "sc_batch_set_force": (I, [P, I, P, P, P]),
     "sc_batch_set_output": (I, [P, I, I, P, P, L]),
     "sc_batch_run": (I, [P, I, I]),
@@ -62,6 +65,7 @@ SIGNATURES = {
     "sc_nb_time_explicit": (I, [P, I, ctypes.POINTER(ctypes.c_float)]),
     "sc_nb_apply": (I, [P, I, P, P]),
     "sc_nb_adjoint": (I, [P, P, ctypes.POINTER(D), P, P]),
+    "sc_nb_adjoint_timings": (I, [P, ctypes.POINTER(ctypes.c_float)]),
     "sc_nb_destroy": (I, [P]),
 }
 

@@ -57,7 +57,7 @@ class ExplicitAdjoint:
         Me1 = dv.host(me).reshape(len(first), self.n_en, 3, self.n_en, 3)
         Mc = np.einsum("tacbc->tabc", Me1)  # [types, a, b, c]: component-c mass coupling
         free = (eqmap[elem_idx] >= 0).astype(float)  # [E, n_en, 3]
-        self.ml1 = dv.to_dev(np.einsum("eabc,ebc->eac", Mc[ktype], free), torch.float64)
+        self.ml1 = dv.to_dev(np.einsum("eabc,ebc->eac", Mc[ktype], free), torch.float32)
         self.elem = dv.to_dev(elem_idx, torch.int32)
 
     def _lysmer_entries(self, E, rho, eq2slot):
@@ -119,6 +119,8 @@ class _Prepared:
         """Receiver velocities [n_steps+1, n_rec] of the explicit scheme from rest (host)."""
         a = self.adj
         s = self.solver
+        s.u.zero_()
+        s.v.zero_()
         s.set_output(1, a.rec_eq, a.n_steps + 1, what=("v",))
         s.run_explicit(0, a.n_steps)
         return dv.host(s.out["v"]).reshape(a.n_steps + 1, len(a.rec_eq))
@@ -138,6 +140,12 @@ class _Prepared:
         J = ctypes.c_double()
         nat.call("sc_nb_adjoint", self.solver.h, ctypes.byref(d), ctypes.byref(J), gE.data_ptr(), gR.data_ptr())
         return J.value, dv.host(gE), dv.host(gR)
+
+    def timings(self):
+        """Device ms of the last gradient's phases: forward with checkpoints, recompute, backward."""
+        ms = (ctypes.c_float * 3)()
+        nat.call("sc_nb_adjoint_timings", self.solver.h, ms)
+        return tuple(float(x) for x in ms)
 
     def close(self):
         self.solver.close()

@@ -60,9 +60,8 @@ class BatchedExplicit:
         s = dv.stream_ptr()
         # lumped mass in slot space
         rp = g.pattern.rowptr
-        counts = (rp[1:] - rp[:-1]).long()
-        rows = torch.repeat_interleave(torch.arange(g.n_eq, device=rp.device), counts)
-        ml_eq = torch.zeros(g.n_eq, dtype=torch.float64, device=rp.device).index_add_(0, rows, g.M_d)
+        ml_eq = torch.empty(g.n_eq, dtype=torch.float64, device=rp.device)
+        nat.call("sc_csr_row_sums", g.n_eq, rp.data_ptr(), g.M_d.data_ptr(), 0, ml_eq.data_ptr(), s)
         em = torch.as_tensor(eqmap.reshape(-1), device=rp.device).long()
         free = em >= 0
         self.ml = torch.ones(3 * N, dtype=torch.float64, device=rp.device)
@@ -145,6 +144,16 @@ class BatchedExplicit:
         self.l_elem = dv.to_dev(el.astype(np.int32), torch.int32)
         self.l_c = dv.to_dev(c.astype(np.float32), torch.float32)
         self.l_s = dv.to_dev(sv.astype(np.float32), torch.float32)
+
+    def config(self):
+        """(realisations per thread, threads per block, tuned ms per step) of the step kernel."""
+        rpt, tpb, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        nat.call("sc_batch_config", self.h, ctypes.byref(rpt), ctypes.byref(tpb), ctypes.byref(ms))
+        return rpt.value, tpb.value, ms.value
+
+    def set_shape(self, realisations_per_thread, threads_per_block):
+        """Override the tuned kernel shape (testing aid)."""
+        nat.call("sc_batch_set_shape", self.h, int(realisations_per_thread), int(threads_per_block))
 
     def set_force(self, table: ForceTable):
         eq = dv.to_dev(table.f_eq, torch.int64)

@@ -580,6 +580,23 @@ extern "C" int sc_lysmer_values(int n_face, int nf, const int* eqs, const double
   return rc;
 }
 
+__global__ void k_row_sums(int64_t n, const int64_t* __restrict__ rowptr, const double* __restrict__ vals, int absolute,
+                           double* __restrict__ out) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) s += absolute ? fabs(vals[k]) : vals[k];
+    out[r] = s;
+  }
+}
+
+extern "C" int sc_csr_row_sums(int64_t n, const int64_t* rowptr, const double* vals, int absolute, double* out,
+                               void* stream) {
+  if (n < 0 || (n > 0 && (!rowptr || !vals || !out))) return SC_BAD_ARG;
+  if (n == 0) return SC_OK;
+  k_row_sums<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, rowptr, vals, absolute, out);
+  return check_launch("sc_csr_row_sums");
+}
+
 extern "C" int sc_combine(int64_t n, double c0, const double* x, double c1, const double* y, double c2,
                           const double* z, double* out, void* stream) {
   if (n < 0 || !out) return SC_BAD_ARG;

@@ -7,12 +7,15 @@
 // shared, and the Lysmer terms of scatter/system_matrix.py:362-376 scaled per realisation:
 // rho v_p, rho v_s grow as sqrt(E) (dashpots), E_c and G as E (springs).
 //
-// Layout: every per-realisation array is [slot or element][R] (realisation fastest), so the
-// R threads of a block (one per realisation) read and write 32-wide coalesced rows.  A block
-// takes one node at a time (grid-stride), gathers K1 blocks of the node's elements (shared
-// across threads, L1 broadcasts), scales by E_{e,r} and updates the node's DOFs.  u and v
-// are FP64 and updated in place (own node only); w = u + beta v and v are also kept as FP32
-// ping-pong copies that neighbours read.
+// Layout: every per-realisation array is [slot or element][R] (realisation fastest).  A node
+// is handled by ceil(R / RPT) threads, each owning RPT consecutive realisations: the node's
+// incident elements are walked once, each K1 entry (the same for every realisation, a
+// broadcast load) feeds RPT FMAs, and w, E, u, v are read as 8- to 32-byte vectors.  The
+// accumulators u and v are FP32 (hi, lo) pairs (about 48 significant bits) updated in place
+// (own node only): the step has no FP64 instruction, which on GB300 runs at 1/64 of the FP32
+// rate; the caller's FP64 u, v are converted in at the start of a run and out at its end.
+// w = u + beta v and v are also kept as FP32 ping-pong copies that neighbours read.  RPT and the nodes per block come from a short
+// timing of the candidates on scratch copies of the state when the handle is created.
 #include "sc_common.cuh"
 
 struct sc_batch_desc {
@@ -32,7 +35,10 @@ namespace bt {
 
 struct Args {
   sc_batch_desc d;
-  double *u, *v;
+  double *u, *v;        // the caller's FP64 state (converted at run start and end)
+  float2 *u2, *v2;      // the accumulators as (hi, lo) pairs, [slot][R]
+  const float *ml32, *iml32;  // lumped mass and its reciprocal, FP32
+  float dth, dtl, alpha32, beta32;  // dt as a pair; Rayleigh coefficients
   double* f;  // dense force, slot space (shared by the realisations)
   int* t;     // device step counter
   int n_t;
@@ -43,21 +49,109 @@ struct Args {
   const int* rec_map;  // slot -> receiver index or -1
   double* out_v;       // [n_out][n_rec][R]
   int64_t n_out;
+  unsigned* ticket;    // blocks finished in the current launch (last-block detection)
 };
 
-template <int NEN>
+template <int RPT>
+__device__ __forceinline__ void ldf(const float* p, float (&v)[RPT]) {
+  if constexpr (RPT % 4 == 0) {
+#pragma unroll
+    for (int q = 0; q < RPT / 4; ++q) {
+      const float4 a = __ldg(reinterpret_cast<const float4*>(p) + q);
+      v[4 * q] = a.x; v[4 * q + 1] = a.y; v[4 * q + 2] = a.z; v[4 * q + 3] = a.w;
+    }
+  } else if constexpr (RPT == 2) {
+    const float2 a = __ldg(reinterpret_cast<const float2*>(p));
+    v[0] = a.x; v[1] = a.y;
+  } else {
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) v[q] = __ldg(p + q);
+  }
+}
+template <int RPT>
+__device__ __forceinline__ void stf(float* p, const float (&v)[RPT]) {
+  if constexpr (RPT % 4 == 0) {
+#pragma unroll
+    for (int q = 0; q < RPT / 4; ++q)
+      reinterpret_cast<float4*>(p)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+  } else if constexpr (RPT == 2) {
+    *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) p[q] = v[q];
+  }
+}
+template <int RPT>
+__device__ __forceinline__ void ldp(const float2* p, float2 (&v)[RPT]) {
+  if constexpr (RPT % 2 == 0) {
+#pragma unroll
+    for (int q = 0; q < RPT / 2; ++q) {
+      const float4 a = reinterpret_cast<const float4*>(p)[q];
+      v[2 * q] = make_float2(a.x, a.y);
+      v[2 * q + 1] = make_float2(a.z, a.w);
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) v[q] = p[q];
+  }
+}
+template <int RPT>
+__device__ __forceinline__ void stp(float2* p, const float2 (&v)[RPT]) {
+  if constexpr (RPT % 2 == 0) {
+#pragma unroll
+    for (int q = 0; q < RPT / 2; ++q)
+      reinterpret_cast<float4*>(p)[q] = make_float4(v[2 * q].x, v[2 * q].y, v[2 * q + 1].x, v[2 * q + 1].y);
+  } else {
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) p[q] = v[q];
+  }
+}
+
+// x += a b + extra for a (hi, lo) pair x: the product split exactly with fmaf, the sum's
+// rounding error kept by two-sum, then renormalised (extra is below a b's last bit)
+__device__ __forceinline__ void pair_madd(float2& x, float a, float b, float extra) {
+  const float p = __fmul_rn(a, b);
+  const float pe = fmaf(a, b, -p);
+  const float t = __fadd_rn(x.x, p);
+  const float bp = __fsub_rn(t, x.x);
+  const float e = __fadd_rn(__fsub_rn(x.x, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  const float lo = __fadd_rn(x.y, __fadd_rn(e, __fadd_rn(pe, extra)));
+  const float h = __fadd_rn(t, lo);
+  x = make_float2(h, __fsub_rn(lo, __fsub_rn(h, t)));
+}
+
+__device__ inline bool batch_last_block(unsigned* ticket) {
+  __shared__ bool am_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) am_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  return am_last;
+}
+
+// One step for all realisations.  tpn threads per node (tpn * RPT >= R), blockDim / tpn
+// nodes per block.  The last block to finish advances the step counter and swaps the force
+// entries in f from step t to step t + 1 (every block has read f by then).
+template <int NEN, int RPT>
 __global__ void __launch_bounds__(256) k_batch_step(Args g, const float* __restrict__ w_in, float* __restrict__ w_out,
-                                                    const float* __restrict__ vf_in, float* __restrict__ vf_out) {
+                                                    const float* __restrict__ vf_in, float* __restrict__ vf_out,
+                                                    int tpn) {
   const sc_batch_desc& d = g.d;
   const int R = d.R;
-  const int r = threadIdx.x;
-  const bool active = r < R;
   constexpr int ND = NEN * 3;
+  const int npb = blockDim.x / tpn;
+  const int sub = threadIdx.x / tpn;
+  const int r0 = (threadIdx.x % tpn) * RPT;
+  const bool active = sub < npb && r0 < R;
   const int step = *g.t + 1;
   const bool rec_now = g.n_rec > 0 && g.out_interval > 0 && step % g.out_interval == 0 &&
                        step / g.out_interval < g.n_out;
-  for (int a = blockIdx.x; a < d.n_nodes; a += gridDim.x) {
-    float acc[3] = {0.f, 0.f, 0.f};
+  for (int a = blockIdx.x * npb + sub; active && a < d.n_nodes; a += gridDim.x * npb) {
+    float acc[3][RPT];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) acc[c][r] = 0.f;
     for (int k = d.inc_ptr[a]; k < d.inc_ptr[a + 1]; ++k) {
       const int e = d.inc[k];
       const int* en = d.elem + (int64_t)e * NEN;
@@ -66,78 +160,140 @@ __global__ void __launch_bounds__(256) k_batch_step(Args g, const float* __restr
       for (int q = 0; q < NEN; ++q)
         if (en[q] == a) la = q;
       const float* K1 = d.ke1 + (int64_t)d.ke_type[e] * ND * ND + (int64_t)(la * 3) * ND;
-      float t0 = 0.f, t1 = 0.f, t2 = 0.f;
-      if (active) {
-#pragma unroll 4
-        for (int lb = 0; lb < NEN; ++lb) {
-          const int64_t bs = (int64_t)en[lb] * 3;
-          const float w0 = w_in[(bs + 0) * R + r], w1 = w_in[(bs + 1) * R + r], w2 = w_in[(bs + 2) * R + r];
-          const float* kr = K1 + lb * 3;
-          t0 = fmaf(__ldg(kr + 0), w0, fmaf(__ldg(kr + 1), w1, fmaf(__ldg(kr + 2), w2, t0)));
-          t1 = fmaf(__ldg(kr + ND + 0), w0, fmaf(__ldg(kr + ND + 1), w1, fmaf(__ldg(kr + ND + 2), w2, t1)));
-          t2 = fmaf(__ldg(kr + 2 * ND + 0), w0, fmaf(__ldg(kr + 2 * ND + 1), w1, fmaf(__ldg(kr + 2 * ND + 2), w2, t2)));
+      float t[3][RPT];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) t[c][r] = 0.f;
+#pragma unroll 2
+      for (int lb = 0; lb < NEN; ++lb) {
+        const int64_t bs = (int64_t)en[lb] * 3;
+        float w0[RPT], w1[RPT], w2[RPT];
+        ldf<RPT>(w_in + (bs + 0) * R + r0, w0);
+        ldf<RPT>(w_in + (bs + 1) * R + r0, w1);
+        ldf<RPT>(w_in + (bs + 2) * R + r0, w2);
+        const float* kr = K1 + lb * 3;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float k0 = __ldg(kr + c * ND + 0), k1 = __ldg(kr + c * ND + 1), k2 = __ldg(kr + c * ND + 2);
+#pragma unroll
+          for (int r = 0; r < RPT; ++r) t[c][r] = fmaf(k0, w0[r], fmaf(k1, w1[r], fmaf(k2, w2[r], t[c][r])));
         }
-        const float Ee = d.young[(int64_t)e * R + r];
-        acc[0] = fmaf(Ee, t0, acc[0]);
-        acc[1] = fmaf(Ee, t1, acc[1]);
-        acc[2] = fmaf(Ee, t2, acc[2]);
       }
+      float Ee[RPT];
+      ldf<RPT>(d.young + (int64_t)e * R + r0, Ee);
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) acc[c][r] = fmaf(Ee[r], t[c][r], acc[c][r]);
     }
-    if (!active) continue;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const int64_t i = (int64_t)a * 3 + c;
-      const int64_t ir = i * R + r;
+      const int64_t ir = i * R + r0;
+      float wo[RPT], vo[RPT];
       if (d.fixed[i]) {
-        w_out[ir] = 0.f;
-        vf_out[ir] = 0.f;
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) wo[r] = vo[r] = 0.f;
+        stf<RPT>(w_out + ir, wo);
+        stf<RPT>(vf_out + ir, vo);
         continue;
       }
-      float spring = 0.f, dash = 0.f;
+      float spring[RPT], dash[RPT];
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) spring[r] = dash[r] = 0.f;
       for (int64_t q = d.l_ptr[i]; q < d.l_ptr[i + 1]; ++q) {
-        const int64_t jr = (int64_t)d.l_col[q] * R + r;
-        const float Eq = d.young[(int64_t)d.l_elem[q] * R + r];
-        spring = fmaf(d.l_s[q] * Eq, w_in[jr], spring);
-        dash = fmaf(d.l_c[q] * sqrtf(Eq), vf_in[jr], dash);
+        const int64_t jr = (int64_t)d.l_col[q] * R + r0;
+        float Eq[RPT], wj[RPT], vj[RPT];
+        ldf<RPT>(d.young + (int64_t)d.l_elem[q] * R + r0, Eq);
+        ldf<RPT>(w_in + jr, wj);
+        ldf<RPT>(vf_in + jr, vj);
+        const float ls = d.l_s[q], lc = d.l_c[q];
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) {
+          spring[r] = fmaf(__fmul_rn(ls, Eq[r]), wj[r], spring[r]);
+          dash[r] = fmaf(__fmul_rn(lc, sqrtf(Eq[r])), vj[r], dash[r]);
+        }
       }
-      const double vi = g.v[ir], ml = d.ml[i];
-      const double kw = (double)acc[c] + (double)spring;
-      const double accel = (g.f[i] - kw - d.alpha * ml * vi - (double)dash) / ml;
-      const double vn = fma(d.dt, accel, vi);
-      const double un = fma(d.dt, vn, g.u[ir]);
-      g.v[ir] = vn;
-      g.u[ir] = un;
-      w_out[ir] = (float)fma(d.beta, vn, un);
-      vf_out[ir] = (float)vn;
+      float2 vp[RPT], up[RPT];
+      float vown[RPT];
+      ldp<RPT>(g.v2 + ir, vp);
+      ldp<RPT>(g.u2 + ir, up);
+      ldf<RPT>(vf_in + ir, vown);
+      const float fi = (float)g.f[i], mlf = g.ml32[i], imlf = g.iml32[i];
+      const float aml = __fmul_rn(g.alpha32, mlf);
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) {
+        // FP32 acceleration (its inputs are FP32 products); _rn intrinsics keep the rounding
+        // the same for every kernel shape
+        const float kw = __fadd_rn(acc[c][r], spring[r]);
+        const float num = __fsub_rn(__fsub_rn(__fsub_rn(fi, kw), __fmul_rn(aml, vown[r])), dash[r]);
+        const float accel = __fmul_rn(num, imlf);
+        pair_madd(vp[r], g.dth, accel, __fmul_rn(g.dtl, accel));                           // v += dt a
+        pair_madd(up[r], g.dth, vp[r].x, fmaf(g.dth, vp[r].y, __fmul_rn(g.dtl, vp[r].x)));  // u += dt v
+        wo[r] = fmaf(g.beta32, vp[r].x, up[r].x);
+        vo[r] = vp[r].x;
+      }
+      stp<RPT>(g.v2 + ir, vp);
+      stp<RPT>(g.u2 + ir, up);
+      stf<RPT>(w_out + ir, wo);
+      stf<RPT>(vf_out + ir, vo);
       if (rec_now) {
         const int rj = g.rec_map[i];
-        if (rj >= 0) g.out_v[((int64_t)(step / g.out_interval) * g.n_rec + rj) * R + r] = vn;
+        if (rj >= 0) {
+          double* o = g.out_v + ((int64_t)(step / g.out_interval) * g.n_rec + rj) * R + r0;
+#pragma unroll
+          for (int r = 0; r < RPT; ++r) o[r] = (double)vp[r].x + (double)vp[r].y;
+        }
       }
+    }
+  }
+  if (batch_last_block(g.ticket)) {
+    const int t = step - 1;
+    if (g.f_ptr) {
+      if (t >= 0 && t < g.n_t)
+        for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f[g.f_slot[k]] = 0.0;
+      __syncthreads();
+      if (t + 1 < g.n_t)
+        for (int64_t k = g.f_ptr[t + 1] + threadIdx.x; k < g.f_ptr[t + 2]; k += blockDim.x) g.f[g.f_slot[k]] += g.f_val[k];
+    }
+    if (threadIdx.x == 0) {
+      *g.ticket = 0;
+      *g.t = step;
     }
   }
 }
 
-// advance the step counter and set the force of the new step (f holds step t's entries)
-__global__ void k_batch_force(Args g) {
-  __shared__ int t;
-  if (threadIdx.x == 0) t = *g.t + 1;
-  __syncthreads();
-  if (g.f_ptr) {
-    if (t - 1 >= 0 && t - 1 < g.n_t)
-      for (int64_t k = g.f_ptr[t - 1] + threadIdx.x; k < g.f_ptr[t]; k += blockDim.x) g.f[g.f_slot[k]] = 0.0;
-    __syncthreads();
-    if (t < g.n_t)
-      for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f[g.f_slot[k]] += g.f_val[k];
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) *g.t = t;
+__device__ inline float2 split2(double x) {
+  const float h = (float)x;
+  return make_float2(h, (float)(x - (double)h));
 }
 
+// run start: the caller's FP64 u, v into the pair accumulators and the FP32 copies
 __global__ void k_batch_init(Args g, float* w, float* vf) {
   const int64_t n = (int64_t)g.d.n_nodes * 3 * g.d.R;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-    w[q] = (float)fma(g.d.beta, g.v[q], g.u[q]);
-    vf[q] = (float)g.v[q];
+    const float2 u2 = split2(g.u[q]), v2 = split2(g.v[q]);
+    g.u2[q] = u2;
+    g.v2[q] = v2;
+    w[q] = fmaf(g.beta32, v2.x, u2.x);
+    vf[q] = v2.x;
+  }
+}
+
+// run end: the pair accumulators back into the caller's FP64 u, v
+__global__ void k_batch_final(Args g) {
+  const int64_t n = (int64_t)g.d.n_nodes * 3 * g.d.R;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    g.u[q] = (double)g.u2[q].x + (double)g.u2[q].y;
+    g.v[q] = (double)g.v2[q].x + (double)g.v2[q].y;
+  }
+}
+
+__global__ void k_batch_consts(int64_t n, const double* ml, float* ml32, float* iml32) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    ml32[q] = (float)ml[q];
+    iml32[q] = (float)(1.0 / ml[q]);
   }
 }
 
@@ -161,10 +317,14 @@ struct sc_batch {
   int* rec_map = nullptr;
   double* f = nullptr;
   int* t = nullptr;
+  unsigned* ticket = nullptr;
+  float2 *u2 = nullptr, *v2 = nullptr;
+  float *ml32 = nullptr, *iml32 = nullptr;
   cudaGraphExec_t exec[2] = {nullptr, nullptr};
   cudaGraph_t graph[2] = {nullptr, nullptr};
   unsigned blocks = 1;
-  int parity = 0;
+  int rpt = 1, threads = 32, tpn = 32;  // shape chosen by the tuner
+  float tuned_ms = 0.f;
 };
 
 static void batch_drop_graphs(sc_batch* h) {
@@ -174,22 +334,122 @@ static void batch_drop_graphs(sc_batch* h) {
   }
 }
 
+template <int NEN>
+static void launch_rpt(int rpt, unsigned blocks, int threads, int tpn, cudaStream_t st, const Args& g,
+                       const float* wi, float* wo, const float* vi, float* vo) {
+  switch (rpt) {
+    case 8: k_batch_step<NEN, 8><<<blocks, threads, 0, st>>>(g, wi, wo, vi, vo, tpn); break;
+    case 4: k_batch_step<NEN, 4><<<blocks, threads, 0, st>>>(g, wi, wo, vi, vo, tpn); break;
+    case 2: k_batch_step<NEN, 2><<<blocks, threads, 0, st>>>(g, wi, wo, vi, vo, tpn); break;
+    default: k_batch_step<NEN, 1><<<blocks, threads, 0, st>>>(g, wi, wo, vi, vo, tpn); break;
+  }
+}
+
+static void batch_launch(const sc_batch* h, const Args& g, int rpt, int threads, int tpn, cudaStream_t st,
+                         const float* wi, float* wo, const float* vi, float* vo) {
+  const int npb = threads / tpn;
+  const int64_t want = ((int64_t)g.d.n_nodes + npb - 1) / npb;
+  const unsigned blocks = (unsigned)(want < 152 * 32 ? want : 152 * 32);
+  switch (g.d.n_en) {
+    case 8: launch_rpt<8>(rpt, blocks, threads, tpn, st, g, wi, wo, vi, vo); break;
+    case 4: launch_rpt<4>(rpt, blocks, threads, tpn, st, g, wi, wo, vi, vo); break;
+    case 10: launch_rpt<10>(rpt, blocks, threads, tpn, st, g, wi, wo, vi, vo); break;
+    default: launch_rpt<20>(rpt, blocks, threads, tpn, st, g, wi, wo, vi, vo); break;
+  }
+}
+
+// Realisations per thread (1, 2, 4, 8; vector loads need R divisible by it, and by 4 for
+// 4 and 8) and threads per block (128, 256): each candidate advances scratch copies of the
+// state (no force, no receivers) 2 + 5 times, and the fastest of the 5 timed launches wins.
+// Every candidate performs the same operations in the same order per realisation, so the
+// choice changes the speed, not the results.
+static int batch_tune(sc_batch* h) {
+  const Args& g0 = h->g;
+  const int R = g0.d.R;
+  cudaStream_t st = h->user;
+  const int64_t nsr = (int64_t)g0.d.n_nodes * 3 * R;
+  double *u = nullptr, *v = nullptr;
+  float *w = nullptr, *vf = nullptr;
+  int* t = nullptr;
+  unsigned* tk = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = SC_OK;
+  float best = -1.f;
+  do {
+    if ((rc = check(cudaMallocAsync((void**)&u, 8 * nsr, st), "tune malloc")) ||
+        (rc = check(cudaMallocAsync((void**)&v, 8 * nsr, st), "tune malloc")) ||
+        (rc = check(cudaMallocAsync((void**)&w, 8 * nsr, st), "tune malloc")) ||
+        (rc = check(cudaMallocAsync((void**)&vf, 8 * nsr, st), "tune malloc")) ||
+        (rc = check(cudaMallocAsync((void**)&t, sizeof(int), st), "tune malloc")) ||
+        (rc = check(cudaMallocAsync((void**)&tk, sizeof(unsigned), st), "tune malloc")))
+      break;
+    cudaMemsetAsync(u, 0, 8 * nsr, st);
+    cudaMemsetAsync(v, 0, 8 * nsr, st);
+    cudaMemsetAsync(w, 0, 8 * nsr, st);
+    cudaMemsetAsync(vf, 0, 8 * nsr, st);
+    cudaMemsetAsync(t, 0, sizeof(int), st);
+    cudaMemsetAsync(tk, 0, sizeof(unsigned), st);
+    if ((rc = check(cudaEventCreate(&e0), "event")) || (rc = check(cudaEventCreate(&e1), "event"))) break;
+    Args g = g0;
+    g.u = u;
+    g.v = v;
+    g.u2 = reinterpret_cast<float2*>(u);  // zeros: valid pairs
+    g.v2 = reinterpret_cast<float2*>(v);
+    g.t = t;
+    g.ticket = tk;
+    g.f_ptr = nullptr;
+    g.n_rec = 0;
+    const int rpts[4] = {1, 2, 4, 8};
+    const int tpbs[2] = {128, 256};
+    for (int ri = 0; ri < 4 && !rc; ++ri) {
+      const int rpt = rpts[ri];
+      if (R % rpt != 0 || (rpt >= 4 && R % 4 != 0)) continue;
+      const int tpn = (R + rpt - 1) / rpt;
+      for (int bi = 0; bi < 2 && !rc; ++bi) {
+        if (tpn > tpbs[bi]) continue;
+        const int threads = (tpbs[bi] / tpn) * tpn;
+        float* wh = w;
+        float* wl = w + nsr;
+        float* vh = vf;
+        float* vl = vf + nsr;
+        for (int q = 0; q < 2; ++q) batch_launch(h, g, rpt, threads, tpn, st, wh, wl, vh, vl);
+        float ms_min = -1.f;
+        for (int q = 0; q < 5 && !rc; ++q) {
+          cudaEventRecord(e0, st);
+          batch_launch(h, g, rpt, threads, tpn, st, (q & 1) ? wl : wh, (q & 1) ? wh : wl, (q & 1) ? vl : vh,
+                       (q & 1) ? vh : vl);
+          cudaEventRecord(e1, st);
+          if ((rc = check_launch("batch tune"))) break;
+          if ((rc = check(cudaEventSynchronize(e1), "tune sync"))) break;
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          if (ms_min < 0.f || ms < ms_min) ms_min = ms;
+        }
+        if (!rc && (best < 0.f || ms_min < best)) {
+          best = ms_min;
+          h->rpt = rpt;
+          h->threads = threads;
+          h->tpn = tpn;
+        }
+      }
+    }
+  } while (0);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamSynchronize(st);
+  void* frees[] = {u, v, w, vf, t, tk};
+  for (void* q : frees)
+    if (q) cudaFree(q);
+  h->tuned_ms = best;
+  if (!rc && best < 0.f) rc = SC_BAD_ARG;  // no candidate fits (R > 2048)
+  return rc;
+}
+
 static int batch_build(sc_batch* h) {
   for (int k = 0; k < 2; ++k) {
     int rc = check(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal), "capture batch");
     if (rc) return rc;
-    const float* wi = h->w[k];
-    float* wo = h->w[k ^ 1];
-    const float* vi = h->vf[k];
-    float* vo = h->vf[k ^ 1];
-    const int threads = ((h->g.d.R + 31) / 32) * 32;
-    switch (h->g.d.n_en) {
-      case 8: k_batch_step<8><<<h->blocks, threads, 0, h->cap>>>(h->g, wi, wo, vi, vo); break;
-      case 4: k_batch_step<4><<<h->blocks, threads, 0, h->cap>>>(h->g, wi, wo, vi, vo); break;
-      case 10: k_batch_step<10><<<h->blocks, threads, 0, h->cap>>>(h->g, wi, wo, vi, vo); break;
-      default: k_batch_step<20><<<h->blocks, threads, 0, h->cap>>>(h->g, wi, wo, vi, vo); break;
-    }
-    k_batch_force<<<1, 256, 0, h->cap>>>(h->g);
+    batch_launch(h, h->g, h->rpt, h->threads, h->tpn, h->cap, h->w[k], h->w[k ^ 1], h->vf[k], h->vf[k ^ 1]);
     cudaGraph_t gr;
     if ((rc = check(cudaStreamEndCapture(h->cap, &gr), "end batch"))) return rc;
     if ((rc = check(cudaGraphInstantiate(&h->exec[k], gr, 0), "instantiate batch"))) {
@@ -207,6 +467,8 @@ extern "C" int sc_batch_create(sc_batch** out, const sc_batch_desc* d, double* u
     return SC_BAD_ARG;
   if (d->n_en != 8 && d->n_en != 4 && d->n_en != 10 && d->n_en != 20) return SC_BAD_ARG;
   if (!(d->dt > 0)) return SC_BAD_ARG;
+  // at most 256 threads per node: R > 256 needs 2 (R <= 512) or 4 realisations per thread
+  if (d->R > 256 && !(d->R % 4 == 0 || (d->R <= 512 && d->R % 2 == 0))) return SC_BAD_ARG;
   sc_batch* h = new sc_batch();
   h->user = (cudaStream_t)stream;
   h->g = Args{};
@@ -226,13 +488,29 @@ extern "C" int sc_batch_create(sc_batch** out, const sc_batch_desc* d, double* u
     if ((rc = check(cudaMallocAsync((void**)&h->rec_map, 4 * ns, st), "malloc"))) break;
     if ((rc = check(cudaMallocAsync((void**)&h->f, 8 * ns, st), "malloc"))) break;
     if ((rc = check(cudaMallocAsync((void**)&h->t, sizeof(int), st), "malloc"))) break;
+    if ((rc = check(cudaMallocAsync((void**)&h->ticket, sizeof(unsigned), st), "malloc"))) break;
+    if ((rc = check(cudaMallocAsync((void**)&h->u2, 8 * nsr, st), "malloc"))) break;
+    if ((rc = check(cudaMallocAsync((void**)&h->v2, 8 * nsr, st), "malloc"))) break;
+    if ((rc = check(cudaMallocAsync((void**)&h->ml32, 4 * ns, st), "malloc"))) break;
+    if ((rc = check(cudaMallocAsync((void**)&h->iml32, 4 * ns, st), "malloc"))) break;
+    k_batch_consts<<<grid_for(ns, 256), 256, 0, st>>>(ns, d->ml, h->ml32, h->iml32);
+    h->g.u2 = h->u2;
+    h->g.v2 = h->v2;
+    h->g.ml32 = h->ml32;
+    h->g.iml32 = h->iml32;
+    h->g.dth = (float)d->dt;
+    h->g.dtl = (float)(d->dt - (double)h->g.dth);
+    h->g.alpha32 = (float)d->alpha;
+    h->g.beta32 = (float)d->beta;
     cudaMemsetAsync(h->rec_map, 0xff, 4 * ns, st);
     cudaMemsetAsync(h->f, 0, 8 * ns, st);
     cudaMemsetAsync(h->t, 0, sizeof(int), st);
+    cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), st);
     h->g.f = h->f;
     h->g.t = h->t;
+    h->g.ticket = h->ticket;
     h->g.rec_map = h->rec_map;
-    h->blocks = (unsigned)(d->n_nodes < 152 * 16 ? d->n_nodes : 152 * 16);
+    if ((rc = batch_tune(h))) break;
     rc = check(cudaStreamSynchronize(st), "sync");
   } while (0);
   if (rc) {
@@ -240,6 +518,28 @@ extern "C" int sc_batch_create(sc_batch** out, const sc_batch_desc* d, double* u
     return rc;
   }
   *out = h;
+  return SC_OK;
+}
+
+extern "C" int sc_batch_set_shape(sc_batch* h, int realisations_per_thread, int threads_per_block) {
+  if (!h) return SC_BAD_ARG;
+  const int R = h->g.d.R, rpt = realisations_per_thread;
+  if (rpt != 1 && rpt != 2 && rpt != 4 && rpt != 8) return SC_BAD_ARG;
+  if (R % rpt != 0 || (rpt >= 4 && R % 4 != 0)) return SC_BAD_ARG;
+  const int tpn = (R + rpt - 1) / rpt;
+  if (threads_per_block < tpn || threads_per_block > 256 || threads_per_block % tpn != 0) return SC_BAD_ARG;
+  h->rpt = rpt;
+  h->threads = threads_per_block;
+  h->tpn = tpn;
+  batch_drop_graphs(h);
+  return SC_OK;
+}
+
+extern "C" int sc_batch_config(sc_batch* h, int* realisations_per_thread, int* threads_per_block, float* ms_per_step) {
+  if (!h) return SC_BAD_ARG;
+  if (realisations_per_thread) *realisations_per_thread = h->rpt;
+  if (threads_per_block) *threads_per_block = h->threads;
+  if (ms_per_step) *ms_per_step = h->tuned_ms;
   return SC_OK;
 }
 
@@ -286,7 +586,8 @@ extern "C" int sc_batch_run(sc_batch* h, int t_begin, int t_end) {
   int k = 0;
   for (int t = t_begin; t < t_end; ++t, k ^= 1)
     if ((rc = check(cudaGraphLaunch(h->exec[k], st), "batch launch"))) return rc;
-  return SC_OK;
+  k_batch_final<<<grid_for((int64_t)h->g.d.n_nodes * 3 * h->g.d.R, 256, 152 * 32), 256, 0, st>>>(h->g);
+  return check_launch("batch final");
 }
 
 extern "C" int sc_batch_destroy(sc_batch* h) {
@@ -300,6 +601,10 @@ extern "C" int sc_batch_destroy(sc_batch* h) {
   if (h->rec_map) cudaFree(h->rec_map);
   if (h->f) cudaFree(h->f);
   if (h->t) cudaFree(h->t);
+  if (h->ticket) cudaFree(h->ticket);
+  void* more[] = {h->u2, h->v2, h->ml32, h->iml32};
+  for (void* q : more)
+    if (q) cudaFree(q);
   if (h->cap) cudaStreamDestroy(h->cap);
   delete h;
   return SC_OK;

@@ -13,6 +13,7 @@ type of ``NewmarkExplicit``; the velocity reported at step n+1 is v_{n+1/2}.
 import numpy as np
 import torch
 
+from . import _native as nat
 from . import device as dv
 from .solvers import ForceTable, NodeBlockNewmark
 from .system_matrix import GenerateMatrix
@@ -22,10 +23,10 @@ def critical_time_step(g: GenerateMatrix):
     """2 / omega_max with omega_max^2 bounded by Gershgorin on M_L^-1 K (a lower bound on the
     true CFL limit of the lumped scheme)."""
     rp = g.pattern.rowptr
-    counts = (rp[1:] - rp[:-1]).long()
-    rows = torch.repeat_interleave(torch.arange(g.n_eq, device=rp.device), counts)
-    ml = torch.zeros(g.n_eq, dtype=torch.float64, device=rp.device).index_add_(0, rows, g.M_d)
-    ka = torch.zeros(g.n_eq, dtype=torch.float64, device=rp.device).index_add_(0, rows, g.K_d.abs())
+    ml = torch.empty(g.n_eq, dtype=torch.float64, device=rp.device)
+    ka = torch.empty(g.n_eq, dtype=torch.float64, device=rp.device)
+    nat.call("sc_csr_row_sums", g.n_eq, rp.data_ptr(), g.M_d.data_ptr(), 0, ml.data_ptr(), dv.stream_ptr())
+    nat.call("sc_csr_row_sums", g.n_eq, rp.data_ptr(), g.K_d.data_ptr(), 1, ka.data_ptr(), dv.stream_ptr())
     bound = float((ka / ml).max().item())
     if float(ml.min().item()) <= 0:
         raise ValueError("lumped mass has non-positive entries (row-sum lumping of this element type)")
@@ -33,7 +34,8 @@ def critical_time_step(g: GenerateMatrix):
 
 
 class ExplicitLumped:
-    def __init__(self, check_cfl=True):
+    def __init__(self, check_cfl=True, arithmetic="pair"):
+        self.arithmetic = arithmetic  # K w products: "pair" (FP32 pairs) or "fp64"
         self.output_interval = 1
         self.update_rhs_at_time_step_func = None
         self.force_table = None
@@ -66,7 +68,7 @@ class ExplicitLumped:
         if table is None:
             func = self.update_rhs_at_time_step_func or (lambda t: F)
             table = ForceTable.from_callback(func, n_t, g.n_eq)
-        s = NodeBlockNewmark(g, dt)
+        s = NodeBlockNewmark(g, dt, explicit=self.arithmetic)
         s.set_force(table)
         rec = np.arange(g.n_eq) if self.receivers is None else np.asarray(self.receivers)
         n_out = len(range(0, n_t, self.output_interval))

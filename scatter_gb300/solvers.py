@@ -153,7 +153,7 @@ class NodeBlockNewmark:
     State in slot space (slot = node * dim + dof); the eq <-> slot maps translate force
     entries, receivers and outputs from/to the reference's equation numbering."""
 
-    def __init__(self, g, dt, rtol=1e-12, max_iter=1000, precond="fsai", spmv="pair"):
+    def __init__(self, g, dt, rtol=1e-12, max_iter=1000, precond="fsai", spmv="pair", explicit="pair"):
         if g.adj_ptr is None:
             raise ValueError("GenerateMatrix has no node structure")
         self.g = g
@@ -201,7 +201,8 @@ class NodeBlockNewmark:
                  {"fsai": 0, "jacobi": 1}[precond], self.u.data_ptr(), self.v.data_ptr(), self.a.data_ptr(), self.ws.data_ptr(), wsb, dv.stream_ptr())
         self.h = h
         self.dt = dt
-        nat.call("sc_nb_set_options", self.h, {"pair": 0, "fp64": 1}[spmv])
+        # bit 0: PCG SpMV in FP64 instead of FP32 pairs; bit 1: explicit K w in FP64
+        nat.call("sc_nb_set_options", self.h, {"pair": 0, "fp64": 1}[spmv] | {"pair": 0, "fp64": 2}[explicit])
 
     def set_force(self, table: ForceTable):
         eq = dv.to_dev(table.f_eq, torch.int64)

@@ -39,9 +39,10 @@ def test_adjoint_matches_oracle(run):
     gpu, (J, gE, gR), _ = run
     _, (Jg, gEg, gRg) = gpu(case.CHECKPOINT)
     assert abs(Jg - J) <= 1e-10 * J
-    # dJ/dE: element products in FP32 (after removing rigid translations); Lysmer part FP64
+    # element products in FP32 (after removing rigid translations), per-element sums and the
+    # Lysmer parts in FP64
     assert rel_l2(gEg, gE) <= 1e-5
-    assert rel_l2(gRg, gR) <= 1e-9
+    assert rel_l2(gRg, gR) <= 1e-5
 
 
 def test_adjoint_repeatable_and_checkpoint_independent(run):

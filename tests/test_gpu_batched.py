@@ -89,3 +89,34 @@ def test_batched_matches_per_realisation_fp64(cuda):
         s.calculate(g, g, g, None, 0, n_t - 1)
         assert rel_l2(vb[:, :, r], s.v[:, rec]) <= 1e-5
         assert rel_l2(ub[r], s.u[-1]) <= 1e-5
+
+
+def test_batched_shapes_agree_bitwise(cuda):
+    """Every kernel shape the tuner may pick (realisations per thread, threads per block)
+    gives bitwise the same histories: the per-realisation arithmetic is the same."""
+    from scatter_gb300 import meshgen
+    from scatter_gb300.batched import BatchedExplicit
+    from scatter_gb300.force_external import ricker_table
+    from scatter_gb300.random_fields import element_centroids, lognormal_fields
+
+    m = meshgen.box_model(6, 4, 3, 0.5, bottom="020", x_faces="200", z_faces="002")
+    R = 8
+    young = lognormal_fields(element_centroids(m), seed=5, R=R, lengths=(5.0, 1.0, 5.0), mean=50e6, sd=12.5e6)
+    dt, n_t = 5e-5, 120
+    time = np.linspace(0, dt * (n_t - 1), n_t)
+    top = m.top_nodes()
+    table = ricker_table(m, int(top[len(top) // 2]), -1e4, 20.0, 0.002, time)
+    rec = [int(m.eq_nb_dof[m.node_index()[n], 1]) for n in top[::5]]
+    results = []
+    for rpt, tpb in ((1, 128), (1, 256), (2, 128), (4, 256), (8, 128)):
+        b = BatchedExplicit(m, young, 0.3, 1900.0, [1, 0.02, 50, 0.02], [1, 1], 1e3, dt)
+        b.set_shape(rpt, tpb)
+        b.set_force(table)
+        b.set_output(1, rec, n_t)
+        b.run(0, n_t - 1)
+        results.append((b.velocities(), b.state()[0]))
+        b.close()
+    assert np.abs(results[0][0]).max() > 0
+    for vb, ub in results[1:]:
+        np.testing.assert_array_equal(vb, results[0][0])
+        np.testing.assert_array_equal(ub, results[0][1])

@@ -304,9 +304,11 @@ def test_node_block_and_csr_agree_and_repeat(torch_cuda):
     assert rel_l2(a.u, c.u) <= 1e-10
 
 
-@pytest.mark.parametrize("name", ["column_hexa8_pulse", "cube_abs5"])
-def test_explicit_vs_oracle(torch_cuda, name):
-    """Explicit lumped-mass scheme: GPU fused step vs oracle/explicit.py (FP64)."""
+@pytest.mark.parametrize("name,arithmetic", [("column_hexa8_pulse", "pair"), ("cube_abs5", "pair"),
+                                             ("cube_abs5", "fp64")])
+def test_explicit_vs_oracle(torch_cuda, name, arithmetic):
+    """Explicit lumped-mass scheme: GPU fused step (K w in FP32 pairs or FP64) vs
+    oracle/explicit.py (FP64)."""
     from oracle import explicit, loads
     from scatter_gb300.explicit import ExplicitLumped, critical_time_step
     from scatter_gb300.solvers import ForceTable
@@ -320,7 +322,7 @@ def test_explicit_vs_oracle(torch_cuda, name):
     F = loads.table(load, time, model) if load["type"] != "moving" else None
     if F is None:
         pytest.skip("moving load table needs the golden time grid")
-    s = ExplicitLumped()
+    s = ExplicitLumped(arithmetic=arithmetic)
     s.initialise(ns.number_eq, time)
     s.force_table = ForceTable.from_dense(F)
     s.calculate(g, g, g, F[0], 0, n_t - 1)
