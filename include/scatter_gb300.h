@@ -219,7 +219,9 @@ int sc_nb_create(sc_nb_newmark** h, int n_nodes, int dim, const int* eqmap, cons
                  double* a, void* workspace, int64_t workspace_bytes, void* stream);
 /* options bit 0: run the PCG SpMV in FP64 instead of the default FP32-pair arithmetic
  * (A as hi + lo FP32 pairs, exact TwoProd/TwoSum accumulation, ~2^-46 relative per product;
- * the residual, dot products and state stay FP64). */
+ * the residual, dot products and state stay FP64).  bit 1: run the explicit scheme in FP64
+ * instead of its default FP32-pair state and products (sc_nb_explicit_run); the adjoint needs
+ * the default. */
 int sc_nb_set_options(sc_nb_newmark* h, int options);
 int sc_nb_set_force(sc_nb_newmark* h, int n_t, const int64_t* f_ptr, const int* f_slot, const double* f_val);
 int sc_nb_set_output(sc_nb_newmark* h, int out_interval, int n_rec, const int* rec_slot, double* out_u,
@@ -233,10 +235,18 @@ int sc_nb_time_spmv(sc_nb_newmark* h, int reps, float* ms_per_launch, int64_t* b
  * reference's mass is always consistent):
  *   a_n = M_L^-1 (f_n - K (u_n + beta v_{n-1/2}) - alpha M_L v_{n-1/2} - Cabs v_{n-1/2}),
  *   v_{n+1/2} = v_{n-1/2} + dt a_n,  u_{n+1} = u_n + dt v_{n+1/2},
- * M_L the row-sum lumped mass; one fused kernel per step over the sliced-ELL K.  Receivers
- * record u_{n+1} and v_{n+1/2}.  Conditionally stable (dt below the lumped-mass CFL limit).
- * The first call allocates the scheme's extra vectors (setup); later calls allocate nothing. */
+ * M_L the row-sum lumped mass (or sc_nb_set_lumped_mass); one fused kernel per step over the
+ * sliced-ELL K.  By default u, v, w, the force and the mass terms are FP32 (hi, lo) pairs
+ * (~48 significant bits, no FP64 instruction in the step; the FP64 u, v are split at the start
+ * and joined at the end of a run).  Receivers record u_{n+1} and v_{n+1/2}.  Conditionally
+ * stable (dt below the lumped-mass CFL limit).  The first call allocates the scheme's extra
+ * vectors (setup); later calls allocate nothing. */
 int sc_nb_explicit_run(sc_nb_newmark* h, int t_begin, int t_end);
+/* The explicit scheme's lumped mass set by the caller (slot space, FP64, device; fixed slots
+ * ignored), e.g. a diagonal-scaled mass for element types whose consistent-mass row sums are
+ * not positive (the reference's 4-point tetra10 mass has negative corner row sums).  No
+ * reference counterpart. */
+int sc_nb_set_lumped_mass(sc_nb_newmark* h, const double* ml);
 /* timing aid: the explicit step kernel alone, `reps` launches between CUDA events */
 int sc_nb_time_explicit(sc_nb_newmark* h, int reps, float* ms_per_step);
 /* Adjoint of the explicit scheme (no reference counterpart): misfit
@@ -250,8 +260,8 @@ int sc_nb_time_explicit(sc_nb_newmark* h, int reps, float* ms_per_step);
  * (deterministic).  Descriptor fields:
  *   elem [n_elem][n_en] node indices; ke_type [n_elem] -> ke1 [types][3 n_en][3 n_en] FP32
  *   unit-E element stiffness; young, rho [n_elem]; ml1 [n_elem][n_en][3] FP32 unit lumped mass
- *   (free columns); l_eptr [n_elem+1], l_row, l_col (slots), l_c, l_s: the element's Lysmer
- *   dashpot and spring entries at the current parameters.  3D only.  grad_E, grad_rho [n_elem]
+ *   (free columns); l_eptr [n_elem+1], l_row, l_col (slots), l_c, l_s (FP32): the element's
+ *   Lysmer dashpot and spring entries at the current parameters.  3D only.  grad_E, grad_rho [n_elem]
  *   device outputs; J_host may be NULL.  Allocates its checkpoint buffers (setup). */
 typedef struct sc_adj_desc sc_adj_desc;
 int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* desc, double* J_host, double* grad_E, double* grad_rho);

@@ -62,6 +62,7 @@ SIGNATURES = {
     "sc_nb_status": (I, [P, ctypes.POINTER(L), ctypes.POINTER(I), ctypes.POINTER(I)]),
     "sc_nb_time_spmv": (I, [P, I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(L)]),
     "sc_nb_explicit_run": (I, [P, I, I]),
+    "sc_nb_set_lumped_mass": (I, [P, P]),
     "sc_nb_time_explicit": (I, [P, I, ctypes.POINTER(ctypes.c_float)]),
     "sc_nb_apply": (I, [P, I, P, P]),
     "sc_nb_adjoint": (I, [P, P, ctypes.POINTER(D), P, P]),

@@ -111,8 +111,8 @@ class _Prepared:
         eptr, lr, lcol, lc, ls = adj._lysmer_entries(E, rho, e2s)
         self.rec = dv.to_dev(e2s[adj.rec_eq].astype(np.int32), torch.int32)
         self._keep = [dv.to_dev(x, t) for x, t in ((E, torch.float64), (rho, torch.float64), (eptr, torch.int64),
-                                                    (lr, torch.int32), (lcol, torch.int32), (lc, torch.float64),
-                                                    (ls, torch.float64))]
+                                                    (lr, torch.int32), (lcol, torch.int32), (lc, torch.float32),
+                                                    (ls, torch.float32))]
         self.n_elem = len(E)
 
     def forward(self):

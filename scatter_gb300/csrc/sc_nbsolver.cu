@@ -25,105 +25,10 @@
 
 #include <vector>
 
-#include "sc_common.cuh"
+#include "sc_nb.cuh"
 
 namespace sc {
 namespace nb {
-
-constexpr int kThreads = 256;
-constexpr int kMaxFsai = 64;  // FSAI row pattern capacity (slots); larger rows fall back to Jacobi
-
-struct Scal {
-  double rz, pw, rr, bb, alpha, beta, tol2, pad0;
-  long long total_iters;
-  int it, max_it, max_seen, status, t, fsai_fallback;
-  unsigned int ticket;
-  int hist;  // valid previous accelerations (0..2) for the warm start
-  int done;  // eager mode: set when the PCG loop should stop
-  unsigned int pad2[1];
-};
-
-struct Args {
-  int n_nodes, D;
-  int64_t n_s;  // slots
-  int64_t nnzb;
-  const int64_t* adj_ptr;
-  const int* adj;
-  const int64_t* diag;  // position of the node itself in its adjacency row
-  const int* fixed;     // [n_s] 1 = fixed slot
-  const double *KB, *AB, *MS;
-  const float *GB, *GTB;
-  const int64_t* cab_ptr;
-  const int* cab_col;
-  const double* cab_val;
-  // sliced-ELL copies used by the per-step kernels (32 node rows per slice, column-major):
-  // full pattern (K, A, M), lower (G), upper (G^T)
-  int64_t n_slices;
-  const int64_t *sf_ptr, *sl_ptr, *su_ptr;
-  const int *sf_col, *sl_col, *su_col;
-  int64_t sf_n, sl_n, su_n;
-  const double *KS, *AS, *MSS;
-  const float *GS, *GTS;
-  const float2* APS;       // A as FP32 (hi, lo) pairs (hi + lo = A to 48 bits) for the pair-arithmetic SpMV
-  const float2* KPS;       // K as FP32 pairs, for the explicit step and the adjoint (built on first use)
-  float2* p2;              // p as (hi, lo) FP32 pairs, written with p
-  int spmv_pair;           // 1: PCG SpMV in FP32-pair arithmetic, 0: FP64
-  int keep_l2;             // 1: matrix planes fit in L2, loaded with the default (keep) policy;
-                           // 0: streamed with evict-first loads
-  double alpha_r, beta_r;  // Rayleigh coefficients
-  double aM, aK, aC;       // A = aM M + aK K + aC Cabs
-  double dt;
-  double *u, *v, *a, *a1, *a2;
-  double *q1, *q2, *y1, *x0, *x, *r, *z, *p, *w, *f;
-  float* t32;
-  double* part;
-  Scal* s;
-  // force (slot indices)
-  int n_t;
-  const int64_t* f_ptr;
-  const int* f_slot;
-  const double* f_val;
-  // output
-  int out_interval, n_rec;
-  const int* rec_slot;
-  double *out_u, *out_v, *out_a;
-  int64_t n_out;
-};
-
-__device__ inline bool last_block(unsigned int* ticket) {
-  __shared__ bool am_last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) am_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
-  __syncthreads();
-  return am_last;
-}
-
-// kMode 0: inside the step graph (drives the WHILE conditional); 1: eager launches (the host
-// reads Scal::done); 2: standalone timing launch (no solver scalars touched)
-template <int kMode>
-__device__ inline void pcg_continue(cudaGraphConditionalHandle hc, Scal* s, bool go) {
-  if (kMode == 0) cudaGraphSetConditional(hc, go ? 1u : 0u);
-  else if (kMode == 1) s->done = go ? 0 : 1;
-}
-
-__device__ inline double reduce_parts(const double* part, int k, double* sh) {
-  double s = 0.0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(part + b * 4 + k);
-  return block_sum(s, sh);
-}
-
-template <int D>
-__device__ inline void warp_sum3(double* s) {
-#pragma unroll
-  for (int c = 0; c < D; ++c) s[c] = warp_sum(s[c]);
-}
-
-// (hi, lo) FP32 pair of a double: hi + lo reproduces x to 48 bits
-__device__ inline float2 split_pair(double x) {
-  const float hi = (float)x;
-  return make_float2(hi, (float)(x - (double)hi));
-}
 
 // ------------------------------------------------------------------ per-step kernels
 __global__ void k_force(Args g) {
@@ -161,107 +66,6 @@ __global__ void k_predict(Args g) {
     g.x0[i] = x0;
     if (g.spmv_pair) g.p2[i] = split_pair(x0);  // p2 is scratch until p is first written
   }
-}
-
-// Per-step block kernels: one thread per node row over the sliced-ELL copies.  A warp is one
-// slice of 32 consecutive node rows.  The slice's width W (its longest row, rounded up to a
-// multiple of 4) is stored as W/4 chunks: entry j of the row in lane l sits at
-//   ptr[slice] + 128 (j / 4) + 4 l + (j % 4),
-// so a lane's four entries of a chunk are adjacent (one 16-byte column load, one 16- or
-// 32-byte load per plane) and a warp reads 512 contiguous bytes per 4-byte plane.  Padding
-// entries point at the row's own node with zero values.
-#define SELL_ROW_LOOP(ptr)                                                                      \
-  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < g.n_slices * 32;    \
-       row += (int64_t)gridDim.x * blockDim.x)
-// first entry of this lane's row and the slice's chunk count
-#define SELL_ROW_BEGIN(ptr)                                 \
-  const int64_t sl_ = row >> 5;                             \
-  const int64_t p0 = (ptr)[sl_] + 4 * (row & 31);           \
-  const int64_t nq = ((ptr)[sl_ + 1] - (ptr)[sl_]) >> 7;
-
-__device__ __forceinline__ void cols4(const int* c, int64_t pos, int (&v)[4], int keep) {
-  const int4* q = reinterpret_cast<const int4*>(c + pos);
-  const int4 a = keep ? __ldg(q) : __ldcs(q);
-  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-}
-__device__ __forceinline__ void ld4(const double* p, double (&v)[4], int keep) {
-  const double2* q = reinterpret_cast<const double2*>(p);
-  const double2 a = keep ? __ldg(q) : __ldcs(q);
-  const double2 b = keep ? __ldg(q + 1) : __ldcs(q + 1);
-  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
-}
-__device__ __forceinline__ void ld4(const float* p, float (&v)[4], int keep) {
-  const float4* q = reinterpret_cast<const float4*>(p);
-  const float4 a = keep ? __ldg(q) : __ldcs(q);
-  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-}
-__device__ __forceinline__ void ld4(const float2* p, float2 (&v)[4], int keep) {
-  const float4* q = reinterpret_cast<const float4*>(p);
-  const float4 a = keep ? __ldg(q) : __ldcs(q);
-  const float4 b = keep ? __ldg(q + 1) : __ldcs(q + 1);
-  v[0] = make_float2(a.x, a.y); v[1] = make_float2(a.z, a.w); v[2] = make_float2(b.x, b.y); v[3] = make_float2(b.z, b.w);
-}
-__device__ __forceinline__ void ld2(const double* p, double (&v)[2], int keep) {
-  const double2* q = reinterpret_cast<const double2*>(p);
-  const double2 a = keep ? __ldg(q) : __ldcs(q);
-  v[0] = a.x; v[1] = a.y;
-}
-__device__ __forceinline__ void ld2(const float2* p, float2 (&v)[2], int keep) {
-  const float4* q = reinterpret_cast<const float4*>(p);
-  const float4 a = keep ? __ldg(q) : __ldcs(q);
-  v[0] = make_float2(a.x, a.y); v[1] = make_float2(a.z, a.w);
-}
-// TPR threads per node row (TPR divides 32): the row's chunks are dealt round-robin to its
-// TPR lanes and the partial sums combined by shuffles.  A warp covers 32 / TPR rows of one
-// slice, so loop trips are warp-uniform (full-mask shuffles are safe).
-#define SELL_ROW_LOOP_T(tpr)                                                                            \
-  for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / (tpr); row < g.n_slices * 32; \
-       row += (int64_t)gridDim.x * blockDim.x / (tpr))
-
-// hi/lo accumulation of a * p in FP32-pair arithmetic (a = ah + al, p = p.x + p.y): the
-// product's rounding error (fmaf) and the sum's (two-sum) go to lo; _rn intrinsics keep the
-// compiler from contracting the error terms
-__device__ __forceinline__ void pair_fma(float ah, float al, float2 pv, float& hi, float& lo) {
-  const float pr = __fmul_rn(ah, pv.x);
-  const float pe = fmaf(ah, pv.x, -pr);
-  const float t = __fadd_rn(hi, pr);
-  const float bp = __fsub_rn(t, hi);
-  const float e2 = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(pr, bp));
-  hi = t;
-  lo += (pe + e2) + fmaf(ah, pv.y, al * pv.x);
-}
-
-// (hi, lo) += (h2, l2), the rounding error of the hi sum kept in lo
-__device__ __forceinline__ void pair_add(float& hi, float& lo, float h2, float l2) {
-  const float t = __fadd_rn(hi, h2);
-  const float bp = __fsub_rn(t, hi);
-  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(h2, bp));
-  hi = t;
-  lo = __fadd_rn(__fadd_rn(lo, l2), e);
-}
-
-// combine the TPR lanes' partial sums of a row; every lane ends with the group leader's result
-template <int TPR>
-__device__ __forceinline__ void group_pair_sum(float& hi, float& lo) {
-  if constexpr (TPR > 1) {
-#pragma unroll
-    for (int o = 1; o < TPR; o <<= 1) {
-      const float h2 = __shfl_xor_sync(0xffffffffu, hi, o), l2 = __shfl_xor_sync(0xffffffffu, lo, o);
-      pair_add(hi, lo, h2, l2);
-    }
-    const int lead = (threadIdx.x & 31) & ~(TPR - 1);
-    hi = __shfl_sync(0xffffffffu, hi, lead);
-    lo = __shfl_sync(0xffffffffu, lo, lead);
-  }
-}
-template <int TPR>
-__device__ __forceinline__ double group_sum(double x) {
-  if constexpr (TPR > 1) {
-#pragma unroll
-    for (int o = 1; o < TPR; o <<= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    x = __shfl_sync(0xffffffffu, x, (threadIdx.x & 31) & ~(TPR - 1));
-  }
-  return x;
 }
 
 // r = b - A x0 with b = f - K q1 - M q2 - Cabs y1; bb = |b|^2.  x = x0.
@@ -913,204 +717,6 @@ __global__ void k_transpose_g(Args g, const float* GB, float* GTB) {
 }
 
 // ------------------------------------------------------------------ explicit scheme
-// Central difference with the row-sum lumped mass M_L (no counterpart in the reference, whose
-// mass is always consistent):
-//   a_n = M_L^-1 (f_n - K (u_n + beta v_{n-1/2}) - alpha M_L v_{n-1/2} - Cabs v_{n-1/2})
-//   v_{n+1/2} = v_{n-1/2} + dt a_n ;  u_{n+1} = u_n + dt v_{n+1/2}
-// Where a step also stores its new state (the adjoint's recompute): u, v of state k of the
-// current segment go to u[k n_s ...], v[k n_s ...], k = state index - *t0.
-struct StateStore {
-  double *u, *v;
-  const int* t0;
-};
-
-// One thread per node row over the sliced-ELL K; w = u + beta v and v are ping-ponged
-// (neighbours read the previous step's values), u is updated in place (own row only).  kPair:
-// K w in FP32-pair arithmetic on the K pair planes with w kept as (hi, lo) pairs (GB300's
-// FP64 rate, not HBM, bounds the FP64 products); the update itself stays FP64.  The last
-// block to finish advances the step counter and swaps the force entries in f from step t to
-// step t + 1 (every block has read f by then).
-template <int D, bool kPair, int TPR>
-__global__ void __launch_bounds__(kThreads) k_explicit(Args g, const double* __restrict__ ML,
-                                                       const double* __restrict__ IML,
-                                                       const double* __restrict__ v_in, double* __restrict__ v_out,
-                                                       const double* __restrict__ w_in, double* __restrict__ w_out,
-                                                       const int* __restrict__ rec_map, StateStore store) {
-  const float2* w2_in = reinterpret_cast<const float2*>(w_in);
-  float2* w2_out = reinterpret_cast<float2*>(w_out);
-  const int step = g.s->t + 1;
-  const int64_t sk = store.u ? (int64_t)(step - *store.t0) * g.n_s : 0;
-  const bool rec_now = g.n_rec > 0 && g.out_interval > 0 && (step % g.out_interval) == 0 &&
-                       step / g.out_interval < g.n_out;
-  const int64_t orow = rec_now ? step / g.out_interval : 0;
-  const int sub = threadIdx.x % TPR;
-  SELL_ROW_LOOP_T(TPR) {
-    SELL_ROW_BEGIN(g.sf_ptr)
-    double s[D][D];
-    float hi[D], lo[D];
-#pragma unroll
-    for (int c = 0; c < D; ++c) {
-      hi[c] = lo[c] = 0.f;
-#pragma unroll
-      for (int d = 0; d < D; ++d) s[c][d] = 0.0;
-    }
-    for (int64_t q = sub; q < nq; q += TPR) {
-      const int64_t pos = p0 + 128 * q;
-      int cl[4];
-      cols4(g.sf_col, pos, cl, g.keep_l2);
-      if constexpr (kPair) {
-        float2 wa[4][D];
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-#pragma unroll
-          for (int d = 0; d < D; ++d) wa[e][d] = w2_in[(int64_t)cl[e] * D + d];
-#pragma unroll
-        for (int c = 0; c < D; ++c)
-#pragma unroll
-          for (int d = 0; d < D; ++d) {
-            float2 k4[4];
-            ld4(g.KPS + (int64_t)(c * D + d) * g.sf_n + pos, k4, g.keep_l2);
-#pragma unroll
-            for (int e = 0; e < 4; ++e) pair_fma(k4[e].x, k4[e].y, wa[e][d], hi[c], lo[c]);
-          }
-      } else {
-        double wa[4][D];
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-#pragma unroll
-          for (int d = 0; d < D; ++d) wa[e][d] = w_in[(int64_t)cl[e] * D + d];
-#pragma unroll
-        for (int c = 0; c < D; ++c)
-#pragma unroll
-          for (int d = 0; d < D; ++d) {
-            double kv[4];
-            ld4(g.KS + (int64_t)(c * D + d) * g.sf_n + pos, kv, g.keep_l2);
-#pragma unroll
-            for (int e = 0; e < 4; ++e) s[c][d] = fma(kv[e], wa[e][d], s[c][d]);
-          }
-      }
-    }
-#pragma unroll
-    for (int c = 0; c < D; ++c) {
-      if (kPair) {
-        group_pair_sum<TPR>(hi[c], lo[c]);
-      } else {
-#pragma unroll
-        for (int d = 0; d < D; ++d) s[c][d] = group_sum<TPR>(s[c][d]);
-      }
-    }
-    if (row < g.n_nodes) {
-#pragma unroll
-      for (int c = 0; c < D; ++c) {
-        if (TPR > 1 && c % TPR != sub) continue;  // one lane per component
-        const int64_t i = row * D + c;
-        if (g.fixed[i]) {
-          v_out[i] = 0.0;
-          if (kPair) w2_out[i] = make_float2(0.f, 0.f);
-          else w_out[i] = 0.0;
-          if (store.u) store.u[sk + i] = store.v[sk + i] = 0.0;
-          continue;
-        }
-        double kw = 0.0;
-        if (kPair) {
-          kw = (double)hi[c] + (double)lo[c];
-        } else {
-#pragma unroll
-          for (int d = 0; d < D; ++d) kw += s[c][d];
-        }
-        double cab = 0.0;
-        for (int64_t k = g.cab_ptr[i]; k < g.cab_ptr[i + 1]; ++k) cab = fma(g.cab_val[k], v_in[g.cab_col[k]], cab);
-        const double vi = v_in[i], ml = ML[i];
-        const double acc = (g.f[i] - kw - g.alpha_r * ml * vi - cab) * IML[i];
-        const double vn = fma(g.dt, acc, vi);
-        const double un = fma(g.dt, vn, g.u[i]);
-        v_out[i] = vn;
-        g.u[i] = un;
-        if (kPair) w2_out[i] = split_pair(fma(g.beta_r, vn, un));
-        else w_out[i] = fma(g.beta_r, vn, un);
-        if (store.u) {
-          store.u[sk + i] = un;
-          store.v[sk + i] = vn;
-        }
-        if (rec_now) {
-          const int rj = rec_map[i];
-          if (rj >= 0) {
-            if (g.out_u) g.out_u[orow * g.n_rec + rj] = un;
-            if (g.out_v) g.out_v[orow * g.n_rec + rj] = vn;
-          }
-        }
-      }
-    }
-  }
-  if (last_block(&g.s->ticket)) {
-    const int t = step - 1;
-    if (g.f_ptr) {
-      if (t >= 0 && t < g.n_t)
-        for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f[g.f_slot[k]] = 0.0;
-      __syncthreads();
-      if (t + 1 >= 0 && t + 1 < g.n_t)
-        for (int64_t k = g.f_ptr[t + 1] + threadIdx.x; k < g.f_ptr[t + 2]; k += blockDim.x) g.f[g.f_slot[k]] += g.f_val[k];
-    }
-    if (threadIdx.x == 0) {
-      g.s->ticket = 0;
-      g.s->t = step;
-    }
-  }
-}
-
-// f = entries of step s->t (f zeroed beforehand)
-__global__ void k_force_explicit0(Args g) {
-  const int t = g.s->t;
-  if (!g.f_ptr || t < 0 || t >= g.n_t) return;
-  for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f[g.f_slot[k]] += g.f_val[k];
-}
-
-// f holds the entries of step t (= s->t); clear those of t-1
-__global__ void k_force_explicit(Args g) {
-  const int t = g.s->t;
-  if (!g.f_ptr) return;
-  const int t0 = t - 1;
-  if (t0 >= 0 && t0 < g.n_t)
-    for (int64_t k = g.f_ptr[t0] + threadIdx.x; k < g.f_ptr[t0 + 1]; k += blockDim.x) g.f[g.f_slot[k]] = 0.0;
-  __syncthreads();
-  if (t >= 0 && t < g.n_t)
-    for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f[g.f_slot[k]] += g.f_val[k];
-}
-
-// row-sum lumped mass over free columns, and w = u + beta v
-__global__ void k_lumped(Args g, double* ML) {
-  for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < g.n_nodes; a += (int64_t)gridDim.x * blockDim.x) {
-    for (int c = 0; c < g.D; ++c) {
-      double m = 0.0;
-      for (int64_t k = g.adj_ptr[a]; k < g.adj_ptr[a + 1]; ++k)
-        if (!g.fixed[(int64_t)g.adj[k] * g.D + c]) m += g.MS[k];
-      ML[a * g.D + c] = g.fixed[a * g.D + c] ? 1.0 : m;
-    }
-  }
-}
-
-__global__ void k_w_init(Args g, double* w, int pair) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
-    const double x = fma(g.beta_r, g.v[i], g.u[i]);
-    if (pair) reinterpret_cast<float2*>(w)[i] = split_pair(x);
-    else w[i] = x;
-  }
-}
-
-__global__ void k_reciprocal(int64_t n, const double* __restrict__ x, double* __restrict__ y) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = 1.0 / x[i];
-}
-
-__global__ void k_rec_map(Args g, int* map) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x)
-    map[i] = -1;
-}
-__global__ void k_rec_map_fill(Args g, int* map) {
-  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.n_rec; j += (int64_t)gridDim.x * blockDim.x)
-    map[g.rec_slot[j]] = (int)j;
-}
-
 // ------------------------------------------------------------------ sliced-ELL construction
 // kind 0: full row [adj_ptr[a], adj_ptr[a+1]); 1: lower [adj_ptr[a], diag[a]]; 2: upper [diag[a], adj_ptr[a+1])
 __device__ inline void row_range(int kind, const int64_t* adj_ptr, const int64_t* diag, int64_t a, int64_t& b,
@@ -1180,35 +786,12 @@ __global__ void k_init_scal(Scal* s, double tol2, int max_it) {
   s->hist = 0;
 }
 
-__global__ void k_set_t(Scal* s, int t) { s->t = t; }
-
 }  // namespace nb
 }  // namespace sc
 
 using namespace sc;
 using namespace sc::nb;
 
-struct sc_nb_newmark {
-  Args g;
-  void* sell_mem[16] = {};
-  int n_sell_mem = 0;
-  // explicit scheme state (allocated on first use)
-  double *ML = nullptr, *IML = nullptr, *v1 = nullptr, *w0 = nullptr, *w1 = nullptr;
-  float2* KPS = nullptr;
-  int explicit_pair = 1;  // K w of the explicit step and the adjoint in FP32-pair arithmetic
-  float adj_ms[3] = {0.f, 0.f, 0.f};  // last sc_nb_adjoint: forward, recompute, backward (device time)
-  int* rec_map = nullptr;
-  cudaGraphExec_t ex_exec[2] = {nullptr, nullptr};
-  cudaGraph_t ex_graph[2] = {nullptr, nullptr};
-  cudaStream_t user = nullptr, cap = nullptr, cap2 = nullptr;
-  unsigned node_blocks = 1, vec_blocks = 1;
-  // threads per node row of the explicit step and the adjoint rows (more on small meshes, so
-  // the SMs have enough warps to cover load latency) and their grid
-  int tpr = 1;
-  unsigned tpr_blocks = 1;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-};
 
 namespace {
 
@@ -1290,7 +873,6 @@ int build_graph(sc_nb_newmark* h) {
 }
 
 }  // namespace
-static void drop_explicit_graphs(sc_nb_newmark* h);
 namespace {
 
 void drop_graph(sc_nb_newmark* h) {
@@ -1300,12 +882,6 @@ void drop_graph(sc_nb_newmark* h) {
 
 }  // namespace
 
-__global__ void k_split_pairs(int64_t n, const double* __restrict__ x, float2* __restrict__ hl) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float h = (float)x[i];
-    hl[i] = make_float2(h, (float)(x[i] - (double)h));
-  }
-}
 
 // Sliced-ELL copies of K, A, M (full pattern), G (lower) and G^T (upper) for the per-step
 // kernels; allocated here (setup) from the stream-ordered pool and freed by sc_nb_destroy.
@@ -1633,613 +1209,6 @@ extern "C" int sc_nb_run(sc_nb_newmark* h, int t_begin, int t_end) {
   return SC_OK;
 }
 
-static void drop_explicit_graphs(sc_nb_newmark* h) {
-  for (int k = 0; k < 2; ++k) {
-    if (h->ex_exec[k]) cudaGraphExecDestroy(h->ex_exec[k]), h->ex_exec[k] = nullptr;
-    if (h->ex_graph[k]) cudaGraphDestroy(h->ex_graph[k]), h->ex_graph[k] = nullptr;
-  }
-}
-
-template <int D, int TPR>
-static void launch_explicit_t(const sc_nb_newmark* h, cudaStream_t st, const Args& g, const double* vin,
-                              double* vout, const double* win, double* wout, StateStore store) {
-  if (h->explicit_pair)
-    k_explicit<D, true, TPR><<<h->tpr_blocks, kThreads, 0, st>>>(g, h->ML, h->IML, vin, vout, win, wout, h->rec_map,
-                                                                 store);
-  else
-    k_explicit<D, false, TPR><<<h->tpr_blocks, kThreads, 0, st>>>(g, h->ML, h->IML, vin, vout, win, wout, h->rec_map,
-                                                                  store);
-}
-template <int D>
-static void launch_explicit(const sc_nb_newmark* h, cudaStream_t st, const Args& g, const double* vin, double* vout,
-                            const double* win, double* wout, StateStore store) {
-  switch (h->tpr) {
-    case 4: launch_explicit_t<D, 4>(h, st, g, vin, vout, win, wout, store); break;
-    case 2: launch_explicit_t<D, 2>(h, st, g, vin, vout, win, wout, store); break;
-    default: launch_explicit_t<D, 1>(h, st, g, vin, vout, win, wout, store); break;
-  }
-}
-
-template <int D>
-static int build_explicit_graph(sc_nb_newmark* h, int k) {
-  Args g = h->g;
-  const double* vin = k == 0 ? g.v : h->v1;
-  double* vout = k == 0 ? h->v1 : g.v;
-  const double* win = k == 0 ? h->w0 : h->w1;
-  double* wout = k == 0 ? h->w1 : h->w0;
-  cudaStream_t cs = h->cap;
-  int rc = check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "capture explicit");
-  if (rc) return rc;
-  launch_explicit<D>(h, cs, g, vin, vout, win, wout, StateStore{});
-  cudaGraph_t graph;
-  if ((rc = check(cudaStreamEndCapture(cs, &graph), "end explicit"))) return rc;
-  if ((rc = check(cudaGraphInstantiate(&h->ex_exec[k], graph, 0), "instantiate explicit"))) {
-    cudaGraphDestroy(graph);
-    return rc;
-  }
-  h->ex_graph[k] = graph;
-  return SC_OK;
-}
-
-// Explicit central-difference steps t_begin .. t_end-1 on the same handle (u, v are the
-// handle's state vectors; a is not used).  At t_begin == 0 the force entries of step 0 are
-// written; the run always ends with the state in the caller's u and v.
-extern "C" int sc_nb_explicit_run(sc_nb_newmark* h, int t_begin, int t_end) {
-  if (!h || t_begin < 0 || t_end < t_begin) return SC_BAD_ARG;
-  Args& g = h->g;
-  cudaStream_t st = h->user;
-  int rc;
-  if (!h->ML) {
-    const int64_t ns = g.n_s;
-    if ((rc = check(cudaMallocAsync((void**)&h->ML, 8 * ns, st), "malloc"))) return rc;
-    if ((rc = check(cudaMallocAsync((void**)&h->v1, 8 * ns, st), "malloc"))) return rc;
-    if ((rc = check(cudaMallocAsync((void**)&h->w0, 8 * ns, st), "malloc"))) return rc;
-    if ((rc = check(cudaMallocAsync((void**)&h->w1, 8 * ns, st), "malloc"))) return rc;
-    if ((rc = check(cudaMallocAsync((void**)&h->rec_map, 4 * ns, st), "malloc"))) return rc;
-    if ((rc = check(cudaMallocAsync((void**)&h->IML, 8 * ns, st), "malloc"))) return rc;
-    k_lumped<<<grid_for(g.n_nodes, 256), 256, 0, st>>>(g, h->ML);
-    k_reciprocal<<<grid_for(ns, 256), 256, 0, st>>>(ns, h->ML, h->IML);
-  }
-  if (h->explicit_pair && !h->KPS) {
-    const int64_t n2 = (int64_t)g.D * g.D * g.sf_n;
-    if ((rc = check(cudaMallocAsync((void**)&h->KPS, 8 * n2, st), "malloc"))) return rc;
-    k_split_pairs<<<grid_for(n2, 256, 152 * 32), 256, 0, st>>>(n2, g.KS, h->KPS);
-    g.KPS = h->KPS;
-    drop_explicit_graphs(h);
-  }
-  if (!h->ex_exec[0]) {
-    k_rec_map<<<grid_for(g.n_s, 256), 256, 0, st>>>(g, h->rec_map);
-    if (g.n_rec > 0) k_rec_map_fill<<<grid_for(g.n_rec, 256), 256, 0, st>>>(g, h->rec_map);
-    for (int k = 0; k < 2; ++k) {
-      rc = g.D == 3 ? build_explicit_graph<3>(h, k) : build_explicit_graph<2>(h, k);
-      if (rc) return rc;
-    }
-  }
-  k_w_init<<<h->vec_blocks, 256, 0, st>>>(g, h->w0, h->explicit_pair);
-  if (t_begin == 0 && g.f_ptr) {
-    cudaMemsetAsync(g.f, 0, 8 * g.n_s, st);
-    k_set_t<<<1, 1, 0, st>>>(g.s, 0);
-    k_force_explicit<<<1, 256, 0, st>>>(g);  // step 0 entries
-  }
-  k_set_t<<<1, 1, 0, st>>>(g.s, t_begin);
-  if ((rc = check_launch("explicit prepare"))) return rc;
-  int k = 0;
-  for (int t = t_begin; t < t_end; ++t, k ^= 1)
-    if ((rc = check(cudaGraphLaunch(h->ex_exec[k], st), "explicit launch"))) return rc;
-  if (k == 1) {  // state is in v1 / w1: bring v back to the caller's buffer
-    if ((rc = check(cudaMemcpyAsync(g.v, h->v1, 8 * g.n_s, cudaMemcpyDeviceToDevice, st), "copy v"))) return rc;
-  }
-  return SC_OK;
-}
-
-extern "C" int sc_nb_time_explicit(sc_nb_newmark* h, int reps, float* ms_per_step) {
-  if (!h || reps <= 0 || !ms_per_step || !h->ex_exec[0]) return SC_BAD_ARG;
-  cudaStream_t st = h->user;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  const int t = 0;
-  (void)t;
-  cudaEventRecord(e0, st);
-  for (int i = 0; i < reps; ++i) {
-    const Args& g = h->g;
-    if (g.D == 3) launch_explicit<3>(h, st, g, g.v, h->v1, h->w0, h->w1, StateStore{});
-    else launch_explicit<2>(h, st, g, g.v, h->v1, h->w0, h->w1, StateStore{});
-  }
-  cudaEventRecord(e1, st);
-  int rc = check_launch("explicit timing");
-  if (!rc) rc = check(cudaEventSynchronize(e1), "sync");
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, e0, e1);
-  *ms_per_step = ms / reps;
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  return rc;
-}
-
-// ------------------------------------------------------------------ adjoint of the explicit scheme
-// Discrete adjoint of sc_nb_explicit_run for the receiver-velocity misfit
-//   J = 1/2 sum_{n=1..N} |P v_n - d_n|^2
-// with respect to per-element E and rho (K = sum E_e K1_e + springs, M_L = sum rho_e ml1_e,
-// Cab = sum sqrt(rho_e E_e) C1_f).  Forward with checkpoints every C steps, then per segment
-// (last first) recompute the states and run the backward recursion (g = mu_v + dt mu_u,
-// y = M_L^-1 g, mu_u -= dt K y, mu_v = g - dt (beta K y + Cab y + alpha M_L y) + P^T(P v_n - d_n))
-// accumulating dJ/dE_e, dJ/drho_e element by element (deterministic, no atomics).
-struct sc_adj_desc {
-  int n_steps, checkpoint;
-  int n_rec;
-  const int* rec_slot;
-  const double* target;
-  int n_elem, n_en;
-  const int *elem, *ke_type;
-  const float* ke1;
-  const double *young, *rho;
-  const float* ml1;
-  const int64_t* l_eptr;
-  const int *l_row, *l_col;
-  const double *l_c, *l_s;
-};
-namespace {
-
-struct AdjState {
-  double *seg_u, *seg_v, *mu_u, *mu_v, *out_v, *gE, *gR;
-  double* y[2];        // (mu_v + dt mu_u) / M_L of the step being reversed, and of the next one
-  int *n_dev, *n_dev_e;  // step being reversed, one counter per backward kernel
-  unsigned* ticket_e;  // finished blocks of the element kernel
-  int *seg_t0, *rec_map;
-  double* J;
-  // FP32 inputs of the element kernel for the step being reversed ([cur]) and the next
-  // ([cur ^ 1]): w = u + beta v as (hi, lo) pairs, v, a = (v_{n+1} - v_n) / dt, y
-  float2* wp[2];
-  float *v32[2], *a32[2], *y32[2];
-};
-
-__device__ __forceinline__ double y_at(const double* y, int64_t i, bool pair) {
-  if (pair) {
-    const float2 p = reinterpret_cast<const float2*>(y)[i];
-    return (double)p.x + (double)p.y;
-  }
-  return y[i];
-}
-
-// FP32 element inputs of step n = *n_dev from the segment's FP64 states (k = n - t0)
-__device__ __forceinline__ void adj_prep_slot(const Args& g, const AdjState& a, int buf, int64_t k, int64_t i,
-                                              double y_i) {
-  float2* wp = buf ? a.wp[1] : a.wp[0];
-  float* v32 = buf ? a.v32[1] : a.v32[0];
-  float* a32 = buf ? a.a32[1] : a.a32[0];
-  float* y32 = buf ? a.y32[1] : a.y32[0];
-  if (g.fixed[i]) {
-    wp[i] = make_float2(0.f, 0.f);
-    v32[i] = a32[i] = y32[i] = 0.f;
-    return;
-  }
-  const double u0 = a.seg_u[k * g.n_s + i], v0 = a.seg_v[k * g.n_s + i], v1 = a.seg_v[(k + 1) * g.n_s + i];
-  wp[i] = split_pair(fma(g.beta_r, v0, u0));
-  v32[i] = (float)v0;
-  a32[i] = (float)((v1 - v0) / g.dt);
-  y32[i] = (float)y_i;
-}
-
-// Backward step n (state n -> n+1 reversed), node rows: with y = y[cur],
-//   mu_u <- mu_u - dt K y,  mu_v <- g - dt (beta K y + Cab y + alpha M_L y) + P^T (P v_n - d_n),
-//   y[cur ^ 1] = (mu_v + dt mu_u) / M_L   (the y of step n - 1).
-// kPair: K y in FP32-pair arithmetic on the K pair planes, y kept as (hi, lo) pairs.
-// The last block to finish decrements the row kernel's step counter.
-
-template <int D, bool kPair, int TPR>
-__global__ void __launch_bounds__(kThreads) k_adj_rows(Args g, const double* __restrict__ ML,
-                                                       const double* __restrict__ IML, sc_adj_desc d, AdjState a,
-                                                       int cur) {
-  const int n = *a.n_dev;
-  const int k = n - *a.seg_t0;
-  const double* y = cur ? a.y[1] : a.y[0];  // (a select: no local copy of the parameter)
-  double* yn = cur ? a.y[0] : a.y[1];
-  const float2* y2 = reinterpret_cast<const float2*>(y);
-  const int sub = threadIdx.x % TPR;
-  SELL_ROW_LOOP_T(TPR) {
-    SELL_ROW_BEGIN(g.sf_ptr)
-    double s[D];
-    float hi[D], lo[D];
-#pragma unroll
-    for (int c = 0; c < D; ++c) {
-      s[c] = 0.0;
-      hi[c] = lo[c] = 0.f;
-    }
-    for (int64_t q = sub; q < nq; q += TPR) {
-      const int64_t pos = p0 + 128 * q;
-      int cl[4];
-      cols4(g.sf_col, pos, cl, g.keep_l2);
-      if constexpr (kPair) {
-        float2 ya[4][D];
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-#pragma unroll
-          for (int dd = 0; dd < D; ++dd) ya[e][dd] = y2[(int64_t)cl[e] * D + dd];
-#pragma unroll
-        for (int c = 0; c < D; ++c)
-#pragma unroll
-          for (int dd = 0; dd < D; ++dd) {
-            float2 k4[4];
-            ld4(g.KPS + (int64_t)(c * D + dd) * g.sf_n + pos, k4, g.keep_l2);
-#pragma unroll
-            for (int e = 0; e < 4; ++e) pair_fma(k4[e].x, k4[e].y, ya[e][dd], hi[c], lo[c]);
-          }
-      } else {
-        double ya[4][D];
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-#pragma unroll
-          for (int dd = 0; dd < D; ++dd) ya[e][dd] = y[(int64_t)cl[e] * D + dd];
-#pragma unroll
-        for (int c = 0; c < D; ++c)
-#pragma unroll
-          for (int dd = 0; dd < D; ++dd) {
-            double kv[4];
-            ld4(g.KS + (int64_t)(c * D + dd) * g.sf_n + pos, kv, g.keep_l2);
-#pragma unroll
-            for (int e = 0; e < 4; ++e) s[c] = fma(kv[e], ya[e][dd], s[c]);
-          }
-      }
-    }
-#pragma unroll
-    for (int c = 0; c < D; ++c) {
-      if (kPair) group_pair_sum<TPR>(hi[c], lo[c]);
-      else s[c] = group_sum<TPR>(s[c]);
-    }
-    if (row < g.n_nodes) {
-#pragma unroll
-      for (int c = 0; c < D; ++c) {
-        if (TPR > 1 && c % TPR != sub) continue;  // one lane per component
-        const int64_t i = row * D + c;
-        if (g.fixed[i]) {
-          a.mu_u[i] = a.mu_v[i] = 0.0;
-          if (kPair) reinterpret_cast<float2*>(yn)[i] = make_float2(0.f, 0.f);
-          else yn[i] = 0.0;
-          if (k >= 1) adj_prep_slot(g, a, cur ^ 1, k - 1, i, 0.0);
-          continue;
-        }
-        const double ky = kPair ? (double)hi[c] + (double)lo[c] : s[c];
-        double cy = 0.0;
-        for (int64_t q = g.cab_ptr[i]; q < g.cab_ptr[i + 1]; ++q) cy = fma(g.cab_val[q], y_at(y, g.cab_col[q], kPair), cy);
-        const double yi = y_at(y, i, kPair);
-        const double gg = fma(g.dt, a.mu_u[i], a.mu_v[i]);
-        const double mu = fma(-g.dt, ky, a.mu_u[i]);
-        double mv = gg - g.dt * (g.beta_r * ky + cy + g.alpha_r * ML[i] * yi);
-        const int rj = a.rec_map[i];
-        if (rj >= 0 && n >= 1) mv += a.seg_v[(int64_t)k * g.n_s + i] - d.target[(int64_t)n * d.n_rec + rj];
-        a.mu_u[i] = mu;
-        a.mu_v[i] = mv;
-        const double ynext = fma(g.dt, mu, mv) * IML[i];
-        if (kPair) reinterpret_cast<float2*>(yn)[i] = split_pair(ynext);
-        else yn[i] = ynext;
-        // the element kernel's FP32 inputs of step n - 1 when its state is in this segment
-        // (the first step reversed in a segment gets them from k_adj_prep)
-        if (k >= 1) adj_prep_slot(g, a, cur ^ 1, k - 1, i, ynext);
-      }
-    }
-  }
-  if (last_block(&g.s->ticket)) {
-    if (threadIdx.x == 0) {
-      g.s->ticket = 0;
-      *a.n_dev = n - 1;
-    }
-  }
-}
-
-constexpr int kAdjElemThreads = 128;
-
-// Backward step n, element gradients: one lane per element node (32 / n_en elements per
-// warp), lane (e, la) owning the element DOFs 3 la .. 3 la + 2:
-//   dJ/dE_e   -= dt y_e . [K1_e (u + beta v)_e + Lysmer terms]
-//   dJ/drho_e -= dt sum ml1_e y_e (a + alpha v)_e + Lysmer term.
-// Differences of FP64 states (translations removed, v_{n+1} - v_n) are taken in FP64 and the
-// products in FP32 (GB300's FP64 rate is a fraction of its FP32 rate); per-element sums are
-// FP64, made by the element's first lane in lane order (deterministic).  The last block to
-// finish decrements the element kernel's step counter.
-__global__ void __launch_bounds__(kAdjElemThreads) k_adj_elems(Args g, sc_adj_desc d, AdjState a, int cur, int ypair) {
-  __shared__ float sw[kAdjElemThreads / 32][96];
-  __shared__ float part[kAdjElemThreads / 32][32][2];
-  const int n = *a.n_dev_e;
-  const int k = n - *a.seg_t0;
-  const double* y = cur ? a.y[1] : a.y[0];
-  const float2* wp = cur ? a.wp[1] : a.wp[0];
-  const float* v32 = cur ? a.v32[1] : a.v32[0];
-  const float* a32 = cur ? a.a32[1] : a.a32[0];
-  const float* y32 = cur ? a.y32[1] : a.y32[0];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int ne = d.n_en, nd = 3 * ne, epw = 32 / ne;
-  const int grp = lane / ne, la = lane % ne, base = grp * ne;
-  const float alpha = (float)g.alpha_r;
-  const int64_t warps = (int64_t)gridDim.x * (kAdjElemThreads / 32);
-  for (int64_t wg = (int64_t)blockIdx.x * (kAdjElemThreads / 32) + wib; wg * epw < d.n_elem; wg += warps) {
-    const int64_t e = wg * epw + grp;
-    const bool on = grp < epw && e < d.n_elem;
-    float ya[3] = {0.f, 0.f, 0.f}, gr = 0.f;
-    if (on) {
-      const int* en = d.elem + e * ne;
-      const int64_t sa = (int64_t)en[la] * 3, s0 = (int64_t)en[0] * 3;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        // K1 annihilates rigid translations: (u + beta v) relative to the element's first
-        // node, differenced on the (hi, lo) pairs, so the FP32 products see strains
-        const float2 wb = wp[sa + c], w0 = wp[s0 + c];
-        sw[wib][base * 3 + 3 * la + c] = (wb.x - w0.x) + (wb.y - w0.y);
-        ya[c] = y32[sa + c];
-        gr = fmaf(d.ml1[e * nd + 3 * la + c] * ya[c], fmaf(alpha, v32[sa + c], a32[sa + c]), gr);
-      }
-    }
-    __syncwarp();
-    float ge = 0.f;
-    if (on) {
-      const float* K1 = d.ke1 + (int64_t)d.ke_type[e] * nd * nd + (int64_t)(3 * la) * nd;
-      const float* wv = &sw[wib][base * 3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float row = 0.f;
-        for (int b = 0; b < nd; ++b) row = fmaf(__ldg(K1 + c * nd + b), wv[b], row);
-        ge = fmaf(ya[c], row, ge);
-      }
-    }
-    part[wib][lane][0] = ge;
-    part[wib][lane][1] = gr;
-    __syncwarp();
-    if (on && la == 0) {
-      float ge_e = 0.f, gr_e = 0.f;
-      for (int q = 0; q < ne; ++q) {
-        ge_e += part[wib][base + q][0];
-        gr_e += part[wib][base + q][1];
-      }
-      double gE = (double)ge_e, gR = (double)gr_e;
-      const int64_t q0 = d.l_eptr[e], q1 = d.l_eptr[e + 1];
-      if (q1 > q0) {  // Lysmer terms of boundary elements, FP64
-        const double* u = a.seg_u + (int64_t)k * g.n_s;
-        const double* v = a.seg_v + (int64_t)k * g.n_s;
-        const double iE = 1.0 / d.young[e], iR = 1.0 / d.rho[e];
-        for (int64_t q = q0; q < q1; ++q) {
-          const double yr = y_at(y, d.l_row[q], ypair);
-          const int cl = d.l_col[q];
-          gE += yr * (d.l_s[q] * iE * fma(g.beta_r, v[cl], u[cl]) + 0.5 * d.l_c[q] * iE * v[cl]);
-          gR += yr * 0.5 * d.l_c[q] * iR * v[cl];
-        }
-      }
-      a.gE[e] -= g.dt * gE;
-      a.gR[e] -= g.dt * gR;
-    }
-    __syncwarp();
-  }
-  if (last_block(a.ticket_e)) {
-    if (threadIdx.x == 0) {
-      *a.ticket_e = 0;
-      *a.n_dev_e = n - 1;
-    }
-  }
-}
-
-// the element kernel's FP32 inputs of the first step reversed in a segment
-__global__ void k_adj_prep(Args g, AdjState a, int buf, int pair) {
-  const int64_t k = *a.n_dev - *a.seg_t0;
-  const double* y = buf ? a.y[1] : a.y[0];
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x)
-    adj_prep_slot(g, a, buf, k, i, y_at(y, i, pair));
-}
-
-// start of the backward sweep: mu_u = 0, mu_v = P^T (v_N - d_N), y = mu_v / M_L
-__global__ void k_adj_init(Args g, const double* __restrict__ IML, AdjState a, const double* target, int n_rec,
-                           int N, int pair) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
-    a.mu_u[i] = 0.0;
-    const int rj = a.rec_map[i];
-    const double mv = rj >= 0 && !g.fixed[i] ? a.out_v[(int64_t)N * n_rec + rj] - target[(int64_t)N * n_rec + rj] : 0.0;
-    a.mu_v[i] = mv;
-    const double y0 = g.fixed[i] ? 0.0 : mv * IML[i];
-    if (pair) reinterpret_cast<float2*>(a.y[0])[i] = split_pair(y0);
-    else a.y[0][i] = y0;
-  }
-}
-
-__global__ void k_adj_misfit(const double* out_v, const double* target, int n_rec, int N, double* J) {
-  __shared__ double sh[32];
-  double s = 0.0;
-  for (int64_t q = (int64_t)n_rec + threadIdx.x; q < (int64_t)(N + 1) * n_rec; q += blockDim.x) {
-    const double r = out_v[q] - target[q];
-    s += r * r;
-  }
-  s = block_sum(s, sh);
-  if (threadIdx.x == 0) *J = 0.5 * s;
-}
-
-__global__ void k_rec_map2(int n_s, int n_rec, const int* rec, int* map) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_s; i += (int64_t)gridDim.x * blockDim.x) map[i] = -1;
-}
-__global__ void k_rec_map2_fill(int n_rec, const int* rec, int* map) {
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n_rec; j += gridDim.x * blockDim.x) map[rec[j]] = j;
-}
-
-}  // namespace
-
-template <int TPR>
-static void launch_adj_rows_t(const sc_nb_newmark* h, cudaStream_t st, const Args& g, const sc_adj_desc& d,
-                              const AdjState& a, int cur) {
-  if (h->explicit_pair) k_adj_rows<3, true, TPR><<<h->tpr_blocks, kThreads, 0, st>>>(g, h->ML, h->IML, d, a, cur);
-  else k_adj_rows<3, false, TPR><<<h->tpr_blocks, kThreads, 0, st>>>(g, h->ML, h->IML, d, a, cur);
-}
-static void launch_adj_rows(const sc_nb_newmark* h, cudaStream_t st, const Args& g, const sc_adj_desc& d,
-                            const AdjState& a, int cur) {
-  switch (h->tpr) {
-    case 4: launch_adj_rows_t<4>(h, st, g, d, a, cur); break;
-    case 2: launch_adj_rows_t<2>(h, st, g, d, a, cur); break;
-    default: launch_adj_rows_t<1>(h, st, g, d, a, cur); break;
-  }
-}
-
-extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_host, double* grad_E,
-                             double* grad_rho) {
-  if (!h || !dp || !grad_E || !grad_rho) return SC_BAD_ARG;
-  const sc_adj_desc d = *dp;
-  if (d.n_steps <= 0 || d.checkpoint <= 0 || d.n_rec <= 0 || !d.rec_slot || !d.target || d.n_elem <= 0 ||
-      d.n_en <= 0 || d.n_en > 32 || !d.elem || !d.ke_type || !d.ke1 || !d.young || !d.rho || !d.ml1 ||
-      !d.l_eptr || h->g.D != 3)
-    return SC_BAD_ARG;
-  Args& g = h->g;
-  cudaStream_t st = h->user;
-  const int N = d.n_steps, C = d.checkpoint < d.n_steps ? d.checkpoint : d.n_steps, nseg = (N + C - 1) / C;
-  const int64_t ns = g.n_s;
-  // save the caller's output configuration
-  const int o_int = g.out_interval, o_nrec = g.n_rec;
-  const int* o_rec = g.rec_slot;
-  double *o_u = g.out_u, *o_v = g.out_v, *o_a = g.out_a;
-  const int64_t o_nout = g.n_out;
-  AdjState a{};
-  double *ck_u = nullptr, *ck_v = nullptr;
-  int* t_host = nullptr;  // segment starts and backward starts, pinned (copied by the stream)
-  int rc = SC_OK;
-  auto M = [&](void** p, size_t b) { return check(cudaMallocAsync(p, b, st), "adjoint malloc"); };
-  cudaGraphExec_t rec_exec[2] = {nullptr, nullptr}, bwd_exec[2] = {nullptr, nullptr};
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  // phase timers: [0, 1] forward, then per segment [2 + 4 s ... 5 + 4 s] recompute and backward
-  std::vector<cudaEvent_t> tev;
-  cudaGraph_t rec_graph[2] = {nullptr, nullptr}, bwd_graph[2] = {nullptr, nullptr};
-  do {
-    if ((rc = M((void**)&ck_u, 8 * ns * nseg)) || (rc = M((void**)&ck_v, 8 * ns * nseg)) ||
-        (rc = M((void**)&a.seg_u, 8 * ns * (C + 1))) || (rc = M((void**)&a.seg_v, 8 * ns * (C + 1))) ||
-        (rc = M((void**)&a.mu_u, 8 * ns)) || (rc = M((void**)&a.mu_v, 8 * ns)) || (rc = M((void**)&a.y[0], 8 * ns)) ||
-        (rc = M((void**)&a.y[1], 8 * ns)) || (rc = M((void**)&a.out_v, 8 * (int64_t)(N + 1) * d.n_rec)) ||
-        (rc = M((void**)&a.n_dev, 4)) || (rc = M((void**)&a.n_dev_e, 4)) || (rc = M((void**)&a.ticket_e, 4)) ||
-        (rc = M((void**)&a.seg_t0, 4)) || (rc = M((void**)&a.rec_map, 4 * ns)) || (rc = M((void**)&a.J, 8)) ||
-        (rc = M((void**)&a.wp[0], 8 * ns)) || (rc = M((void**)&a.wp[1], 8 * ns)) || (rc = M((void**)&a.v32[0], 4 * ns)) ||
-        (rc = M((void**)&a.v32[1], 4 * ns)) || (rc = M((void**)&a.a32[0], 4 * ns)) || (rc = M((void**)&a.a32[1], 4 * ns)) ||
-        (rc = M((void**)&a.y32[0], 4 * ns)) || (rc = M((void**)&a.y32[1], 4 * ns)))
-      break;
-    if ((rc = check(cudaMallocHost((void**)&t_host, 8 * (size_t)nseg), "adjoint pinned"))) break;
-    tev.assign(2 + 4 * (size_t)nseg, nullptr);
-    for (auto& ev : tev)
-      if ((rc = check(cudaEventCreate(&ev), "adjoint timer"))) break;
-    if (rc) break;
-    a.gE = grad_E;
-    a.gR = grad_rho;
-    cudaMemsetAsync(a.ticket_e, 0, 4, st);
-    cudaMemsetAsync(grad_E, 0, 8 * (size_t)d.n_elem, st);
-    cudaMemsetAsync(grad_rho, 0, 8 * (size_t)d.n_elem, st);
-    cudaMemsetAsync(a.out_v, 0, 8 * (size_t)(N + 1) * d.n_rec, st);
-    k_rec_map2<<<grid_for(ns, 256), 256, 0, st>>>((int)ns, d.n_rec, d.rec_slot, a.rec_map);
-    k_rec_map2_fill<<<grid_for(d.n_rec, 128), 128, 0, st>>>(d.n_rec, d.rec_slot, a.rec_map);
-    // forward from rest with checkpoints; receivers recorded into a.out_v
-    cudaMemsetAsync(g.u, 0, 8 * ns, st);
-    cudaMemsetAsync(g.v, 0, 8 * ns, st);
-    if ((rc = sc_nb_set_output(h, 1, d.n_rec, d.rec_slot, nullptr, a.out_v, nullptr, N + 1))) break;
-    cudaEventRecord(tev[0], st);
-    for (int sgi = 0; sgi < nseg && !rc; ++sgi) {
-      const int t0 = sgi * C, t1 = t0 + C < N ? t0 + C : N;
-      cudaMemcpyAsync(ck_u + sgi * ns, g.u, 8 * ns, cudaMemcpyDeviceToDevice, st);
-      cudaMemcpyAsync(ck_v + sgi * ns, g.v, 8 * ns, cudaMemcpyDeviceToDevice, st);
-      rc = sc_nb_explicit_run(h, t0, t1);
-    }
-    if (rc) break;
-    cudaEventRecord(tev[1], st);
-    k_adj_misfit<<<1, 1024, 0, st>>>(a.out_v, d.target, d.n_rec, N, a.J);
-    // graphs: recompute step (explicit step storing its state), backward step (y ping-pong)
-    const StateStore store{a.seg_u, a.seg_v, a.seg_t0};
-    for (int kk = 0; kk < 2 && !rc; ++kk) {
-      const double* vin = kk == 0 ? g.v : h->v1;
-      double* vout = kk == 0 ? h->v1 : g.v;
-      const double* win = kk == 0 ? h->w0 : h->w1;
-      double* wout = kk == 0 ? h->w1 : h->w0;
-      if ((rc = check(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal), "capture rec"))) break;
-      launch_explicit<3>(h, h->cap, g, vin, vout, win, wout, store);
-      if ((rc = check(cudaStreamEndCapture(h->cap, &rec_graph[kk]), "end rec"))) break;
-      rc = check(cudaGraphInstantiate(&rec_exec[kk], rec_graph[kk], 0), "inst rec");
-    }
-    // backward step: the element kernel (forked onto the second capture stream) and the row
-    // kernel run side by side; they read y[cur] and the segment's states and write disjoint data
-    const int64_t elem_warps = (d.n_elem + 32 / d.n_en - 1) / (32 / d.n_en);
-    const unsigned elem_blocks = grid_for(elem_warps, kAdjElemThreads / 32, 152 * 32);
-    if (!ev_fork && (rc = check(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "event"))) break;
-    if (!ev_join && (rc = check(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "event"))) break;
-    for (int kk = 0; kk < 2 && !rc; ++kk) {
-      if ((rc = check(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal), "capture bwd"))) break;
-      cudaEventRecord(ev_fork, h->cap);
-      cudaStreamWaitEvent(h->cap2, ev_fork, 0);
-      k_adj_elems<<<elem_blocks, kAdjElemThreads, 0, h->cap2>>>(g, d, a, kk, h->explicit_pair);
-      launch_adj_rows(h, h->cap, g, d, a, kk);
-      cudaEventRecord(ev_join, h->cap2);
-      cudaStreamWaitEvent(h->cap, ev_join, 0);
-      if ((rc = check(cudaStreamEndCapture(h->cap, &bwd_graph[kk]), "end bwd"))) break;
-      rc = check(cudaGraphInstantiate(&bwd_exec[kk], bwd_graph[kk], 0), "inst bwd");
-    }
-    if (rc) break;
-    k_adj_init<<<h->vec_blocks, 256, 0, st>>>(g, h->IML, a, d.target, d.n_rec, N, h->explicit_pair);
-    int yk = 0;  // y[yk] holds the y of the next step to reverse
-    for (int sgi = nseg - 1; sgi >= 0 && !rc; --sgi) {
-      const int t0 = sgi * C, t1 = t0 + C < N ? t0 + C : N;
-      t_host[2 * sgi] = t0;
-      t_host[2 * sgi + 1] = t1 - 1;
-      cudaMemcpyAsync(g.u, ck_u + sgi * ns, 8 * ns, cudaMemcpyDeviceToDevice, st);
-      cudaMemcpyAsync(g.v, ck_v + sgi * ns, 8 * ns, cudaMemcpyDeviceToDevice, st);
-      cudaMemcpyAsync(a.seg_u, g.u, 8 * ns, cudaMemcpyDeviceToDevice, st);
-      cudaMemcpyAsync(a.seg_v, g.v, 8 * ns, cudaMemcpyDeviceToDevice, st);
-      cudaMemcpyAsync(a.seg_t0, t_host + 2 * sgi, 4, cudaMemcpyHostToDevice, st);
-      // recompute states t0+1 .. t1 from the checkpoint (f = the entries of step t0)
-      k_w_init<<<h->vec_blocks, 256, 0, st>>>(g, h->w0, h->explicit_pair);
-      cudaMemsetAsync(g.f, 0, 8 * ns, st);
-      k_set_t<<<1, 1, 0, st>>>(g.s, t0);
-      k_force_explicit0<<<1, 256, 0, st>>>(g);
-      int kk = 0;
-      cudaEventRecord(tev[2 + 4 * sgi], st);
-      for (int t = t0; t < t1 && !rc; ++t, kk ^= 1) rc = check(cudaGraphLaunch(rec_exec[kk], st), "rec launch");
-      cudaEventRecord(tev[3 + 4 * sgi], st);
-      // backward t1-1 .. t0
-      cudaMemcpyAsync(a.n_dev, t_host + 2 * sgi + 1, 4, cudaMemcpyHostToDevice, st);
-      cudaMemcpyAsync(a.n_dev_e, t_host + 2 * sgi + 1, 4, cudaMemcpyHostToDevice, st);
-      cudaEventRecord(tev[4 + 4 * sgi], st);
-      k_adj_prep<<<h->vec_blocks, 256, 0, st>>>(g, a, yk, h->explicit_pair);
-      for (int t = t1 - 1; t >= t0 && !rc; --t, yk ^= 1) rc = check(cudaGraphLaunch(bwd_exec[yk], st), "bwd launch");
-      cudaEventRecord(tev[5 + 4 * sgi], st);
-    }
-    if (!rc && J_host) {
-      rc = check(cudaMemcpyAsync(J_host, a.J, 8, cudaMemcpyDeviceToHost, st), "J");
-    }
-    if (!rc) rc = check(cudaStreamSynchronize(st), "sync adjoint");
-    if (!rc) {
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, tev[0], tev[1]);
-      h->adj_ms[0] = ms;
-      h->adj_ms[1] = h->adj_ms[2] = 0.f;
-      for (int sgi = 0; sgi < nseg; ++sgi) {
-        cudaEventElapsedTime(&ms, tev[2 + 4 * sgi], tev[3 + 4 * sgi]);
-        h->adj_ms[1] += ms;
-        cudaEventElapsedTime(&ms, tev[4 + 4 * sgi], tev[5 + 4 * sgi]);
-        h->adj_ms[2] += ms;
-      }
-    }
-  } while (0);
-  cudaStreamSynchronize(st);
-  for (int kk = 0; kk < 2; ++kk) {
-    if (rec_exec[kk]) cudaGraphExecDestroy(rec_exec[kk]);
-    if (rec_graph[kk]) cudaGraphDestroy(rec_graph[kk]);
-    if (bwd_exec[kk]) cudaGraphExecDestroy(bwd_exec[kk]);
-    if (bwd_graph[kk]) cudaGraphDestroy(bwd_graph[kk]);
-  }
-  for (auto ev : tev)
-    if (ev) cudaEventDestroy(ev);
-  if (ev_fork) cudaEventDestroy(ev_fork);
-  if (ev_join) cudaEventDestroy(ev_join);
-  void* frees[] = {ck_u, ck_v, a.seg_u, a.seg_v, a.mu_u, a.mu_v, a.y[0], a.y[1], a.out_v, a.n_dev, a.n_dev_e,
-                   a.ticket_e, a.seg_t0, a.rec_map, a.J, a.wp[0], a.wp[1], a.v32[0], a.v32[1], a.a32[0], a.a32[1],
-                   a.y32[0], a.y32[1]};
-  for (void* q : frees)
-    if (q) cudaFree(q);
-  if (t_host) cudaFreeHost(t_host);
-  sc_nb_set_output(h, o_int, o_nrec, o_rec, o_u, o_v, o_a, o_nout);
-  return rc;
-}
-
-extern "C" int sc_nb_adjoint_timings(sc_nb_newmark* h, float* ms3) {
-  if (!h || !ms3) return SC_BAD_ARG;
-  for (int i = 0; i < 3; ++i) ms3[i] = h->adj_ms[i];
-  return SC_OK;
-}
-
 extern "C" int sc_nb_status(sc_nb_newmark* h, int64_t* total_iters, int* max_iters, int* fsai_fallback_rows) {
   if (!h) return SC_BAD_ARG;
   int rc = check(cudaStreamSynchronize(h->user), "sync");
@@ -2343,7 +1312,6 @@ extern "C" int sc_nb_apply(sc_nb_newmark* h, int which, const double* x, double*
     case 3: {
       // r <- x, t = G r, z = G^T t (the solver's own kernels), y <- z
       k_copy<<<grid_for(g.n_s, 256), 256, 0, st>>>(g.n_s, x, g.r);
-      cudaGraphConditionalHandle none = 0;
       if (g.D == 3) {
         k_prec_lower<3><<<h->node_blocks, kThreads, 0, st>>>(g);
         k_prec_upper_nograph<3><<<h->node_blocks, kThreads, 0, st>>>(g);
@@ -2351,7 +1319,6 @@ extern "C" int sc_nb_apply(sc_nb_newmark* h, int which, const double* x, double*
         k_prec_lower<2><<<h->node_blocks, kThreads, 0, st>>>(g);
         k_prec_upper_nograph<2><<<h->node_blocks, kThreads, 0, st>>>(g);
       }
-      (void)none;
       k_copy<<<grid_for(g.n_s, 256), 256, 0, st>>>(g.n_s, g.z, y);
       break;
     }
@@ -2366,13 +1333,7 @@ extern "C" int sc_nb_destroy(sc_nb_newmark* h) {
   drop_graph(h);
   drop_explicit_graphs(h);
   for (int i = 0; i < h->n_sell_mem; ++i) cudaFree(h->sell_mem[i]);
-  if (h->ML) cudaFree(h->ML);
-  if (h->IML) cudaFree(h->IML);
-  if (h->KPS) cudaFree(h->KPS);
-  if (h->v1) cudaFree(h->v1);
-  if (h->w0) cudaFree(h->w0);
-  if (h->w1) cudaFree(h->w1);
-  if (h->rec_map) cudaFree(h->rec_map);
+  free_explicit(h);
   if (h->cap) cudaStreamDestroy(h->cap);
   if (h->cap2) cudaStreamDestroy(h->cap2);
   delete h;
