@@ -247,6 +247,11 @@ int sc_nb_explicit_run(sc_nb_newmark* h, int t_begin, int t_end);
  * not positive (the reference's 4-point tetra10 mass has negative corner row sums).  No
  * reference counterpart. */
 int sc_nb_set_lumped_mass(sc_nb_newmark* h, const double* ml);
+/* Autotuner of the explicit step (no reference counterpart): threads per node row (1, 2, 4)
+ * chosen by timing `reps` launches of each candidate on the handle; leaves the force entries,
+ * receivers and the caller's u, v as they were.  Pair arithmetic only.  Reports the choice and
+ * its time per step. */
+int sc_nb_tune_explicit(sc_nb_newmark* h, int reps, int* tpr_chosen, float* ms_per_step);
 /* timing aid: the explicit step kernel alone, `reps` launches between CUDA events */
 int sc_nb_time_explicit(sc_nb_newmark* h, int reps, float* ms_per_step);
 /* Adjoint of the explicit scheme (no reference counterpart): misfit

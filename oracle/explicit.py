@@ -22,12 +22,18 @@ def lumped(M):
     return np.asarray(sp.csr_matrix(M).sum(axis=1)).ravel()
 
 
-def solve(M, Cabs, K, alpha, beta, force, n_t, dt, output_interval=1, rec=None):
-    """force: dense [n_t, n] or callable t -> f.  Returns (U, V) at output steps
-    (rows for steps 0, k, 2k, ...), restricted to ``rec`` if given."""
+def hrz(M, factor):
+    """Diagonal-scaled lumped mass: factor * diag(M), factor = sum(M_e) / trace(M_e) of the
+    element (the lumping the ragged path uses for quadratic tetrahedra)."""
+    return factor * sp.csr_matrix(M).diagonal()
+
+
+def solve(M, Cabs, K, alpha, beta, force, n_t, dt, output_interval=1, rec=None, ml=None):
+    """force: dense [n_t, n] or callable t -> f; ml: lumped mass (default: row sums of M).
+    Returns (U, V) at output steps (rows for steps 0, k, 2k, ...), restricted to ``rec``."""
     K = sp.csr_matrix(K)
     Cabs = sp.csr_matrix(Cabs)
-    ml = lumped(M)
+    ml = lumped(M) if ml is None else np.asarray(ml, dtype=float)
     n = K.shape[0]
     get = force if callable(force) else (lambda t: force[t])
     u = np.zeros(n)

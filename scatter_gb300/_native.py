@@ -64,6 +64,7 @@ SIGNATURES = {
     "sc_nb_explicit_run": (I, [P, I, I]),
     "sc_nb_set_lumped_mass": (I, [P, P]),
     "sc_nb_time_explicit": (I, [P, I, ctypes.POINTER(ctypes.c_float)]),
+    "sc_nb_tune_explicit": (I, [P, I, ctypes.POINTER(I), ctypes.POINTER(ctypes.c_float)]),
     "sc_nb_apply": (I, [P, I, P, P]),
     "sc_nb_adjoint": (I, [P, P, ctypes.POINTER(D), P, P]),
     "sc_nb_adjoint_timings": (I, [P, ctypes.POINTER(ctypes.c_float)]),

@@ -530,6 +530,69 @@ extern "C" int sc_nb_set_lumped_mass(sc_nb_newmark* h, const double* ml) {
   return check_launch("lumped mass");
 }
 
+// Threads per node row of the explicit step (1, 2, 4) picked by timing `reps` launches of each
+// candidate (after one untimed launch) on the handle's pair buffers; the force entries and the
+// receiver setting are saved and restored, and the state is rebuilt from the caller's u, v by
+// the next sc_nb_explicit_run, so the timing leaves no trace.  Pair arithmetic only.
+extern "C" int sc_nb_tune_explicit(sc_nb_newmark* h, int reps, int* tpr_chosen, float* ms_per_step) {
+  if (!h || reps <= 0 || !h->explicit_pair) return SC_BAD_ARG;
+  int rc = explicit_prepare(h);
+  if (rc) return rc;
+  Args& g = h->g;
+  cudaStream_t st = h->user;
+  const int64_t ns = g.n_s;
+  float2* f_save = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const int n_rec = g.n_rec;
+  const int tpr0 = h->tpr;
+  const unsigned blocks0 = h->tpr_blocks;
+  float best = -1.f;
+  int best_tpr = tpr0;
+  do {
+    if ((rc = check(cudaMallocAsync((void**)&f_save, 8 * ns, st), "tune malloc"))) break;
+    cudaMemcpyAsync(f_save, h->f2, 8 * ns, cudaMemcpyDeviceToDevice, st);
+    if ((rc = check(cudaEventCreate(&e0), "event")) || (rc = check(cudaEventCreate(&e1), "event"))) break;
+    g.n_rec = 0;  // no receiver records while timing
+    const int cands[3] = {1, 2, 4};
+    for (int ci = 0; ci < 3 && !rc; ++ci) {
+      h->tpr = cands[ci];
+      const int64_t want = (((int64_t)g.n_nodes + 31) / 32 * 32 * h->tpr + kThreads - 1) / kThreads;
+      h->tpr_blocks = (unsigned)(want < 152 * 16 ? (want < 1 ? 1 : want) : 152 * 16);
+      launch_step(h, st, 0, SegStore{});
+      cudaEventRecord(e0, st);
+      for (int i = 0; i < reps; ++i) launch_step(h, st, i & 1, SegStore{});
+      cudaEventRecord(e1, st);
+      if ((rc = check_launch("explicit tune"))) break;
+      if ((rc = check(cudaEventSynchronize(e1), "tune sync"))) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= reps;
+      if (best < 0.f || ms < best) {
+        best = ms;
+        best_tpr = h->tpr;
+      }
+    }
+    cudaMemcpyAsync(h->f2, f_save, 8 * ns, cudaMemcpyDeviceToDevice, st);
+  } while (0);
+  g.n_rec = n_rec;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamSynchronize(st);
+  if (f_save) cudaFree(f_save);
+  if (rc || best < 0.f) {
+    h->tpr = tpr0;
+    h->tpr_blocks = blocks0;
+    return rc ? rc : SC_BAD_ARG;
+  }
+  h->tpr = best_tpr;
+  const int64_t want = (((int64_t)g.n_nodes + 31) / 32 * 32 * h->tpr + kThreads - 1) / kThreads;
+  h->tpr_blocks = (unsigned)(want < 152 * 16 ? (want < 1 ? 1 : want) : 152 * 16);
+  drop_explicit_graphs(h);
+  if (tpr_chosen) *tpr_chosen = best_tpr;
+  if (ms_per_step) *ms_per_step = best;
+  return explicit_prepare(h);
+}
+
 extern "C" int sc_nb_time_explicit(sc_nb_newmark* h, int reps, float* ms_per_step) {
   if (!h || reps <= 0 || !ms_per_step || !h->ex_exec[0]) return SC_BAD_ARG;
   cudaStream_t st = h->user;

@@ -275,6 +275,12 @@ class NodeBlockNewmark:
     def run_explicit(self, t_begin, t_end):
         nat.call("sc_nb_explicit_run", self.h, int(t_begin), int(t_end))
 
+    def tune_explicit(self, reps=5):
+        """Pick the explicit step's threads per node row by timing; returns (choice, ms/step)."""
+        tpr, ms = ctypes.c_int(), ctypes.c_float()
+        nat.call("sc_nb_tune_explicit", self.h, int(reps), ctypes.byref(tpr), ctypes.byref(ms))
+        return tpr.value, ms.value
+
     def time_explicit(self, reps=20):
         ms = ctypes.c_float()
         nat.call("sc_nb_time_explicit", self.h, int(reps), ctypes.byref(ms))

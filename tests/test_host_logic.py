@@ -117,3 +117,37 @@ def test_validator_defaults():
     assert load["ini_steps"] == 5
     with pytest.raises(Exception):
         ValidateLoad.validate({"type": "unknown"})
+
+
+def test_ragged_mesh_specs_seeded():
+    from scatter_gb300.ragged import mesh_specs
+
+    a = mesh_specs(64, seed=3)
+    b = mesh_specs(64, seed=3)
+    assert a == b and len(a) == 64
+    assert {s["element"] for s in a} == {"hexa8", "tetra10"}
+    for s in a:
+        lo, hi = (10, 80) if s["element"] == "hexa8" else (5, 40)
+        assert all(lo <= d <= hi for d in s["dims"])
+        assert 20e6 <= s["E"] <= 200e6 and 0.2 <= s["nu"] <= 0.35 and 1700 <= s["rho"] <= 2100
+
+
+def test_hrz_lumping_of_the_reference_tetra10_mass_is_positive():
+    """Row sums of the reference's tetra10 consistent mass are negative at the corners, so the
+    ragged path lumps quadratic tetrahedra by diagonal scaling; the oracle's HRZ mass is
+    positive and keeps the element mass."""
+    import numpy as np
+
+    from oracle import elements as el
+    from scatter_gb300 import meshgen
+
+    m = meshgen.box_model(1, 1, 1, 0.5, element="tetra10")
+    X = m.nodes[:, 1:][m.node_index()[m.elem]]
+    n = len(m.elem)
+    _, Me = el.element_matrices("tetra10", X, np.ones(n), np.full(n, 0.3), np.full(n, 2000.0))
+    Mx = Me[0][::3, ::3]
+    assert Mx.sum(axis=1)[:4].max() < 0  # corner row sums
+    f = Mx.sum() / np.trace(Mx)
+    lumped = f * np.diag(Mx)
+    assert lumped.min() > 0
+    assert abs(lumped.sum() / Mx.sum() - 1) < 1e-12
