@@ -75,7 +75,7 @@ def peaks():
 
 def profile_traffic():
     """dram bytes per launch of the SpMV kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "k_spmv_box120x80x60.md")
+    path = os.path.join(ROOT, "profiles", "k_spmv_pair_box120x80x60.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -260,13 +260,15 @@ def run_gb300(args):
                       "parallelism": f"replicas x{ws}",
                       "l2": "inputs larger than L2 (CSR values+cols 5.1 GB), no flush",
                       "solver": "Newmark beta=1/4 gamma=1/2; per step PCG (FSAI preconditioner, FP32 factor), "
-                                "quadratic warm start, rtol 1e-12; node-block FP64 operator"},
+                                "quadratic warm start, rtol 1e-12; node-block operator, SpMV products in FP32 "
+                                "pairs, residual, dot products and state FP64"},
            "cg_iters_per_step": iters / K_steps, "cg_iters_max": it_max,
            "setup_s": {"host_mesh_and_loads": round(t_host, 2), "gpu_assembly_lysmer_rayleigh": round(t_assembly, 3),
                        "gpu_solver_setup_fsai": round(t_solver_setup, 3)},
            "fsai_fallback_rows": solver.fsai_fallback_rows,
            "gpu_launches": 8 * K_steps + 5 * iters + 1,
-           "roofline": {"bound": "hbm", "kernel": "nb::k_spmv (3x3 node blocks FP64, w = A p)", "achieved": achieved,
+           "roofline": {"bound": "hbm", "kernel": "nb::k_spmv_pair (PCG w = A p, 3x3 node blocks, FP32-pair products)",
+                        "achieved": achieved,
                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                         "traffic": traffic, "bytes_per_launch": bytes_spmv, "ms_per_launch": ms_spmv},
            "clocks": clk.summary(), "e2e": e2e, "explicit_lumped": explicit, "batched": batched,
@@ -308,7 +310,8 @@ def explicit_run(g, table, rec_eq, k, w, n):
     return {"value": n * k / (ms / 1e3), "unit": "DOF-steps/s", "ms_per_step": ms / k, "steps": k,
             "dt": DT, "dt_critical_bound": dtc, "kernel_ms": ms_k,
             "kernel_gbs": bytes_step / (ms_k * 1e-3) / 1e9,
-            "note": "central difference, row-sum lumped mass (no reference counterpart); FP64"}
+            "note": "central difference, row-sum lumped mass (no reference counterpart); u, v, K w in FP32 (hi, lo) "
+                    "pairs, FP64 at the run boundary"}
 
 
 def _top_receivers(model, n, seed):
