@@ -120,6 +120,46 @@ __device__ __forceinline__ void pair_madd(float2& x, float a, float b, float ext
   x = make_float2(h, __fsub_rn(lo, __fsub_rn(h, t)));
 }
 
+// t += k2 w2, then k1 w1, then k0 w0, per realisation; pairs of realisations use the paired
+// FP32 FMA (two independently rounded FMAs in one instruction: the same values as fmaf, half
+// the issue slots)
+template <int RPT>
+__device__ __forceinline__ void fma3(float (&t)[RPT], float k0, float k1, float k2, const float (&w0)[RPT],
+                                     const float (&w1)[RPT], const float (&w2)[RPT]) {
+  if constexpr (RPT % 2 == 0) {
+    const float2 K0 = make_float2(k0, k0), K1 = make_float2(k1, k1), K2 = make_float2(k2, k2);
+#pragma unroll
+    for (int r = 0; r < RPT; r += 2) {
+      float2 x = make_float2(t[r], t[r + 1]);
+      x = __ffma2_rn(K2, make_float2(w2[r], w2[r + 1]), x);
+      x = __ffma2_rn(K1, make_float2(w1[r], w1[r + 1]), x);
+      x = __ffma2_rn(K0, make_float2(w0[r], w0[r + 1]), x);
+      t[r] = x.x;
+      t[r + 1] = x.y;
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) t[r] = fmaf(k0, w0[r], fmaf(k1, w1[r], fmaf(k2, w2[r], t[r])));
+  }
+}
+
+// acc += E t per realisation (paired as above)
+template <int RPT>
+__device__ __forceinline__ void fma1(float (&acc)[RPT], const float (&E)[RPT], const float (&t)[RPT]) {
+  if constexpr (RPT % 2 == 0) {
+#pragma unroll
+    for (int r = 0; r < RPT; r += 2) {
+      const float2 x = __ffma2_rn(make_float2(E[r], E[r + 1]), make_float2(t[r], t[r + 1]),
+                                  make_float2(acc[r], acc[r + 1]));
+      acc[r] = x.x;
+      acc[r + 1] = x.y;
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) acc[r] = fmaf(E[r], t[r], acc[r]);
+  }
+}
+
 __device__ inline bool batch_last_block(unsigned* ticket) {
   __shared__ bool am_last;
   __threadfence();
@@ -174,18 +214,13 @@ __global__ void __launch_bounds__(256) k_batch_step(Args g, const float* __restr
         ldf<RPT>(w_in + (bs + 2) * R + r0, w2);
         const float* kr = K1 + lb * 3;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float k0 = __ldg(kr + c * ND + 0), k1 = __ldg(kr + c * ND + 1), k2 = __ldg(kr + c * ND + 2);
-#pragma unroll
-          for (int r = 0; r < RPT; ++r) t[c][r] = fmaf(k0, w0[r], fmaf(k1, w1[r], fmaf(k2, w2[r], t[c][r])));
-        }
+        for (int c = 0; c < 3; ++c)
+          fma3<RPT>(t[c], __ldg(kr + c * ND + 0), __ldg(kr + c * ND + 1), __ldg(kr + c * ND + 2), w0, w1, w2);
       }
       float Ee[RPT];
       ldf<RPT>(d.young + (int64_t)e * R + r0, Ee);
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int r = 0; r < RPT; ++r) acc[c][r] = fmaf(Ee[r], t[c][r], acc[c][r]);
+      for (int c = 0; c < 3; ++c) fma1<RPT>(acc[c], Ee, t[c]);
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {

@@ -56,6 +56,7 @@ struct Args {
   double *u, *v, *a, *a1, *a2;
   double *q1, *q2, *y1, *x0, *x, *r, *z, *p, *w, *f;
   float* t32;
+  float* r32;  // FP32 copy of r, written with r: the lower FSAI half gathers it (no FP64 conversion per gather)
   double* part;
   Scal* s;
   // force (slot indices)

@@ -163,6 +163,7 @@ __global__ void __launch_bounds__(kThreads) k_residual(Args g) {
           rv = kPair ? bv - sx[c] : bv - (sx[c] + g.aC * cx);
         }
         g.r[i] = rv;
+        g.r32[i] = (float)rv;
         g.x[i] = g.x0[i];
         pbb += bv * bv;
       }
@@ -196,7 +197,7 @@ __global__ void __launch_bounds__(kThreads) k_prec_lower(Args g) {
 #pragma unroll
       for (int e = 0; e < 4; ++e)
 #pragma unroll
-        for (int d = 0; d < D; ++d) ra[e][d] = (float)g.r[(int64_t)cl[e] * D + d];
+        for (int d = 0; d < D; ++d) ra[e][d] = g.r32[(int64_t)cl[e] * D + d];
 #pragma unroll
       for (int c = 0; c < D; ++c)
 #pragma unroll
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(kThreads) k_prec_upper(Args g, int mode, cudaG
         g.z[i] = z;
         if (mode == 1) {
           g.p[i] = z;
-          if (g.spmv_pair) g.p2[i] = split_pair(z);
+          if (g.spmv_pair) g.p2[i] = make_float2(s[c], 0.f);  // z is an FP32 value: the pair is exact
         }
         prz += r * z;
         prr += r * r;
@@ -452,6 +453,7 @@ __global__ void k_update(Args g, cudaGraphConditionalHandle hc) {
     g.x[i] = fma(alpha, g.p[i], g.x[i]);
     const double r = fma(-alpha, g.w[i], g.r[i]);
     g.r[i] = r;
+    g.r32[i] = (float)r;
     prr += r * r;
   }
   const double t = block_sum(prr, sh);
@@ -965,7 +967,7 @@ extern "C" int64_t sc_nb_workspace_bytes(int n_nodes, int dim, int64_t nnzb) {
   b += align256(8 * nnzb);                    // MS
   b += 2 * align256(4 * D2 * nnzb);           // GB, GTB
   b += 13 * align256(8 * ns);                 // a1 a2 q1 q2 y1 x0 x r z p w f (+1 spare)
-  b += align256(4 * ns);                      // t32
+  b += 2 * align256(4 * ns);                  // t32, r32
   b += align256(8 * 4 * 152 * 16);            // partials
   b += align256(sizeof(Scal));
   return b;
@@ -1042,6 +1044,7 @@ extern "C" int sc_nb_create(sc_nb_newmark** out, int n_nodes, int dim, const int
   g.p2 = (float2*)take(8 * ns);
   g.spmv_pair = 1;
   g.t32 = (float*)take(4 * ns);
+  g.r32 = (float*)take(4 * ns);
   g.part = (double*)take(8 * 4 * 152 * 16);
   g.s = (Scal*)take(sizeof(Scal));
   h->node_blocks = node_grid(n_nodes);
@@ -1299,6 +1302,13 @@ __global__ void k_copy(int64_t n, const double* __restrict__ x, double* __restri
     y[i] = x[i];
 }
 
+__global__ void k_copy_r(int64_t n, const double* __restrict__ x, double* __restrict__ r, float* __restrict__ r32) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    r[i] = x[i];
+    r32[i] = (float)x[i];
+  }
+}
+
 extern "C" int sc_nb_apply(sc_nb_newmark* h, int which, const double* x, double* y) {
   if (!h || !x || !y || which < 0 || which > 4) return SC_BAD_ARG;
   Args g = h->g;
@@ -1311,7 +1321,7 @@ extern "C" int sc_nb_apply(sc_nb_newmark* h, int which, const double* x, double*
     case 4: k_apply_cab<<<grid_for(g.n_s, 256), 256, 0, st>>>(g, x, y); break;
     case 3: {
       // r <- x, t = G r, z = G^T t (the solver's own kernels), y <- z
-      k_copy<<<grid_for(g.n_s, 256), 256, 0, st>>>(g.n_s, x, g.r);
+      k_copy_r<<<grid_for(g.n_s, 256), 256, 0, st>>>(g.n_s, x, g.r, g.r32);
       if (g.D == 3) {
         k_prec_lower<3><<<h->node_blocks, kThreads, 0, st>>>(g);
         k_prec_upper_nograph<3><<<h->node_blocks, kThreads, 0, st>>>(g);
