@@ -64,8 +64,16 @@ def absorbing(model, props, parameters_viscous, parameters_stiff, order=2):
     etype = str(model["element_type"])
     dim = el.DIM[etype]
     n_eq = int(model["number_eq"])
-    C = sp.lil_matrix((n_eq, n_eq))
-    Kst = sp.lil_matrix((n_eq, n_eq))
+    # entries collected per face in face order and summed by the sparse constructor (the
+    # reference adds face by face into lil matrices, system_matrix.py:362-376); the
+    # equation -> (node, dof) inverse of eq_nb_dof replaces the reference's np.where search
+    c_r, c_c, c_v, k_v = [], [], [], []
+    free = ~np.isnan(eq_nb_dof)
+    eq_node = np.full(n_eq, -1, dtype=np.int64)
+    eq_dof = np.full(n_eq, -1, dtype=np.int64)
+    nn, dd = np.nonzero(free)
+    eq_node[eq_nb_dof[nn, dd].astype(np.int64)] = nn
+    eq_dof[eq_nb_dof[nn, dd].astype(np.int64)] = dd
     if dim != 3:
         return sp.csr_matrix((n_eq, n_eq)), sp.csr_matrix((n_eq, n_eq))
     ftype = el.LOWER[etype]
@@ -73,7 +81,12 @@ def absorbing(model, props, parameters_viscous, parameters_stiff, order=2):
     id2idx = {int(n): i for i, n in enumerate(nodes[:, 0])}
     absorb = BC == 2
     E_, nu_, rho_ = props
-    for e in range(len(elem)):
+    # elements with no absorbing node contribute nothing: visit only the others
+    ids = nodes[:, 0].astype(np.int64)
+    idmap = np.full(int(ids.max()) + 1, -1, dtype=np.int64)
+    idmap[ids] = np.arange(len(ids))
+    touching = np.nonzero(absorb.any(axis=1)[idmap[elem]].any(axis=1))[0]
+    for e in touching:
         idx = [id2idx[int(n)] for n in elem[e]]
         sel = [i for i in idx if absorb[i].any()]
         if not sel:
@@ -96,10 +109,18 @@ def absorbing(model, props, parameters_viscous, parameters_stiff, order=2):
             fct = np.full(nf, parameters_viscous[1] * rho * vs)
             fct2 = np.full(nf, G)
             for k, val in enumerate(i1):
-                j = np.where(eq_nb_dof == val)
-                if BC_dir[j[0], j[1]] == 1:
+                if BC_dir[eq_node[val], eq_dof[val]] == 1:
                     fct[k] = parameters_viscous[0] * rho * vp
                     fct2[k] = Ec
-            C[i1.reshape(-1, 1), i1] = C[i1.reshape(-1, 1), i1] + F * fct
-            Kst[i1.reshape(-1, 1), i1] = Kst[i1.reshape(-1, 1), i1] + np.abs(F) * fct2
-    return sp.csr_matrix(C), sp.csr_matrix(Kst) / parameters_stiff
+            c_r.append(np.repeat(i1, nf))
+            c_c.append(np.tile(i1, nf))
+            c_v.append((F * fct).ravel())
+            k_v.append((np.abs(F) * fct2).ravel())
+    if not c_r:
+        return sp.csr_matrix((n_eq, n_eq)), sp.csr_matrix((n_eq, n_eq))
+    r, c = np.concatenate(c_r), np.concatenate(c_c)
+    C = sp.csr_matrix((np.concatenate(c_v), (r, c)), shape=(n_eq, n_eq))
+    Kst = sp.csr_matrix((np.concatenate(k_v), (r, c)), shape=(n_eq, n_eq))
+    C.sum_duplicates()
+    Kst.sum_duplicates()
+    return C, Kst / parameters_stiff
