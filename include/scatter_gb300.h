@@ -294,6 +294,10 @@ int sc_nb_destroy(sc_nb_newmark* h);
  *   u, v [3 n_nodes][R] FP64 state, read at the start and written at the end of each run (the
  *   step kernel accumulates in FP32 (hi, lo) pairs).  Setup allocates the ping-pong copies and
  *   the pair accumulators; runs allocate nothing.
+ *   node_nen [n_nodes] (optional, uint8): for independent meshes of different element types
+ *     concatenated into one system (one realisation, R = 1): each node's element size; elem
+ *     rows and ke1 tables then use the largest type's stride (n_en, 3 n_en), shorter types
+ *     padded.  NULL: every element has n_en nodes.
  * R <= 1024 (above 256: even up to 512, else divisible by 4); n_en in {4, 8, 10, 20}. */
 typedef struct sc_batch_desc sc_batch_desc;
 typedef struct sc_batch sc_batch;

@@ -24,7 +24,7 @@ class _Desc(ctypes.Structure):
                 ("young", ctypes.c_void_p), ("ml", ctypes.c_void_p), ("fixed", ctypes.c_void_p),
                 ("alpha", ctypes.c_double), ("beta", ctypes.c_double), ("dt", ctypes.c_double),
                 ("l_ptr", ctypes.c_void_p), ("l_col", ctypes.c_void_p), ("l_elem", ctypes.c_void_p),
-                ("l_c", ctypes.c_void_p), ("l_s", ctypes.c_void_p)]
+                ("l_c", ctypes.c_void_p), ("l_s", ctypes.c_void_p), ("node_nen", ctypes.c_void_p)]
 
 
 def element_types(model, nu, tol=1e-9):
@@ -102,7 +102,7 @@ class BatchedExplicit:
         d = _Desc(N, n_elem, n_en, R, self.n_types, self.elem.data_ptr(), self.inc_ptr.data_ptr(), self.inc.data_ptr(),
                   self.ke_type.data_ptr(), self.ke1.data_ptr(), self.young.data_ptr(), self.ml.data_ptr(),
                   self.fixed.data_ptr(), float(alpha), float(beta), float(dt), self.l_ptr.data_ptr(),
-                  self.l_col.data_ptr(), self.l_elem.data_ptr(), self.l_c.data_ptr(), self.l_s.data_ptr())
+                  self.l_col.data_ptr(), self.l_elem.data_ptr(), self.l_c.data_ptr(), self.l_s.data_ptr(), None)
         self._desc = d
         h = ctypes.c_void_p()
         nat.call("sc_batch_create", ctypes.byref(h), ctypes.byref(d), self.u.data_ptr(), self.v.data_ptr(), s)

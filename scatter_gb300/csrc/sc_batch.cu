@@ -28,6 +28,7 @@ struct sc_batch_desc {
   const int64_t* l_ptr;
   const int *l_col, *l_elem;
   const float *l_c, *l_s;
+  const unsigned char* node_nen;  // mixed element types: nodes per element of each node's mesh (NULL: all n_en)
 };
 
 namespace sc {
@@ -169,120 +170,125 @@ __device__ inline bool batch_last_block(unsigned* ticket) {
   return am_last;
 }
 
-// One step for all realisations.  tpn threads per node (tpn * RPT >= R), blockDim / tpn
-// nodes per block.  The last block to finish advances the step counter and swaps the force
-// entries in f from step t to step t + 1 (every block has read f by then).
+// Stiffness forces on node a for RPT realisations: sum over the node's incident elements of
+// E_e K1_e(a, :) w_e.  Element connectivity rows have `estride` entries and K1 tables rows of
+// `kstride` (3 NEN for a single element type; the largest type's for mixed meshes).
 template <int NEN, int RPT>
-__global__ void __launch_bounds__(256) k_batch_step(Args g, const float* __restrict__ w_in, float* __restrict__ w_out,
-                                                    const float* __restrict__ vf_in, float* __restrict__ vf_out,
-                                                    int tpn) {
+__device__ __forceinline__ void node_forces(const Args& g, const float* __restrict__ w_in, int a, int r0, int estride,
+                                            int kstride, float (&acc)[3][RPT]) {
   const sc_batch_desc& d = g.d;
   const int R = d.R;
-  constexpr int ND = NEN * 3;
-  const int npb = blockDim.x / tpn;
-  const int sub = threadIdx.x / tpn;
-  const int r0 = (threadIdx.x % tpn) * RPT;
-  const bool active = sub < npb && r0 < R;
-  const int step = *g.t + 1;
-  const bool rec_now = g.n_rec > 0 && g.out_interval > 0 && step % g.out_interval == 0 &&
-                       step / g.out_interval < g.n_out;
-  for (int a = blockIdx.x * npb + sub; active && a < d.n_nodes; a += gridDim.x * npb) {
-    float acc[3][RPT];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) acc[c][r] = 0.f;
+  for (int k = d.inc_ptr[a]; k < d.inc_ptr[a + 1]; ++k) {
+    const int e = d.inc[k];
+    const int* en = d.elem + (int64_t)e * estride;
+    int la = 0;
+#pragma unroll
+    for (int q = 0; q < NEN; ++q)
+      if (en[q] == a) la = q;
+    const float* K1 = d.ke1 + (int64_t)d.ke_type[e] * kstride * kstride + (int64_t)(la * 3) * kstride;
+    float t[3][RPT];
 #pragma unroll
     for (int c = 0; c < 3; ++c)
 #pragma unroll
-      for (int r = 0; r < RPT; ++r) acc[c][r] = 0.f;
-    for (int k = d.inc_ptr[a]; k < d.inc_ptr[a + 1]; ++k) {
-      const int e = d.inc[k];
-      const int* en = d.elem + (int64_t)e * NEN;
-      int la = 0;
-#pragma unroll
-      for (int q = 0; q < NEN; ++q)
-        if (en[q] == a) la = q;
-      const float* K1 = d.ke1 + (int64_t)d.ke_type[e] * ND * ND + (int64_t)(la * 3) * ND;
-      float t[3][RPT];
+      for (int r = 0; r < RPT; ++r) t[c][r] = 0.f;
+#pragma unroll 2
+    for (int lb = 0; lb < NEN; ++lb) {
+      const int64_t bs = (int64_t)en[lb] * 3;
+      float w0[RPT], w1[RPT], w2[RPT];
+      ldf<RPT>(w_in + (bs + 0) * R + r0, w0);
+      ldf<RPT>(w_in + (bs + 1) * R + r0, w1);
+      ldf<RPT>(w_in + (bs + 2) * R + r0, w2);
+      const float* kr = K1 + lb * 3;
 #pragma unroll
       for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int r = 0; r < RPT; ++r) t[c][r] = 0.f;
-#pragma unroll 2
-      for (int lb = 0; lb < NEN; ++lb) {
-        const int64_t bs = (int64_t)en[lb] * 3;
-        float w0[RPT], w1[RPT], w2[RPT];
-        ldf<RPT>(w_in + (bs + 0) * R + r0, w0);
-        ldf<RPT>(w_in + (bs + 1) * R + r0, w1);
-        ldf<RPT>(w_in + (bs + 2) * R + r0, w2);
-        const float* kr = K1 + lb * 3;
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-          fma3<RPT>(t[c], __ldg(kr + c * ND + 0), __ldg(kr + c * ND + 1), __ldg(kr + c * ND + 2), w0, w1, w2);
-      }
-      float Ee[RPT];
-      ldf<RPT>(d.young + (int64_t)e * R + r0, Ee);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) fma1<RPT>(acc[c], Ee, t[c]);
+        fma3<RPT>(t[c], __ldg(kr + c * kstride + 0), __ldg(kr + c * kstride + 1), __ldg(kr + c * kstride + 2), w0,
+                  w1, w2);
     }
+    float Ee[RPT];
+    ldf<RPT>(d.young + (int64_t)e * R + r0, Ee);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const int64_t i = (int64_t)a * 3 + c;
-      const int64_t ir = i * R + r0;
-      float wo[RPT], vo[RPT];
-      if (d.fixed[i]) {
+    for (int c = 0; c < 3; ++c) fma1<RPT>(acc[c], Ee, t[c]);
+  }
+}
+
+// The update of node a's DOFs for RPT realisations (Lysmer terms, FP32 acceleration, pair
+// accumulators, FP32 copies, receivers)
+template <int RPT>
+__device__ __forceinline__ void node_update(const Args& g, int a, int r0, const float (&acc)[3][RPT],
+                                            const float* __restrict__ w_in, float* __restrict__ w_out,
+                                            const float* __restrict__ vf_in, float* __restrict__ vf_out, int step,
+                                            bool rec_now) {
+  const sc_batch_desc& d = g.d;
+  const int R = d.R;
 #pragma unroll
-        for (int r = 0; r < RPT; ++r) wo[r] = vo[r] = 0.f;
-        stf<RPT>(w_out + ir, wo);
-        stf<RPT>(vf_out + ir, vo);
-        continue;
-      }
-      float spring[RPT], dash[RPT];
+  for (int c = 0; c < 3; ++c) {
+    const int64_t i = (int64_t)a * 3 + c;
+    const int64_t ir = i * R + r0;
+    float wo[RPT], vo[RPT];
+    if (d.fixed[i]) {
 #pragma unroll
-      for (int r = 0; r < RPT; ++r) spring[r] = dash[r] = 0.f;
-      for (int64_t q = d.l_ptr[i]; q < d.l_ptr[i + 1]; ++q) {
-        const int64_t jr = (int64_t)d.l_col[q] * R + r0;
-        float Eq[RPT], wj[RPT], vj[RPT];
-        ldf<RPT>(d.young + (int64_t)d.l_elem[q] * R + r0, Eq);
-        ldf<RPT>(w_in + jr, wj);
-        ldf<RPT>(vf_in + jr, vj);
-        const float ls = d.l_s[q], lc = d.l_c[q];
-#pragma unroll
-        for (int r = 0; r < RPT; ++r) {
-          spring[r] = fmaf(__fmul_rn(ls, Eq[r]), wj[r], spring[r]);
-          dash[r] = fmaf(__fmul_rn(lc, sqrtf(Eq[r])), vj[r], dash[r]);
-        }
-      }
-      float2 vp[RPT], up[RPT];
-      float vown[RPT];
-      ldp<RPT>(g.v2 + ir, vp);
-      ldp<RPT>(g.u2 + ir, up);
-      ldf<RPT>(vf_in + ir, vown);
-      const float fi = (float)g.f[i], mlf = g.ml32[i], imlf = g.iml32[i];
-      const float aml = __fmul_rn(g.alpha32, mlf);
-#pragma unroll
-      for (int r = 0; r < RPT; ++r) {
-        // FP32 acceleration (its inputs are FP32 products); _rn intrinsics keep the rounding
-        // the same for every kernel shape
-        const float kw = __fadd_rn(acc[c][r], spring[r]);
-        const float num = __fsub_rn(__fsub_rn(__fsub_rn(fi, kw), __fmul_rn(aml, vown[r])), dash[r]);
-        const float accel = __fmul_rn(num, imlf);
-        pair_madd(vp[r], g.dth, accel, __fmul_rn(g.dtl, accel));                           // v += dt a
-        pair_madd(up[r], g.dth, vp[r].x, fmaf(g.dth, vp[r].y, __fmul_rn(g.dtl, vp[r].x)));  // u += dt v
-        wo[r] = fmaf(g.beta32, vp[r].x, up[r].x);
-        vo[r] = vp[r].x;
-      }
-      stp<RPT>(g.v2 + ir, vp);
-      stp<RPT>(g.u2 + ir, up);
+      for (int r = 0; r < RPT; ++r) wo[r] = vo[r] = 0.f;
       stf<RPT>(w_out + ir, wo);
       stf<RPT>(vf_out + ir, vo);
-      if (rec_now) {
-        const int rj = g.rec_map[i];
-        if (rj >= 0) {
-          double* o = g.out_v + ((int64_t)(step / g.out_interval) * g.n_rec + rj) * R + r0;
+      continue;
+    }
+    float spring[RPT], dash[RPT];
 #pragma unroll
-          for (int r = 0; r < RPT; ++r) o[r] = (double)vp[r].x + (double)vp[r].y;
-        }
+    for (int r = 0; r < RPT; ++r) spring[r] = dash[r] = 0.f;
+    for (int64_t q = d.l_ptr[i]; q < d.l_ptr[i + 1]; ++q) {
+      const int64_t jr = (int64_t)d.l_col[q] * R + r0;
+      float Eq[RPT], wj[RPT], vj[RPT];
+      ldf<RPT>(d.young + (int64_t)d.l_elem[q] * R + r0, Eq);
+      ldf<RPT>(w_in + jr, wj);
+      ldf<RPT>(vf_in + jr, vj);
+      const float ls = d.l_s[q], lc = d.l_c[q];
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) {
+        spring[r] = fmaf(__fmul_rn(ls, Eq[r]), wj[r], spring[r]);
+        dash[r] = fmaf(__fmul_rn(lc, sqrtf(Eq[r])), vj[r], dash[r]);
+      }
+    }
+    float2 vp[RPT], up[RPT];
+    float vown[RPT];
+    ldp<RPT>(g.v2 + ir, vp);
+    ldp<RPT>(g.u2 + ir, up);
+    ldf<RPT>(vf_in + ir, vown);
+    const float fi = (float)g.f[i], mlf = g.ml32[i], imlf = g.iml32[i];
+    const float aml = __fmul_rn(g.alpha32, mlf);
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+      // FP32 acceleration (its inputs are FP32 products); _rn intrinsics keep the rounding
+      // the same for every kernel shape
+      const float kw = __fadd_rn(acc[c][r], spring[r]);
+      const float num = __fsub_rn(__fsub_rn(__fsub_rn(fi, kw), __fmul_rn(aml, vown[r])), dash[r]);
+      const float accel = __fmul_rn(num, imlf);
+      pair_madd(vp[r], g.dth, accel, __fmul_rn(g.dtl, accel));                           // v += dt a
+      pair_madd(up[r], g.dth, vp[r].x, fmaf(g.dth, vp[r].y, __fmul_rn(g.dtl, vp[r].x)));  // u += dt v
+      wo[r] = fmaf(g.beta32, vp[r].x, up[r].x);
+      vo[r] = vp[r].x;
+    }
+    stp<RPT>(g.v2 + ir, vp);
+    stp<RPT>(g.u2 + ir, up);
+    stf<RPT>(w_out + ir, wo);
+    stf<RPT>(vf_out + ir, vo);
+    if (rec_now) {
+      const int rj = g.rec_map[i];
+      if (rj >= 0) {
+        double* o = g.out_v + ((int64_t)(step / g.out_interval) * g.n_rec + rj) * R + r0;
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) o[r] = (double)vp[r].x + (double)vp[r].y;
       }
     }
   }
+}
+
+// The last block to finish advances the step counter and swaps the force entries in f from
+// step t to step t + 1 (every block has read f by then).
+__device__ __forceinline__ void step_epilogue(const Args& g, int step) {
   if (batch_last_block(g.ticket)) {
     const int t = step - 1;
     if (g.f_ptr) {
@@ -297,6 +303,52 @@ __global__ void __launch_bounds__(256) k_batch_step(Args g, const float* __restr
       *g.t = step;
     }
   }
+}
+
+__device__ __forceinline__ bool record_now(const Args& g, int step) {
+  return g.n_rec > 0 && g.out_interval > 0 && step % g.out_interval == 0 && step / g.out_interval < g.n_out;
+}
+
+// One step for all realisations.  tpn threads per node (tpn * RPT >= R), blockDim / tpn
+// nodes per block.
+template <int NEN, int RPT>
+__global__ void __launch_bounds__(256) k_batch_step(Args g, const float* __restrict__ w_in, float* __restrict__ w_out,
+                                                    const float* __restrict__ vf_in, float* __restrict__ vf_out,
+                                                    int tpn) {
+  const int npb = blockDim.x / tpn;
+  const int sub = threadIdx.x / tpn;
+  const int r0 = (threadIdx.x % tpn) * RPT;
+  const bool active = sub < npb && r0 < g.d.R;
+  const int step = *g.t + 1;
+  const bool rec_now = record_now(g, step);
+  for (int a = blockIdx.x * npb + sub; active && a < g.d.n_nodes; a += gridDim.x * npb) {
+    float acc[3][RPT];
+    node_forces<NEN, RPT>(g, w_in, a, r0, NEN, 3 * NEN, acc);
+    node_update<RPT>(g, a, r0, acc, w_in, w_out, vf_in, vf_out, step, rec_now);
+  }
+  step_epilogue(g, step);
+}
+
+// Mixed element types (independent meshes of different types concatenated, one realisation):
+// one thread per node, the node's mesh type selecting the element loop.  Connectivity rows
+// and K1 tables use the largest type's stride.
+__global__ void __launch_bounds__(256) k_batch_step_mixed(Args g, const float* __restrict__ w_in,
+                                                          float* __restrict__ w_out, const float* __restrict__ vf_in,
+                                                          float* __restrict__ vf_out) {
+  const int step = *g.t + 1;
+  const bool rec_now = record_now(g, step);
+  const int es = g.d.n_en, ks = 3 * g.d.n_en;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < g.d.n_nodes; a += gridDim.x * blockDim.x) {
+    float acc[3][1];
+    switch (g.d.node_nen[a]) {
+      case 4: node_forces<4, 1>(g, w_in, a, 0, es, ks, acc); break;
+      case 8: node_forces<8, 1>(g, w_in, a, 0, es, ks, acc); break;
+      case 10: node_forces<10, 1>(g, w_in, a, 0, es, ks, acc); break;
+      default: node_forces<20, 1>(g, w_in, a, 0, es, ks, acc); break;
+    }
+    node_update<1>(g, a, 0, acc, w_in, w_out, vf_in, vf_out, step, rec_now);
+  }
+  step_epilogue(g, step);
 }
 
 __device__ inline float2 split2(double x) {
@@ -385,6 +437,10 @@ static void batch_launch(const sc_batch* h, const Args& g, int rpt, int threads,
   const int npb = threads / tpn;
   const int64_t want = ((int64_t)g.d.n_nodes + npb - 1) / npb;
   const unsigned blocks = (unsigned)(want < 152 * 32 ? want : 152 * 32);
+  if (g.d.node_nen) {
+    k_batch_step_mixed<<<blocks, threads, 0, st>>>(g, wi, wo, vi, vo);
+    return;
+  }
   switch (g.d.n_en) {
     case 8: launch_rpt<8>(rpt, blocks, threads, tpn, st, g, wi, wo, vi, vo); break;
     case 4: launch_rpt<4>(rpt, blocks, threads, tpn, st, g, wi, wo, vi, vo); break;
@@ -435,12 +491,14 @@ static int batch_tune(sc_batch* h) {
     g.f_ptr = nullptr;
     g.n_rec = 0;
     const int rpts[4] = {1, 2, 4, 8};
-    const int tpbs[2] = {128, 256};
+    const int tpbs[3] = {128, 256, 64};
+    const bool mixed = g0.d.node_nen != nullptr;  // one realisation, one thread per node
     for (int ri = 0; ri < 4 && !rc; ++ri) {
       const int rpt = rpts[ri];
       if (R % rpt != 0 || (rpt >= 4 && R % 4 != 0)) continue;
+      if (mixed && rpt != 1) continue;
       const int tpn = (R + rpt - 1) / rpt;
-      for (int bi = 0; bi < 2 && !rc; ++bi) {
+      for (int bi = 0; bi < (mixed ? 3 : 2) && !rc; ++bi) {
         if (tpn > tpbs[bi]) continue;
         const int threads = (tpbs[bi] / tpn) * tpn;
         float* wh = w;
@@ -502,6 +560,7 @@ extern "C" int sc_batch_create(sc_batch** out, const sc_batch_desc* d, double* u
     return SC_BAD_ARG;
   if (d->n_en != 8 && d->n_en != 4 && d->n_en != 10 && d->n_en != 20) return SC_BAD_ARG;
   if (!(d->dt > 0)) return SC_BAD_ARG;
+  if (d->node_nen && d->R != 1) return SC_BAD_ARG;  // mixed element types: one realisation
   // at most 256 threads per node: R > 256 needs 2 (R <= 512) or 4 realisations per thread
   if (d->R > 256 && !(d->R % 4 == 0 || (d->R <= 512 && d->R % 2 == 0))) return SC_BAD_ARG;
   sc_batch* h = new sc_batch();

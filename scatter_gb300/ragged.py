@@ -68,6 +68,22 @@ def hrz_factor(model, nu, rho, order=2):
     return float(Me.sum() / np.trace(Me))
 
 
+def lumped_mass(Me, ktype, elem_idx, free, rho, hrz=False):
+    """Lumped mass per node and component [n_nodes, 3] from per-type unit-rho element mass
+    blocks Me [types, n_en, n_en] (one component; the consistent mass is m_ab I): row sums over
+    free columns (the row sums of the assembled mass), or the diagonal scaled to the element
+    mass (hrz).  Fixed components get 1."""
+    N = len(free)
+    ml = np.zeros((N, 3))
+    if hrz:
+        f = Me.sum(axis=(1, 2)) / np.einsum("taa->t", Me)
+        contrib = np.einsum("taa,t->ta", Me, f)[ktype][:, :, None] * np.ones(3)
+    else:
+        contrib = np.einsum("eab,ebc->eac", Me[ktype], free[elem_idx].astype(float))
+    np.add.at(ml, elem_idx, contrib * rho)
+    return np.where(free, ml, 1.0)
+
+
 class RaggedExplicit:
     def __init__(self, specs, damping, dt, time_grid, load_amplitude=-10e3, f0=20.0, t0=0.05, order=2,
                  bottom="111", x_faces="100", z_faces="001", tune=True):
@@ -172,3 +188,162 @@ class RaggedExplicit:
 
     def close(self):
         self.solver.close()
+
+
+class RaggedBatch:
+    """The same meshes advanced matrix-free: one thread per node gathers its incident elements'
+    unit-E stiffness (one FP32 table per element shape and nu) scaled by the mesh's E, FP32
+    products with (hi, lo) pair accumulators for u and v (the batched path's arithmetic,
+    csrc/sc_batch.cu with one realisation and per-node element types).  No global matrix is
+    stored, so the memory is a few tens of bytes per DOF and the kernel is compute-bound."""
+
+    def __init__(self, specs, damping, dt, time_grid, load_amplitude=-10e3, f0=20.0, t0=0.05, order=2,
+                 bottom="111", x_faces="100", z_faces="001"):
+        from . import meshgen
+        from .batched import _Desc, element_types
+        from .system_matrix import GenerateMatrix
+
+        dv.require_cuda()
+        s = dv.stream_ptr()
+        alpha, beta = GenerateMatrix.rayleigh_coefficients(damping)
+        nen_max = max(ELEM_NODES[sp["element"]] for sp in specs)
+        nd_max = 3 * nen_max
+        elems, types, young, k1s, fixed, mls, nens, inc_ptrs, incs = [], [], [], [], [], [], [], [], []
+        node_off = elem_off = type_off = inc_off = 0
+        f_parts, rec_slot = [], []
+        self.parts = []
+        for sp in specs:
+            nx, ny, nz = sp["dims"]
+            m = meshgen.box_model(nx, ny, nz, sp["h"], element=sp["element"], bottom=bottom, x_faces=x_faces,
+                                  z_faces=z_faces)
+            etype = str(m.element_type)
+            n_en = ELEM_NODES[etype]
+            nodes, _, elem_idx, eqmap = model_arrays(m)
+            N, n_el = len(nodes), len(elem_idx)
+            nu = np.full(n_el, sp["nu"])
+            first, ktype = element_types(m, nu)
+            # unit-E stiffness and unit-rho mass per element shape
+            X = dv.to_dev(nodes[:, 1:][elem_idx[first]], torch.float64)
+            one = dv.to_dev(np.ones(len(first)), torch.float64)
+            nu_t = dv.to_dev(nu[first], torch.float64)
+            nd = 3 * n_en
+            ke = dv.empty(len(first) * nd * nd, torch.float64)
+            me = dv.empty(len(first) * nd * nd, torch.float64)
+            nat.call("sc_element_matrices", nat.ELEMENT_CODES[etype], order, len(first), X.data_ptr(), one.data_ptr(),
+                     nu_t.data_ptr(), one.data_ptr(), ke.data_ptr(), me.data_ptr(), s)
+            torch.cuda.current_stream().synchronize()
+            Ke = dv.host(ke).reshape(len(first), nd, nd)
+            Me = dv.host(me).reshape(len(first), n_en, 3, n_en, 3)[:, :, 0, :, 0]  # per-component block
+            kp = np.zeros((len(first), nd_max, nd_max), dtype=np.float32)
+            kp[:, :nd, :nd] = Ke
+            k1s.append(kp)
+            # lumped mass per slot: row sums over free columns, or the diagonal scaled to the
+            # element mass for the quadratic tetrahedron
+            free = (eqmap >= 0)
+            mls.append(lumped_mass(Me, ktype, elem_idx, free, sp["rho"], hrz=etype == "tetra10").ravel())
+            fixed.append((~free).astype(np.int32).ravel())
+            # connectivity, padded to the largest element type
+            ep = np.zeros((n_el, nen_max), dtype=np.int64)
+            ep[:, :n_en] = elem_idx + node_off
+            ep[:, n_en:] = ep[:, :1]
+            elems.append(ep)
+            types.append(ktype.astype(np.int64) + type_off)
+            young.append(np.full(n_el, sp["E"], dtype=np.float32))
+            nens.append(np.full(N, n_en, dtype=np.uint8))
+            # node -> element incidence of the mesh, offset into the union
+            el_d = dv.to_dev(elem_idx.astype(np.int32), torch.int32)
+            ip = dv.empty(N + 1, torch.int32)
+            inc = dv.empty(n_el * n_en, torch.int32)
+            work = dv.empty(N, torch.int32)
+            nat.call("sc_node_incidence", n_el, n_en, N, el_d.data_ptr(), ip.data_ptr(), inc.data_ptr(),
+                     work.data_ptr(), s)
+            inc_ptrs.append(dv.host(ip)[:-1].astype(np.int64) + inc_off)
+            incs.append(dv.host(inc).astype(np.int64) + elem_off)
+            # force and receiver in slot space
+            tg = np.asarray(time_grid, dtype=float)
+            c = _top_centre(m)
+            ft = ricker_table(m, c, load_amplitude, f0, t0, tg)
+            inv = np.full(int(m.number_eq), -1, dtype=np.int64)
+            nn, cc = np.nonzero(free)
+            inv[eqmap[nn, cc]] = (nn + node_off) * 3 + cc
+            f_parts.append((ft, inv))
+            rec_slot.append((int(m.node_index()[c]) + node_off) * 3 + 1)
+            self.parts.append({"element": etype, "n_eq": int(m.number_eq), "n_nodes": N})
+            node_off += N
+            elem_off += n_el
+            type_off += len(first)
+            inc_off += n_el * n_en
+        self.n_nodes, self.n_elem = node_off, elem_off
+        self.n_eq = sum(p["n_eq"] for p in self.parts)
+        n_t = len(time_grid)
+        counts = np.zeros(n_t, dtype=np.int64)
+        for ft, _ in f_parts:
+            counts += np.diff(ft.f_ptr)
+        ptr = np.r_[0, np.cumsum(counts)]
+        f_slot = np.empty(ptr[-1], dtype=np.int64)
+        f_val = np.empty(ptr[-1])
+        fill = ptr[:-1].copy()
+        for ft, inv in f_parts:
+            cnt = np.diff(ft.f_ptr)
+            step = np.repeat(np.arange(n_t), cnt)
+            pos = fill[step] + (np.arange(len(step)) - np.repeat(ft.f_ptr[:-1], cnt))
+            f_slot[pos] = inv[ft.f_eq]
+            f_val[pos] = ft.f_val
+            fill += cnt
+        self._t = {
+            "elem": dv.to_dev(np.concatenate(elems).astype(np.int32), torch.int32),
+            "ke_type": dv.to_dev(np.concatenate(types).astype(np.int32), torch.int32),
+            "ke1": dv.to_dev(np.concatenate(k1s), torch.float32),
+            "young": dv.to_dev(np.concatenate(young), torch.float32),
+            "ml": dv.to_dev(np.concatenate(mls), torch.float64),
+            "fixed": dv.to_dev(np.concatenate(fixed), torch.int32),
+            "inc_ptr": dv.to_dev(np.r_[np.concatenate(inc_ptrs), inc_off].astype(np.int32), torch.int32),
+            "inc": dv.to_dev(np.concatenate(incs).astype(np.int32), torch.int32),
+            "node_nen": dv.to_dev(np.concatenate(nens), torch.uint8),
+            "l_ptr": torch.zeros(3 * node_off + 1, dtype=torch.int64, device="cuda"),
+            "l_i": torch.zeros(1, dtype=torch.int32, device="cuda"),
+            "l_f": torch.zeros(1, dtype=torch.float32, device="cuda"),
+            "f_ptr": dv.to_dev(ptr, torch.int64), "f_slot": dv.to_dev(f_slot.astype(np.int32), torch.int32),
+            "f_val": dv.to_dev(f_val, torch.float64),
+            "rec": dv.to_dev(np.asarray(rec_slot, dtype=np.int32), torch.int32)}
+        t = self._t
+        self.u = dv.zeros(3 * node_off, torch.float64)
+        self.v = dv.zeros(3 * node_off, torch.float64)
+        d = _Desc(node_off, elem_off, nen_max, 1, int(t["ke1"].shape[0]), t["elem"].data_ptr(), t["inc_ptr"].data_ptr(),
+                  t["inc"].data_ptr(), t["ke_type"].data_ptr(), t["ke1"].data_ptr(), t["young"].data_ptr(),
+                  t["ml"].data_ptr(), t["fixed"].data_ptr(), float(alpha), float(beta), float(dt), t["l_ptr"].data_ptr(),
+                  t["l_i"].data_ptr(), t["l_i"].data_ptr(), t["l_f"].data_ptr(), t["l_f"].data_ptr(),
+                  t["node_nen"].data_ptr())
+        self._desc = d
+        h = ctypes.c_void_p()
+        nat.call("sc_batch_create", ctypes.byref(h), ctypes.byref(d), self.u.data_ptr(), self.v.data_ptr(), s)
+        self.h = h
+        nat.call("sc_batch_set_force", self.h, n_t, t["f_ptr"].data_ptr(), t["f_slot"].data_ptr(),
+                 t["f_val"].data_ptr())
+        rpt, tpb, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        nat.call("sc_batch_config", self.h, ctypes.byref(rpt), ctypes.byref(tpb), ctypes.byref(ms))
+        self.tuned = (tpb.value, ms.value)
+
+    def set_output(self, interval, n_out):
+        self.n_out = int(n_out)
+        self.out_v = dv.zeros(self.n_out * len(self.parts), torch.float64)
+        nat.call("sc_batch_set_output", self.h, int(interval), len(self.parts), self._t["rec"].data_ptr(),
+                 self.out_v.data_ptr(), self.n_out)
+
+    def run(self, t_begin, t_end):
+        nat.call("sc_batch_run", self.h, int(t_begin), int(t_end))
+
+    def velocities(self):
+        """[n_out, n_meshes]: vertical velocity at each mesh's top-centre node."""
+        return dv.host(self.out_v).reshape(self.n_out, len(self.parts))
+
+    def close(self):
+        if getattr(self, "h", None):
+            nat.value("sc_batch_destroy", self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

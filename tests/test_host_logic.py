@@ -151,3 +151,36 @@ def test_hrz_lumping_of_the_reference_tetra10_mass_is_positive():
     lumped = f * np.diag(Mx)
     assert lumped.min() > 0
     assert abs(lumped.sum() / Mx.sum() - 1) < 1e-12
+
+
+def test_matrix_free_lumped_mass_equals_assembled_row_sums():
+    """The per-element lumped-mass contributions of the matrix-free ragged path (row sums over
+    free columns, scattered to nodes) equal the row sums of the assembled consistent mass."""
+    import numpy as np
+
+    from oracle import assembly as asm
+    from oracle import elements as el
+    from oracle import explicit
+    from scatter_gb300 import meshgen
+    from scatter_gb300.system_matrix import model_arrays
+
+    m = meshgen.box_model(3, 4, 2, 0.5, element="hexa8")
+    nodes, _, elem_idx, eqmap = model_arrays(m)
+    n = len(elem_idx)
+    _, Me = el.element_matrices("hexa8", nodes[:, 1:][elem_idx], np.ones(n), np.full(n, 0.25), np.ones(n))
+    from scatter_gb300.ragged import lumped_mass
+
+    Mx = Me.reshape(n, 8, 3, 8, 3)[:, :, 0, :, 0]
+    free = eqmap >= 0
+    ml = lumped_mass(Mx, np.arange(n), elem_idx, free, 1.0)
+    ref = explicit.lumped(asm.assemble(m.eq_nb_elem, Me, m.number_eq))
+    nn, cc = np.nonzero(free)
+    assert np.abs(ml[nn, cc] - ref[eqmap[nn, cc]]).max() <= 1e-14 * ref.max()
+    # diagonal scaling keeps each element's mass
+    mt = meshgen.box_model(1, 1, 1, 0.5, element="tetra10")
+    nd_, _, ei, em = model_arrays(mt)
+    k = len(ei)
+    _, Mt = el.element_matrices("tetra10", nd_[:, 1:][ei], np.ones(k), np.full(k, 0.3), np.ones(k))
+    Mtx = Mt.reshape(k, 10, 3, 10, 3)[:, :, 0, :, 0]
+    h = lumped_mass(Mtx, np.arange(k), ei, np.ones_like(em, dtype=bool), 1.0, hrz=True)
+    assert h.min() > 0 and abs(h[:, 0].sum() / Mtx.sum() - 1) < 1e-12
