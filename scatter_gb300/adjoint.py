@@ -142,8 +142,10 @@ class _Prepared:
         return J.value, dv.host(gE), dv.host(gR)
 
     def timings(self):
-        """Device ms of the last gradient's phases: forward with checkpoints, recompute, backward."""
-        ms = (ctypes.c_float * 3)()
+        """Device ms of the last gradient's phases: forward with checkpoints, recompute and
+        backward (each summed over the segments; the two overlap on two streams), and the wall
+        time of the reverse sweep."""
+        ms = (ctypes.c_float * 4)()
         nat.call("sc_nb_adjoint_timings", self.solver.h, ms)
         return tuple(float(x) for x in ms)
 

@@ -66,10 +66,10 @@ struct PairStep {
 };
 
 // Adjoint recompute: the step n -> n+1 (n = step - 1, k = n - *t0 within the segment) stores
-// the new state at k + 1 and the element kernel's FP32 inputs of state n at k.
+// the element gradient's inputs of state n at k (the receiver velocities the backward needs
+// are the forward's records, bitwise the same as the recomputed ones).
 struct SegStore {
-  float2 *u, *v;     // [k n_s + i]
-  float2* wp;        // w = u + beta v of state n
+  float2* wp;        // w = u + beta v of state n, [k n_s + i]
   float *v32, *a32;  // v of state n and a of the step n -> n+1 (hi parts)
   const int* t0;
 };
@@ -83,8 +83,7 @@ template <int D, int TPR>
 __global__ void __launch_bounds__(kThreads) k_explicit_pair(Args g, PairStep p, const int* __restrict__ rec_map,
                                                             SegStore st) {
   const int step = g.s->t + 1;
-  const int64_t kn = st.u ? (int64_t)(step - 1 - *st.t0) * g.n_s : 0;
-  const int64_t k1 = kn + g.n_s;
+  const int64_t kn = st.wp ? (int64_t)(step - 1 - *st.t0) * g.n_s : 0;
   const bool rec_now = g.n_rec > 0 && g.out_interval > 0 && (step % g.out_interval) == 0 &&
                        step / g.out_interval < g.n_out;
   const int64_t orow = rec_now ? step / g.out_interval : 0;
@@ -122,8 +121,8 @@ __global__ void __launch_bounds__(kThreads) k_explicit_pair(Args g, PairStep p, 
       const int64_t i = row * D + c;
       if (g.fixed[i]) {
         p.v_out[i] = p.w_out[i] = make_float2(0.f, 0.f);
-        if (st.u) {
-          st.u[k1 + i] = st.v[k1 + i] = st.wp[kn + i] = make_float2(0.f, 0.f);
+        if (st.wp) {
+          st.wp[kn + i] = make_float2(0.f, 0.f);
           st.v32[kn + i] = st.a32[kn + i] = 0.f;
         }
         continue;
@@ -139,9 +138,7 @@ __global__ void __launch_bounds__(kThreads) k_explicit_pair(Args g, PairStep p, 
       p.v_out[i] = vn;
       p.u[i] = un;
       p.w_out[i] = w_of(un, vn, p.beta);
-      if (st.u) {
-        st.u[k1 + i] = un;
-        st.v[k1 + i] = vn;
+      if (st.wp) {
         st.wp[kn + i] = p.w_in[i];
         st.v32[kn + i] = vi.x;
         st.a32[kn + i] = acc.x;
@@ -442,10 +439,11 @@ int explicit_prepare(sc_nb_newmark* h) {
   return check_launch("explicit prepare");
 }
 
-// force entries of step t in f (FP64 mode) or f2 (pair mode)
-void force_reset(sc_nb_newmark* h, int t) {
+// force entries of step t in f (FP64 mode) or f2 (pair mode), on stream st (default: the
+// handle's stream)
+void force_reset(sc_nb_newmark* h, int t, cudaStream_t st = nullptr) {
   Args& g = h->g;
-  cudaStream_t st = h->user;
+  if (!st) st = h->user;
   if (h->explicit_pair) {
     cudaMemsetAsync(h->f2, 0, 8 * g.n_s, st);
     k_force_at<<<1, 256, 0, st>>>(g, t, h->f2);
@@ -635,28 +633,32 @@ struct sc_adj_desc {
 namespace {
 
 struct AdjState {
-  float2 *seg_u, *seg_v;  // states of the segment, [(C + 1) n_s]
-  float2* wp;             // element kernel inputs per state of the segment, [C n_s]
-  float *v32, *a32;
+  // segment buffer (one of two): the element gradient's inputs for each step of the segment
+  float2* wp;        // w = u + beta v of state n, [C n_s]
+  float *v32, *a32;  // v of state n and a of the step n -> n+1 (hi parts), [C n_s]
+  float* ys;         // y of backward step n (hi + lo rounded to FP32), [C n_s]
+  int* seg_t0;       // first step of the segment the buffer holds
+  // shared by both buffers
   float2 *mu_u, *mu_v;
-  float2* y[2];  // (mu_v + dt mu_u) / M_L of the step being reversed ([cur]) and of the next
-  double* out_v;
-  double *gE, *gR;       // gradient outputs [n_elem]
-  float *iE, *iR;        // 1 / E_e, 1 / rho_e
-  int *n_dev, *n_dev_e;  // step being reversed, one counter per backward kernel
-  unsigned* ticket_e;
-  int *seg_t0, *rec_map;
+  float2* y[2];        // (mu_v + dt mu_u) / M_L of the step being reversed ([cur]) and of the next
+  double* out_v;       // the forward's receiver velocities, [(N + 1) n_rec]
+  double *gE, *gR;     // gradient outputs [n_elem]
+  float *iE, *iR;      // 1 / E_e, 1 / rho_e
+  int* n_dev;          // step being reversed
+  unsigned* ticket_r;  // blocks of the row kernel finished in its current launch
+  int* rec_map;
   double* J;
 };
 
 // Backward step n (state n -> n+1 reversed), node rows, all in FP32 pairs: with y = y[cur],
 //   mu_u <- mu_u - dt K y,  mu_v <- g - dt (beta K y + Cab y + alpha M_L y) + P^T (P v_n - d_n),
-//   y[cur ^ 1] = (mu_v + dt mu_u) / M_L   (the y of step n - 1),  g = mu_v + dt mu_u.
-// The last block to finish decrements the row kernel's step counter.
+//   y[cur ^ 1] = (mu_v + dt mu_u) / M_L   (the y of step n - 1),  g = mu_v + dt mu_u;
+// y of step n also goes to the segment buffer (one FP32 value) for the element gradients.
+// The last block to finish decrements the step counter.
 template <int D, int TPR>
 __global__ void __launch_bounds__(kThreads) k_adj_rows(Args g, PairStep p, sc_adj_desc d, AdjState a, int cur) {
   const int n = *a.n_dev;
-  const int64_t k = n - *a.seg_t0;
+  float* ys = a.ys + (int64_t)(n - *a.seg_t0) * g.n_s;
   const float2* y = cur ? a.y[1] : a.y[0];  // (a select: no local copy of the parameter)
   float2* yn = cur ? a.y[0] : a.y[1];
   const int sub = threadIdx.x % TPR;
@@ -690,6 +692,8 @@ __global__ void __launch_bounds__(kThreads) k_adj_rows(Args g, PairStep p, sc_ad
     for (int c = (TPR >= D ? sub : 0); c < D; c += (TPR >= D ? D : 1)) {
       if (TPR > 1 && TPR < D && c % TPR != sub) continue;
       const int64_t i = row * D + c;
+      const float2 yi = y[i];
+      ys[i] = __fadd_rn(yi.x, yi.y);
       if (g.fixed[i]) {
         a.mu_u[i] = a.mu_v[i] = yn[i] = make_float2(0.f, 0.f);
         continue;
@@ -700,17 +704,18 @@ __global__ void __launch_bounds__(kThreads) k_adj_rows(Args g, PairStep p, sc_ad
       const float2 mu_u = a.mu_u[i], mu_v = a.mu_v[i];
       const float2 gg = p_add(mu_v, p_mul(p.dt, mu_u));
       const float2 mu = p_sub(mu_u, p_mul(p.dt, ky));
-      float2 mv = p_sub(gg, p_mul(p.dt, p_add(p_add(p_mul(p.beta, ky), cy), p_mul(p.aml[i], y[i]))));
+      float2 mv = p_sub(gg, p_mul(p.dt, p_add(p_add(p_mul(p.beta, ky), cy), p_mul(p.aml[i], yi))));
       const int rj = a.rec_map[i];
-      if (rj >= 0 && n >= 1) mv = p_add(mv, p_of(p_to_d(a.seg_v[k * g.n_s + i]) - d.target[(int64_t)n * d.n_rec + rj]));
+      if (rj >= 0 && n >= 1)
+        mv = p_add(mv, p_of(a.out_v[(int64_t)n * d.n_rec + rj] - d.target[(int64_t)n * d.n_rec + rj]));
       a.mu_u[i] = mu;
       a.mu_v[i] = mv;
       yn[i] = p_mul(p_add(mv, p_mul(p.dt, mu)), p.iml[i]);
     }
   }
-  if (last_block(&g.s->ticket)) {
+  if (last_block(a.ticket_r)) {
     if (threadIdx.x == 0) {
-      g.s->ticket = 0;
+      *a.ticket_r = 0;
       *a.n_dev = n - 1;
     }
   }
@@ -718,91 +723,117 @@ __global__ void __launch_bounds__(kThreads) k_adj_rows(Args g, PairStep p, sc_ad
 
 constexpr int kAdjElemThreads = 128;
 
-// Backward step n, element gradients: one lane per element node (32 / n_en elements per
-// warp), lane (e, la) owning the element DOFs 3 la .. 3 la + 2, all FP32:
+// Element gradients of one segment, steps t1 - 1 down to t0, once its backward steps are
+// done: one lane per element node (32 / NEN elements per warp), lane (e, la) owning the
+// element DOFs 3 la .. 3 la + 2 and holding its three rows of K1_e in registers for the whole
+// segment (NEN <= 10; read per step for hexa20).  Per step, all FP32:
 //   dJ/dE_e   -= dt y_e . [K1_e (u + beta v)_e + Lysmer terms]
 //   dJ/drho_e -= dt sum ml1_e y_e (a + alpha v)_e + Lysmer term,
 // (u + beta v) taken relative to the element's first node on the (hi, lo) pairs (K1
-// annihilates rigid translations, so the FP32 products see strains); per-element sums made
-// by the element's first lane in lane order (deterministic) and accumulated in FP64; the
-// Lysmer terms of boundary elements are dealt to the element's lanes too (one lane working
-// alone would hold its warp).  The last block to finish decrements the element kernel's step
-// counter.
-__global__ void __launch_bounds__(kAdjElemThreads) k_adj_elems(Args g, sc_adj_desc d, AdjState a, int cur) {
-  __shared__ float sw[kAdjElemThreads / 32][96];
+// annihilates rigid translations, so the FP32 products see strains); the Lysmer terms of
+// boundary elements dealt to the element's lanes; per-element sums made by the element's
+// first lane in lane order and accumulated in FP64 in step order, so the result does not
+// depend on the checkpoint interval.
+template <int NEN>
+__global__ void __launch_bounds__(kAdjElemThreads) k_adj_grad_seg(Args g, sc_adj_desc d, AdjState a, int t0, int t1) {
+  constexpr int ND = 3 * NEN, EPW = 32 / NEN;
+  constexpr bool KREG = NEN <= 10;
+  __shared__ __align__(16) float sw[kAdjElemThreads / 32][96];
   __shared__ float part[kAdjElemThreads / 32][32][2];
-  const int n = *a.n_dev_e;
-  const int64_t k = n - *a.seg_t0;
-  const float2* y = cur ? a.y[1] : a.y[0];
-  const float2* wp = a.wp + k * g.n_s;
-  const float* v32 = a.v32 + k * g.n_s;
-  const float* a32 = a.a32 + k * g.n_s;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int ne = d.n_en, nd = 3 * ne, epw = 32 / ne;
-  const int grp = lane / ne, la = lane % ne, base = grp * ne;
+  const int grp = lane / NEN, la = lane % NEN, base = grp * NEN;
   const float alpha = (float)g.alpha_r;
   const int64_t warps = (int64_t)gridDim.x * (kAdjElemThreads / 32);
-  for (int64_t wg = (int64_t)blockIdx.x * (kAdjElemThreads / 32) + wib; wg * epw < d.n_elem; wg += warps) {
-    const int64_t e = wg * epw + grp;
-    const bool on = grp < epw && e < d.n_elem;
-    float ya[3] = {0.f, 0.f, 0.f}, gr = 0.f;
+  for (int64_t wg = (int64_t)blockIdx.x * (kAdjElemThreads / 32) + wib; wg * EPW < d.n_elem; wg += warps) {
+    const int64_t e = wg * EPW + grp;
+    const bool on = grp < EPW && e < d.n_elem;
+    int64_t sa = 0, s0 = 0, q0 = 0, q1 = 0;
+    const float* K1 = d.ke1;
+    float kr[KREG ? 3 * ND : 1];
+    float ml[3] = {0.f, 0.f, 0.f};
+    float iE = 0.f, iR = 0.f;
+    double accE = 0.0, accR = 0.0;
     if (on) {
-      const int* en = d.elem + e * ne;
-      const int64_t sa = (int64_t)en[la] * 3, s0 = (int64_t)en[0] * 3;
+      const int* en = d.elem + e * NEN;
+      sa = (int64_t)en[la] * 3;
+      s0 = (int64_t)en[0] * 3;
+      K1 = d.ke1 + (int64_t)d.ke_type[e] * ND * ND + (int64_t)(3 * la) * ND;
+      if constexpr (KREG) {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const float2 wb = wp[sa + c], w0 = wp[s0 + c];
-        sw[wib][base * 3 + 3 * la + c] = (wb.x - w0.x) + (wb.y - w0.y);
-        const float2 yv = y[sa + c];
-        ya[c] = yv.x + yv.y;
-        gr = fmaf(d.ml1[e * nd + 3 * la + c] * ya[c], fmaf(alpha, v32[sa + c], a32[sa + c]), gr);
+        for (int j = 0; j < 3 * ND; ++j) kr[j] = __ldg(K1 + j);
       }
-    }
-    __syncwarp();
-    float ge = 0.f;
-    if (on) {
-      const float* K1 = d.ke1 + (int64_t)d.ke_type[e] * nd * nd + (int64_t)(3 * la) * nd;
-      const float* wv = &sw[wib][base * 3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float r = 0.f;
-        for (int b = 0; b < nd; ++b) r = fmaf(__ldg(K1 + c * nd + b), wv[b], r);
-        ge = fmaf(ya[c], r, ge);
-      }
-    }
-    if (on) {
-      // Lysmer terms of boundary elements (dashpots ~ sqrt(rho E), springs ~ E), the element's
-      // entries dealt to its lanes
-      const int64_t q0 = d.l_eptr[e], q1 = d.l_eptr[e + 1];
+      for (int c = 0; c < 3; ++c) ml[c] = d.ml1[e * ND + 3 * la + c];
+      q0 = d.l_eptr[e];
+      q1 = d.l_eptr[e + 1];
       if (q1 > q0) {
-        const float iE = a.iE[e], iR = a.iR[e];
-        for (int64_t q = q0 + la; q < q1; q += ne) {
-          const float2 yv = y[d.l_row[q]], wv = wp[d.l_col[q]];
-          const float yr = yv.x + yv.y, wc = wv.x + wv.y, vc = v32[d.l_col[q]];
+        iE = a.iE[e];
+        iR = a.iR[e];
+      }
+      if (la == 0) {
+        accE = a.gE[e];
+        accR = a.gR[e];
+      }
+    }
+    for (int n = t1 - 1; n >= t0; --n) {
+      const int64_t off = (int64_t)(n - t0) * g.n_s;
+      const float2* wp = a.wp + off;
+      const float* v32 = a.v32 + off;
+      const float* a32 = a.a32 + off;
+      const float* ys = a.ys + off;
+      float ya[3] = {0.f, 0.f, 0.f}, gr = 0.f;
+      if (on) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float2 wb = wp[sa + c], w0 = wp[s0 + c];
+          sw[wib][base * 3 + 3 * la + c] = (wb.x - w0.x) + (wb.y - w0.y);
+          ya[c] = ys[sa + c];
+          gr = fmaf(ml[c] * ya[c], fmaf(alpha, v32[sa + c], a32[sa + c]), gr);
+        }
+      }
+      __syncwarp();
+      float ge = 0.f;
+      if (on) {
+        const float* wv = &sw[wib][base * 3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          float r = 0.f;
+#pragma unroll
+          for (int b = 0; b < ND; ++b) {
+            float kv;
+            if constexpr (KREG) kv = kr[c * ND + b];
+            else kv = __ldg(K1 + c * ND + b);
+            r = fmaf(kv, wv[b], r);
+          }
+          ge = fmaf(ya[c], r, ge);
+        }
+        // Lysmer terms of boundary elements (dashpots ~ sqrt(rho E), springs ~ E)
+        for (int64_t q = q0 + la; q < q1; q += NEN) {
+          const float yr = ys[d.l_row[q]];
+          const float2 wq = wp[d.l_col[q]];
+          const float wc = wq.x + wq.y, vc = v32[d.l_col[q]];
           const float hc = __fmul_rn(0.5f, d.l_c[q]);
           ge = fmaf(yr, fmaf(__fmul_rn(d.l_s[q], iE), wc, __fmul_rn(__fmul_rn(hc, iE), vc)), ge);
           gr = fmaf(yr, __fmul_rn(__fmul_rn(hc, iR), vc), gr);
         }
       }
-    }
-    part[wib][lane][0] = ge;
-    part[wib][lane][1] = gr;
-    __syncwarp();
-    if (on && la == 0) {
-      float ge_e = 0.f, gr_e = 0.f;
-      for (int q = 0; q < ne; ++q) {
-        ge_e += part[wib][base + q][0];
-        gr_e += part[wib][base + q][1];
+      part[wib][lane][0] = ge;
+      part[wib][lane][1] = gr;
+      __syncwarp();
+      if (on && la == 0) {
+        float ge_e = 0.f, gr_e = 0.f;
+        for (int q = 0; q < NEN; ++q) {
+          ge_e += part[wib][base + q][0];
+          gr_e += part[wib][base + q][1];
+        }
+        accE -= g.dt * (double)ge_e;
+        accR -= g.dt * (double)gr_e;
       }
-      a.gE[e] -= g.dt * (double)ge_e;
-      a.gR[e] -= g.dt * (double)gr_e;
+      __syncwarp();
     }
-    __syncwarp();
-  }
-  if (last_block(a.ticket_e)) {
-    if (threadIdx.x == 0) {
-      *a.ticket_e = 0;
-      *a.n_dev_e = n - 1;
+    if (on && la == 0) {
+      a.gE[e] = accE;
+      a.gR[e] = accR;
     }
   }
 }
@@ -857,67 +888,100 @@ void launch_adj_rows(const sc_nb_newmark* h, cudaStream_t st, const sc_adj_desc&
   }
 }
 
+template <int NEN>
+void launch_grad_seg_t(const sc_nb_newmark* h, cudaStream_t st, const sc_adj_desc& d, const AdjState& a, int t0,
+                       int t1) {
+  const int64_t warps = (d.n_elem + 32 / NEN - 1) / (32 / NEN);
+  k_adj_grad_seg<NEN><<<grid_for(warps, kAdjElemThreads / 32, 152 * 32), kAdjElemThreads, 0, st>>>(h->g, d, a, t0, t1);
+}
+void launch_grad_seg(const sc_nb_newmark* h, cudaStream_t st, const sc_adj_desc& d, const AdjState& a, int t0, int t1) {
+  switch (d.n_en) {
+    case 4: launch_grad_seg_t<4>(h, st, d, a, t0, t1); break;
+    case 8: launch_grad_seg_t<8>(h, st, d, a, t0, t1); break;
+    case 10: launch_grad_seg_t<10>(h, st, d, a, t0, t1); break;
+    default: launch_grad_seg_t<20>(h, st, d, a, t0, t1); break;
+  }
+}
+
 }  // namespace
 
-// Forward from rest with pair checkpoints every `checkpoint` steps, then per segment (last
-// first): restore its checkpoint, recompute its states (the explicit step storing them) and
-// reverse its steps (element and row kernels side by side).  The forward and the recompute
-// run the same kernels from the same pair state, so the recomputed states are bitwise the
-// forward's.  Requires the pair arithmetic (the default).
+// Forward from rest with pair checkpoints every `checkpoint` steps, then the reverse sweep
+// over the segments, last first.  Two streams: the handle's stream runs the forward and the
+// backward; a second stream recomputes segment s - 1 from its checkpoint (the explicit step
+// storing the element gradient's inputs into one of two segment buffers) while the backward
+// reverses segment s from the other buffer (one row kernel per step, then one element
+// gradient kernel for the whole segment).  The forward and the recompute run the same kernels
+// from the same pair state, so the recomputed states are bitwise the forward's.  Requires the
+// pair arithmetic (the default).
 extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_host, double* grad_E,
                              double* grad_rho) {
   if (!h || !dp || !grad_E || !grad_rho) return SC_BAD_ARG;
   const sc_adj_desc d = *dp;
   if (d.n_steps <= 0 || d.checkpoint <= 0 || d.n_rec <= 0 || !d.rec_slot || !d.target || d.n_elem <= 0 ||
-      d.n_en <= 0 || d.n_en > 32 || !d.elem || !d.ke_type || !d.ke1 || !d.young || !d.rho || !d.ml1 ||
-      !d.l_eptr || h->g.D != 3 || !h->explicit_pair)
+      !(d.n_en == 4 || d.n_en == 8 || d.n_en == 10 || d.n_en == 20) || !d.elem || !d.ke_type || !d.ke1 ||
+      !d.young || !d.rho || !d.ml1 || !d.l_eptr || h->g.D != 3 || !h->explicit_pair)
     return SC_BAD_ARG;
   Args& g = h->g;
-  cudaStream_t st = h->user;
+  cudaStream_t st = h->user;  // forward and backward
+  cudaStream_t rs = nullptr;  // recompute
   const int N = d.n_steps, C = d.checkpoint < d.n_steps ? d.checkpoint : d.n_steps, nseg = (N + C - 1) / C;
+  const int nbuf = nseg > 1 ? 2 : 1;
+  auto buf = [&](int sgi) { return nbuf == 2 ? (sgi & 1) : 0; };
   const int64_t ns = g.n_s;
   // the caller's output configuration, restored at the end
   const int o_int = g.out_interval, o_nrec = g.n_rec;
   const int* o_rec = g.rec_slot;
   double *o_u = g.out_u, *o_v = g.out_v, *o_a = g.out_a;
   const int64_t o_nout = g.n_out;
-  AdjState a{};
+  AdjState a[2] = {};
+  AdjState& s = a[0];  // the fields both buffers share are set here and copied
   float2 *ck_u = nullptr, *ck_v = nullptr;
-  int* t_host = nullptr;  // segment starts and backward starts, pinned (copied by the stream)
+  int* t_host = nullptr;  // [0, nseg) segment starts, [nseg, 2 nseg) backward starts; pinned
+  int* t0_dev = nullptr;  // the segment start of each buffer
   int rc = SC_OK;
   auto M = [&](void** p, size_t b) { return check(cudaMallocAsync(p, b, st), "adjoint malloc"); };
-  cudaGraphExec_t rec_exec[2] = {nullptr, nullptr}, bwd_exec[2] = {nullptr, nullptr};
-  cudaGraph_t rec_graph[2] = {nullptr, nullptr}, bwd_graph[2] = {nullptr, nullptr};
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  // phase timers: [0, 1] forward, then per segment [2 + 4 s ... 5 + 4 s] recompute and backward
+  cudaGraphExec_t rec_exec[2][2] = {}, bwd_exec[2][2] = {};
+  cudaGraph_t rec_graph[2][2] = {}, bwd_graph[2][2] = {};
+  cudaEvent_t ev_fwd = nullptr, ev_rs_end = nullptr, rec_done[2] = {}, bwd_done[2] = {};
+  // phase timers: [0, 1] forward; per segment [2 + 4 s, 3 + 4 s] recompute (second stream) and
+  // [4 + 4 s, 5 + 4 s] backward
   std::vector<cudaEvent_t> tev;
   do {
     if ((rc = M((void**)&ck_u, 8 * ns * nseg)) || (rc = M((void**)&ck_v, 8 * ns * nseg)) ||
-        (rc = M((void**)&a.seg_u, 8 * ns * (C + 1))) || (rc = M((void**)&a.seg_v, 8 * ns * (C + 1))) ||
-        (rc = M((void**)&a.wp, 8 * ns * C)) || (rc = M((void**)&a.v32, 4 * ns * C)) ||
-        (rc = M((void**)&a.a32, 4 * ns * C)) || (rc = M((void**)&a.mu_u, 8 * ns)) || (rc = M((void**)&a.mu_v, 8 * ns)) ||
-        (rc = M((void**)&a.y[0], 8 * ns)) || (rc = M((void**)&a.y[1], 8 * ns)) ||
-        (rc = M((void**)&a.out_v, 8 * (int64_t)(N + 1) * d.n_rec)) || (rc = M((void**)&a.n_dev, 4)) ||
-        (rc = M((void**)&a.n_dev_e, 4)) || (rc = M((void**)&a.ticket_e, 4)) || (rc = M((void**)&a.seg_t0, 4)) ||
-        (rc = M((void**)&a.rec_map, 4 * ns)) || (rc = M((void**)&a.J, 8)) ||
-        (rc = M((void**)&a.iE, 4 * (size_t)d.n_elem)) || (rc = M((void**)&a.iR, 4 * (size_t)d.n_elem)))
+        (rc = M((void**)&s.mu_u, 8 * ns)) || (rc = M((void**)&s.mu_v, 8 * ns)) || (rc = M((void**)&s.y[0], 8 * ns)) ||
+        (rc = M((void**)&s.y[1], 8 * ns)) || (rc = M((void**)&s.out_v, 8 * (int64_t)(N + 1) * d.n_rec)) ||
+        (rc = M((void**)&s.n_dev, 4)) || (rc = M((void**)&s.ticket_r, 4)) || (rc = M((void**)&t0_dev, 8)) ||
+        (rc = M((void**)&s.rec_map, 4 * ns)) || (rc = M((void**)&s.J, 8)) ||
+        (rc = M((void**)&s.iE, 4 * (size_t)d.n_elem)) || (rc = M((void**)&s.iR, 4 * (size_t)d.n_elem)))
       break;
+    s.gE = grad_E;
+    s.gR = grad_rho;
+    a[1] = s;
+    for (int b = 0; b < nbuf && !rc; ++b) {
+      a[b].seg_t0 = t0_dev + b;
+      if ((rc = M((void**)&a[b].wp, 8 * ns * C)) || (rc = M((void**)&a[b].v32, 4 * ns * C)) ||
+          (rc = M((void**)&a[b].a32, 4 * ns * C)) || (rc = M((void**)&a[b].ys, 4 * ns * C)))
+        break;
+    }
+    if (rc) break;
     if ((rc = check(cudaMallocHost((void**)&t_host, 8 * (size_t)nseg), "adjoint pinned"))) break;
+    if ((rc = check(cudaStreamCreateWithFlags(&rs, cudaStreamNonBlocking), "adjoint stream"))) break;
+    for (cudaEvent_t* ev : {&ev_fwd, &ev_rs_end, &rec_done[0], &rec_done[1], &bwd_done[0], &bwd_done[1]})
+      if ((rc = check(cudaEventCreateWithFlags(ev, cudaEventDisableTiming), "adjoint event"))) break;
+    if (rc) break;
     tev.assign(2 + 4 * (size_t)nseg, nullptr);
     for (auto& ev : tev)
       if ((rc = check(cudaEventCreate(&ev), "adjoint timer"))) break;
     if (rc) break;
-    a.gE = grad_E;
-    a.gR = grad_rho;
-    cudaMemsetAsync(a.ticket_e, 0, 4, st);
-    k_adj_recip<<<grid_for(d.n_elem, 256), 256, 0, st>>>(d.n_elem, d.young, d.rho, a.iE, a.iR);
+    cudaMemsetAsync(s.ticket_r, 0, 4, st);
+    k_adj_recip<<<grid_for(d.n_elem, 256), 256, 0, st>>>(d.n_elem, d.young, d.rho, s.iE, s.iR);
     cudaMemsetAsync(grad_E, 0, 8 * (size_t)d.n_elem, st);
     cudaMemsetAsync(grad_rho, 0, 8 * (size_t)d.n_elem, st);
-    cudaMemsetAsync(a.out_v, 0, 8 * (size_t)(N + 1) * d.n_rec, st);
-    k_adj_recmap<<<grid_for(ns, 256), 256, 0, st>>>((int)ns, d.n_rec, d.rec_slot, a.rec_map);
-    k_adj_recmap_fill<<<grid_for(d.n_rec, 128), 128, 0, st>>>(d.n_rec, d.rec_slot, a.rec_map);
-    // receivers recorded into a.out_v; the explicit graphs are rebuilt for that output
-    if ((rc = sc_nb_set_output(h, 1, d.n_rec, d.rec_slot, nullptr, a.out_v, nullptr, N + 1))) break;
+    cudaMemsetAsync(s.out_v, 0, 8 * (size_t)(N + 1) * d.n_rec, st);
+    k_adj_recmap<<<grid_for(ns, 256), 256, 0, st>>>((int)ns, d.n_rec, d.rec_slot, s.rec_map);
+    k_adj_recmap_fill<<<grid_for(d.n_rec, 128), 128, 0, st>>>(d.n_rec, d.rec_slot, s.rec_map);
+    // receivers recorded into out_v; the explicit graphs are rebuilt for that output
+    if ((rc = sc_nb_set_output(h, 1, d.n_rec, d.rec_slot, nullptr, s.out_v, nullptr, N + 1))) break;
     if ((rc = explicit_prepare(h))) break;
     // forward from rest with checkpoints
     cudaMemsetAsync(h->u2, 0, 8 * ns, st);
@@ -932,60 +996,71 @@ extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_
     }
     if (rc) break;
     cudaEventRecord(tev[1], st);
-    k_adj_misfit<<<1, 1024, 0, st>>>(a.out_v, d.target, d.n_rec, N, a.J);
-    // recompute graphs: the explicit step storing its states
-    const SegStore store{a.seg_u, a.seg_v, a.wp, a.v32, a.a32, a.seg_t0};
-    for (int kk = 0; kk < 2 && !rc; ++kk) {
-      if ((rc = check(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal), "capture rec"))) break;
-      launch_pair<3>(h, h->cap, kk, store);
-      if ((rc = check(cudaStreamEndCapture(h->cap, &rec_graph[kk]), "end rec"))) break;
-      rc = check(cudaGraphInstantiate(&rec_exec[kk], rec_graph[kk], 0), "inst rec");
-    }
-    // backward graphs: the element kernel (forked onto the second capture stream) and the row
-    // kernel run side by side; they read y[cur] and the segment's states and write disjoint data
-    const int64_t elem_warps = (d.n_elem + 32 / d.n_en - 1) / (32 / d.n_en);
-    const unsigned elem_blocks = grid_for(elem_warps, kAdjElemThreads / 32, 152 * 32);
-    if (!rc) rc = check(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "event");
-    if (!rc) rc = check(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "event");
-    for (int kk = 0; kk < 2 && !rc; ++kk) {
-      if ((rc = check(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal), "capture bwd"))) break;
-      cudaEventRecord(ev_fork, h->cap);
-      cudaStreamWaitEvent(h->cap2, ev_fork, 0);
-      k_adj_elems<<<elem_blocks, kAdjElemThreads, 0, h->cap2>>>(g, d, a, kk);
-      launch_adj_rows(h, h->cap, d, a, kk);
-      cudaEventRecord(ev_join, h->cap2);
-      cudaStreamWaitEvent(h->cap, ev_join, 0);
-      if ((rc = check(cudaStreamEndCapture(h->cap, &bwd_graph[kk]), "end bwd"))) break;
-      rc = check(cudaGraphInstantiate(&bwd_exec[kk], bwd_graph[kk], 0), "inst bwd");
-    }
+    k_adj_misfit<<<1, 1024, 0, st>>>(s.out_v, d.target, d.n_rec, N, s.J);
+    // recompute graphs (per buffer and ping-pong parity): the explicit step storing the
+    // element gradient's inputs, recording no receivers (the forward's records stand)
+    g.n_rec = 0;
+    for (int b = 0; b < nbuf && !rc; ++b)
+      for (int kk = 0; kk < 2 && !rc; ++kk) {
+        if ((rc = check(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal), "capture rec"))) break;
+        launch_pair<3>(h, h->cap, kk, SegStore{a[b].wp, a[b].v32, a[b].a32, a[b].seg_t0});
+        if ((rc = check(cudaStreamEndCapture(h->cap, &rec_graph[b][kk]), "end rec"))) break;
+        rc = check(cudaGraphInstantiate(&rec_exec[b][kk], rec_graph[b][kk], 0), "inst rec");
+      }
+    g.n_rec = d.n_rec;
+    // backward graphs: the row kernel per buffer and parity
+    for (int b = 0; b < nbuf && !rc; ++b)
+      for (int kk = 0; kk < 2 && !rc; ++kk) {
+        if ((rc = check(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal), "capture bwd"))) break;
+        launch_adj_rows(h, h->cap, d, a[b], kk);
+        if ((rc = check(cudaStreamEndCapture(h->cap, &bwd_graph[b][kk]), "end bwd"))) break;
+        rc = check(cudaGraphInstantiate(&bwd_exec[b][kk], bwd_graph[b][kk], 0), "inst bwd");
+      }
     if (rc) break;
-    k_adj_init<<<h->vec_blocks, 256, 0, st>>>(g, pair_step(h, 0), a, d.target, d.n_rec, N);
+    k_adj_init<<<h->vec_blocks, 256, 0, st>>>(g, pair_step(h, 0), s, d.target, d.n_rec, N);
+    cudaEventRecord(ev_fwd, st);
+    cudaStreamWaitEvent(rs, ev_fwd, 0);
+    // recompute of segment sgi on the second stream into its buffer
+    auto recompute = [&](int sgi) {
+      const int b = buf(sgi);
+      const int t0 = sgi * C, t1 = t0 + C < N ? t0 + C : N;
+      t_host[sgi] = t0;
+      cudaMemcpyAsync(h->u2, ck_u + sgi * ns, 8 * ns, cudaMemcpyDeviceToDevice, rs);
+      cudaMemcpyAsync(h->v2[0], ck_v + sgi * ns, 8 * ns, cudaMemcpyDeviceToDevice, rs);
+      cudaMemcpyAsync(a[b].seg_t0, t_host + sgi, 4, cudaMemcpyHostToDevice, rs);
+      k_w_pairs<<<h->vec_blocks, 256, 0, rs>>>(ns, h->u2, h->v2[0], host_pair(g.beta_r), h->w2[0]);
+      force_reset(h, t0, rs);
+      k_set_t<<<1, 1, 0, rs>>>(g.s, t0);
+      cudaEventRecord(tev[2 + 4 * sgi], rs);
+      int r = check_launch("recompute set-up"), kk = 0;
+      for (int t = t0; t < t1 && !r; ++t, kk ^= 1) r = check(cudaGraphLaunch(rec_exec[b][kk], rs), "rec launch");
+      cudaEventRecord(tev[3 + 4 * sgi], rs);
+      cudaEventRecord(rec_done[b], rs);
+      return r;
+    };
+    rc = recompute(nseg - 1);
     int yk = 0;  // y[yk] holds the y of the next step to reverse
     for (int sgi = nseg - 1; sgi >= 0 && !rc; --sgi) {
+      const int b = buf(sgi);
       const int t0 = sgi * C, t1 = t0 + C < N ? t0 + C : N;
-      t_host[2 * sgi] = t0;
-      t_host[2 * sgi + 1] = t1 - 1;
-      cudaMemcpyAsync(h->u2, ck_u + sgi * ns, 8 * ns, cudaMemcpyDeviceToDevice, st);
-      cudaMemcpyAsync(h->v2[0], ck_v + sgi * ns, 8 * ns, cudaMemcpyDeviceToDevice, st);
-      cudaMemcpyAsync(a.seg_u, h->u2, 8 * ns, cudaMemcpyDeviceToDevice, st);
-      cudaMemcpyAsync(a.seg_v, h->v2[0], 8 * ns, cudaMemcpyDeviceToDevice, st);
-      cudaMemcpyAsync(a.seg_t0, t_host + 2 * sgi, 4, cudaMemcpyHostToDevice, st);
-      // recompute states t0+1 .. t1 from the checkpoint (f = the entries of step t0)
-      k_w_pairs<<<h->vec_blocks, 256, 0, st>>>(ns, h->u2, h->v2[0], host_pair(g.beta_r), h->w2[0]);
-      force_reset(h, t0);
-      k_set_t<<<1, 1, 0, st>>>(g.s, t0);
-      int kk = 0;
-      cudaEventRecord(tev[2 + 4 * sgi], st);
-      for (int t = t0; t < t1 && !rc; ++t, kk ^= 1) rc = check(cudaGraphLaunch(rec_exec[kk], st), "rec launch");
-      cudaEventRecord(tev[3 + 4 * sgi], st);
-      // backward t1-1 .. t0
-      cudaMemcpyAsync(a.n_dev, t_host + 2 * sgi + 1, 4, cudaMemcpyHostToDevice, st);
-      cudaMemcpyAsync(a.n_dev_e, t_host + 2 * sgi + 1, 4, cudaMemcpyHostToDevice, st);
+      if (sgi >= 1) {
+        // segment sgi - 1 goes to the buffer the backward of segment sgi + 1 read
+        if (sgi + 1 < nseg) cudaStreamWaitEvent(rs, bwd_done[buf(sgi - 1)], 0);
+        if ((rc = recompute(sgi - 1))) break;
+      }
+      cudaStreamWaitEvent(st, rec_done[b], 0);
+      t_host[nseg + sgi] = t1 - 1;
+      cudaMemcpyAsync(s.n_dev, t_host + nseg + sgi, 4, cudaMemcpyHostToDevice, st);
       cudaEventRecord(tev[4 + 4 * sgi], st);
-      for (int t = t1 - 1; t >= t0 && !rc; --t, yk ^= 1) rc = check(cudaGraphLaunch(bwd_exec[yk], st), "bwd launch");
+      for (int t = t1 - 1; t >= t0 && !rc; --t, yk ^= 1) rc = check(cudaGraphLaunch(bwd_exec[b][yk], st), "bwd launch");
+      launch_grad_seg(h, st, d, a[b], t0, t1);
       cudaEventRecord(tev[5 + 4 * sgi], st);
+      cudaEventRecord(bwd_done[b], st);
     }
-    if (!rc && J_host) rc = check(cudaMemcpyAsync(J_host, a.J, 8, cudaMemcpyDeviceToHost, st), "J");
+    if (!rc) rc = check_launch("adjoint sweep");
+    cudaEventRecord(ev_rs_end, rs);
+    cudaStreamWaitEvent(st, ev_rs_end, 0);
+    if (!rc && J_host) rc = check(cudaMemcpyAsync(J_host, s.J, 8, cudaMemcpyDeviceToHost, st), "J");
     if (!rc) rc = check(cudaStreamSynchronize(st), "sync adjoint");
     if (!rc) {
       float ms = 0.f;
@@ -998,21 +1073,29 @@ extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_
         cudaEventElapsedTime(&ms, tev[4 + 4 * sgi], tev[5 + 4 * sgi]);
         h->adj_ms[2] += ms;
       }
+      cudaEventElapsedTime(&ms, tev[1], tev[5]);
+      h->adj_ms[3] = ms;
     }
   } while (0);
+  g.n_rec = d.n_rec;
   cudaStreamSynchronize(st);
-  for (int kk = 0; kk < 2; ++kk) {
-    if (rec_exec[kk]) cudaGraphExecDestroy(rec_exec[kk]);
-    if (rec_graph[kk]) cudaGraphDestroy(rec_graph[kk]);
-    if (bwd_exec[kk]) cudaGraphExecDestroy(bwd_exec[kk]);
-    if (bwd_graph[kk]) cudaGraphDestroy(bwd_graph[kk]);
+  if (rs) {
+    cudaStreamSynchronize(rs);
+    cudaStreamDestroy(rs);
   }
+  for (int b = 0; b < 2; ++b)
+    for (int kk = 0; kk < 2; ++kk) {
+      if (rec_exec[b][kk]) cudaGraphExecDestroy(rec_exec[b][kk]);
+      if (rec_graph[b][kk]) cudaGraphDestroy(rec_graph[b][kk]);
+      if (bwd_exec[b][kk]) cudaGraphExecDestroy(bwd_exec[b][kk]);
+      if (bwd_graph[b][kk]) cudaGraphDestroy(bwd_graph[b][kk]);
+    }
   for (auto ev : tev)
     if (ev) cudaEventDestroy(ev);
-  if (ev_fork) cudaEventDestroy(ev_fork);
-  if (ev_join) cudaEventDestroy(ev_join);
-  void* frees[] = {ck_u, ck_v, a.seg_u, a.seg_v, a.wp, a.v32, a.a32, a.mu_u, a.mu_v, a.y[0], a.y[1], a.out_v,
-                   a.n_dev, a.n_dev_e, a.ticket_e, a.seg_t0, a.rec_map, a.J, a.iE, a.iR};
+  for (cudaEvent_t ev : {ev_fwd, ev_rs_end, rec_done[0], rec_done[1], bwd_done[0], bwd_done[1]})
+    if (ev) cudaEventDestroy(ev);
+  void* frees[] = {ck_u,  ck_v,     s.mu_u, s.mu_v,  s.y[0], s.y[1], s.out_v, s.n_dev, s.ticket_r, t0_dev, s.rec_map,
+                   s.J,   s.iE,     s.iR,   a[0].wp, a[0].v32, a[0].a32, a[0].ys, a[1].wp, a[1].v32, a[1].a32, a[1].ys};
   for (void* q : frees)
     if (q) cudaFree(q);
   if (t_host) cudaFreeHost(t_host);
@@ -1020,8 +1103,10 @@ extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_
   return rc;
 }
 
-extern "C" int sc_nb_adjoint_timings(sc_nb_newmark* h, float* ms3) {
-  if (!h || !ms3) return SC_BAD_ARG;
-  for (int i = 0; i < 3; ++i) ms3[i] = h->adj_ms[i];
+// [0] forward with checkpoints, [1] recompute (summed over segments), [2] backward (summed),
+// [3] the reverse sweep's wall time (recompute and backward overlap on two streams)
+extern "C" int sc_nb_adjoint_timings(sc_nb_newmark* h, float* ms4) {
+  if (!h || !ms4) return SC_BAD_ARG;
+  for (int i = 0; i < 4; ++i) ms4[i] = h->adj_ms[i];
   return SC_OK;
 }

@@ -243,7 +243,7 @@ struct sc_nb_newmark {
   int* rec_map = nullptr;
   cudaGraphExec_t ex_exec[2] = {nullptr, nullptr};
   cudaGraph_t ex_graph[2] = {nullptr, nullptr};
-  float adj_ms[3] = {0.f, 0.f, 0.f};  // last sc_nb_adjoint: forward, recompute, backward (device time)
+  float adj_ms[4] = {0.f, 0.f, 0.f, 0.f};  // last sc_nb_adjoint: forward, recompute, backward, reverse sweep (ms)
 };
 
 // sc_explicit.cu
