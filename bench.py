@@ -364,7 +364,7 @@ def batched_run(k, w, R=256):
                         SETTINGS["absorbing_BC_stiff"], DT)
     b.set_force(table)
     b.set_output(1, rec_eq, n_t)
-    rpt, tpb, tuned_ms = b.config()
+    rpt, tpb, tuned_ms, grid_kernel = b.config()
     b.run(0, w)
     torch.cuda.synchronize()
     e0, e1 = _events()
@@ -401,7 +401,9 @@ def batched_run(k, w, R=256):
     return {"value": vb_rate, "unit": "DOF-steps/s", "single_solve": single, "speedup_vs_single": vb_rate / single,
             "realisations": R, "n_eq": n, "elements": n_el, "steps": k, "warmup": w, "ms_per_step": ms_b / k,
             "single_ms_per_step": ms_s / k, "rel_l2_vs_fp64_realisation0": rel,
-            "tuned_shape": {"realisations_per_thread": rpt, "threads_per_block": tpb, "tuned_ms": tuned_ms},
+            "tuned_shape": {"kernel": "uniform hexa8 grid (k_batch_step_hex8g)" if grid_kernel else
+                            "incidence lists (k_batch_step)", "realisations_per_thread": rpt,
+                            "threads_per_block": tpb, "tuned_ms": tuned_ms},
             "workload": "256 log-normal E realisations, box 40x20x10 m hexa8 0.5 m, Lysmer, Ricker 20 Hz, dt 5e-5",
             "single": "plain FP64 explicit GPU path (node-block graph), realisation 0, same steps"}
 

@@ -289,7 +289,8 @@ int sc_nb_destroy(sc_nb_newmark* h);
  * ratio, and per-realisation Lysmer terms (dashpot coefficients scale with sqrt(E), spring
  * coefficients with E; scatter/system_matrix.py:362-376).  FP32 stiffness products, FP64
  * u and v.  All per-realisation arrays are [slot or element][R] (realisation fastest).
- *   elem [n_elem][n_en] node indices; inc_ptr/inc node -> element incidence (sc_node_incidence)
+ *   elem [n_elem][n_en] node indices; inc_ptr/inc node -> element incidence (each node's list in
+ *     any fixed order: it is the summation order)
  *   ke_type [n_elem] -> ke1 [n_types][3 n_en][3 n_en] float32; young [n_elem][R] float32
  *   ml [3 n_nodes] lumped mass; fixed [3 n_nodes]; alpha, beta Rayleigh; dt time step
  *   l_ptr [3 n_nodes + 1], l_col, l_elem, l_c, l_s: Lysmer entries per slot row: column slot,
@@ -305,13 +306,30 @@ int sc_nb_destroy(sc_nb_newmark* h);
 typedef struct sc_batch_desc sc_batch_desc;
 typedef struct sc_batch sc_batch;
 int sc_batch_create(sc_batch** h, const sc_batch_desc* desc, double* u, double* v, void* stream);
-/* The step kernel's shape (realisations per thread, threads per block) is picked at create
- * time by timing the candidates on scratch copies of the state (no reference counterpart);
- * this reports the choice and its per-step time. */
-int sc_batch_config(sc_batch* h, int* realisations_per_thread, int* threads_per_block, float* ms_per_step);
-/* testing aid: force a shape (realisations per thread in {1, 2, 4, 8} dividing R, by 4 for 4
- * and 8; threads per block a multiple of R / rpt, at most 256) */
+/* The step kernel and its shape (realisations per thread, threads per block) are picked at
+ * create time, and again by sc_batch_set_hex8_grid, by timing the candidates on scratch
+ * copies of the state (no reference counterpart); this reports the choice, its per-step time
+ * and whether it is the uniform hexa8 grid kernel (grid_kernel = 1). */
+int sc_batch_config(sc_batch* h, int* realisations_per_thread, int* threads_per_block, float* ms_per_step,
+                    int* grid_kernel);
+/* Uniform hexa8 grids (no reference counterpart; the meshes scatter/mesher.py reads from
+ * structured gmsh boxes): every element the same shape (n_types = 1), nodes on an integer
+ * lattice along the elements' natural axes (xi, eta, zeta), an element's local node l at its
+ * first node's lattice point plus the natural offset of l (scatter/element_types.py:52-104
+ * order).  The lattice is cut into tiles of 4 x 4 x 2 points; halo [n_tiles][144] int32 lists
+ * the nodes of each tile grown by one point on every side, point (hx, hy, hz) of the 6 x 6 x 4
+ * box at hx + 6 (hy + 6 hz) (-1 where the lattice has no node); elem8 [n_nodes][8] int32 the
+ * element in which the node is local node la (-1 where none).  The incidence lists must be
+ * sorted by the node's local index in the element (that order is the summation order of both
+ * kernels, so they give bitwise the same results).  Device arrays owned by the caller; the
+ * tuner then times both kernels. */
+int sc_batch_set_hex8_grid(sc_batch* h, int n_tiles, const int* halo, const int* elem8);
+/* testing aids: force a shape of the incidence-list kernel (realisations per thread in
+ * {1, 2, 4, 8} dividing R, by 4 for 4 and 8; threads per block a multiple of R / rpt, at most
+ * 256), or of the uniform hexa8 grid kernel (1 or 2 realisations per thread, 128 or 256
+ * threads per block) */
 int sc_batch_set_shape(sc_batch* h, int realisations_per_thread, int threads_per_block);
+int sc_batch_set_grid_shape(sc_batch* h, int realisations_per_thread, int threads_per_block);
 int sc_batch_set_force(sc_batch* h, int n_t, const int64_t* f_ptr, const int* f_slot, const double* f_val);
 /* receivers record v [n_out][n_rec][R] every out_interval steps */
 int sc_batch_set_output(sc_batch* h, int out_interval, int n_rec, const int* rec_slot, double* out_v, int64_t n_out);

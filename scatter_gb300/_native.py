@@ -46,8 +46,11 @@ SIGNATURES = {
     "sc_rf_modes": (I, [ctypes.c_uint64, I, I, D, D, D, P, P]),
     "sc_rf_lognormal": (I, [I, P, I, I, P, D, D, P, P]),
     "sc_batch_create": (I, [ctypes.POINTER(P), P, P, P, P]),
-    "sc_batch_config": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(ctypes.c_float)]),
+    "sc_batch_config": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(ctypes.c_float),
+                            ctypes.POINTER(I)]),
+    "sc_batch_set_hex8_grid": (I, [P, I, P, P]),
     "sc_batch_set_shape": (I, [P, I, I]),
+    "sc_batch_set_grid_shape": (I, [P, I, I]),
     "sc_batch_set_force": (I, [P, I, P, P, P]),
     "sc_batch_set_output": (I, [P, I, I, P, P, L]),
     "sc_batch_run": (I, [P, I, I]),

@@ -39,6 +39,74 @@ def element_types(model, nu, tol=1e-9):
     return first, inv.ravel().astype(np.int32)
 
 
+def incidence_by_local_index(elem_idx, n_nodes):
+    """Node -> element incidence (CSR), each node's elements ordered by the node's local index
+    in the element, then by element."""
+    E, n_en = elem_idx.shape
+    node = elem_idx.ravel()
+    la = np.tile(np.arange(n_en), E)
+    el = np.repeat(np.arange(E), n_en)
+    o = np.lexsort((el, la, node))
+    ptr = np.zeros(n_nodes + 1, dtype=np.int64)
+    ptr[1:] = np.cumsum(np.bincount(node, minlength=n_nodes))
+    if ptr[-1] >= 2**31:
+        raise ValueError("incidence list too long for int32 offsets")
+    return ptr.astype(np.int32), el[o].astype(np.int32)
+
+
+# natural coordinates (0 / 1 for -1 / +1) of the hexa8 nodes in the reference's order
+# (scatter/element_types.py:52-104)
+HEX8_NAT = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]])
+
+
+HEX8_TILE = (4, 4, 2)  # lattice points per tile along xi, eta, zeta (the kernel's kTX, kTY, kTZ)
+
+
+def hex8_grid_tables(xyz, elem_idx, tile=HEX8_TILE):
+    """(halo [n_tiles, (tx+2)(ty+2)(tz+2)], elem8 [n_nodes, 8]) of a uniform hexa8 grid, None
+    for other meshes.  The nodes must sit on an integer lattice along the natural axes of the
+    first element (every element the same shape and orientation), each element's local node l
+    at its first node's lattice point plus the natural offset of l, at most one node per
+    lattice point.  halo lists per tile the nodes of the tile grown by one point on every side
+    (-1 where there is none), point (hx, hy, hz) at hx + (tx+2) (hy + (ty+2) hz); tiles are
+    numbered x fastest.  elem8 [a, la] is the element in which node a is local node la."""
+    n_nodes, E = len(xyz), len(elem_idx)
+    e0 = elem_idx[0]
+    A = np.stack([xyz[e0[1]] - xyz[e0[0]], xyz[e0[3]] - xyz[e0[0]], xyz[e0[4]] - xyz[e0[0]]], axis=1)
+    if abs(np.linalg.det(A)) <= 1e-12 * np.abs(A).max() ** 3:
+        return None
+    L = np.linalg.solve(A, (xyz - xyz[e0[0]]).T).T
+    Li = np.rint(L)
+    if np.abs(L - Li).max() > 1e-6:
+        return None
+    Li = Li.astype(np.int64)
+    Li -= Li.min(axis=0)
+    if np.any(Li[elem_idx] != Li[elem_idx[:, :1]] + HEX8_NAT[None]):
+        return None
+    tile = np.asarray(tile)
+    ext = Li.max(axis=0) + 1
+    nt = -(-ext // tile)
+    box = nt * tile + 2  # padded lattice: one point of margin on every side
+    key = (Li[:, 0] + 1) + box[0] * ((Li[:, 1] + 1) + box[1] * (Li[:, 2] + 1))
+    if len(np.unique(key)) != n_nodes:
+        return None
+    dense = np.full(int(np.prod(box)), -1, dtype=np.int64)
+    dense[key] = np.arange(n_nodes)
+    elem8 = np.full((n_nodes, 8), -1, dtype=np.int64)
+    for la in range(8):
+        elem8[elem_idx[:, la], la] = np.arange(E)
+    hb = tile + 2
+    T = np.arange(int(np.prod(nt)))
+    tx, ty, tz = T % nt[0], (T // nt[0]) % nt[1], T // (nt[0] * nt[1])
+    H = np.arange(int(np.prod(hb)))
+    hx, hy, hz = H % hb[0], (H // hb[0]) % hb[1], H // (hb[0] * hb[1])
+    px = tx[:, None] * tile[0] + hx[None]
+    py = ty[:, None] * tile[1] + hy[None]
+    pz = tz[:, None] * tile[2] + hz[None]
+    halo = dense[px + box[0] * (py + box[1] * pz)]
+    return halo.astype(np.int32), elem8.astype(np.int32)
+
+
 class BatchedExplicit:
     def __init__(self, model, young, nu, rho, damping, absorbing, k_div, dt, order=2):
         """young: per-element, per-realisation E [n_elem, R] (numpy or CUDA float32)."""
@@ -84,13 +152,12 @@ class BatchedExplicit:
         self.ke1 = ke.to(torch.float32)
         self.ke_type = dv.to_dev(ktype, torch.int32)
         self.n_types = len(first)
-        # node -> element incidence
+        # node -> element incidence, each node's list sorted by the node's local index in the
+        # element (then element): the summation order of both step kernels
         self.elem = dv.to_dev(elem_idx, torch.int32)
-        self.inc_ptr = dv.empty(N + 1, torch.int32)
-        self.inc = dv.empty(n_elem * n_en, torch.int32)
-        work = dv.empty(N, torch.int32)
-        nat.call("sc_node_incidence", n_elem, n_en, N, self.elem.data_ptr(), self.inc_ptr.data_ptr(),
-                 self.inc.data_ptr(), work.data_ptr(), s)
+        ptr, inc = incidence_by_local_index(elem_idx, N)
+        self.inc_ptr = dv.to_dev(ptr, torch.int32)
+        self.inc = dv.to_dev(inc, torch.int32)
         # Lysmer entries scaled per realisation (unit E here)
         self._lysmer(model, (ones, nu, rho), absorbing, k_div, order, N)
         self.young = (young if torch.is_tensor(young) else dv.to_dev(np.asarray(young, dtype=np.float32),
@@ -108,6 +175,15 @@ class BatchedExplicit:
         nat.call("sc_batch_create", ctypes.byref(h), ctypes.byref(d), self.u.data_ptr(), self.v.data_ptr(), s)
         self.h = h
         self.dt = dt
+        # uniform hexa8 grids: the neighbour-register kernel joins the tuner's candidates
+        self.grid_tables = None
+        if etype == "hexa8" and self.n_types == 1:
+            self.grid_tables = hex8_grid_tables(nodes[:, 1:].astype(float), elem_idx)
+        if self.grid_tables is not None:
+            self._halo = dv.to_dev(self.grid_tables[0], torch.int32)
+            self._elem8 = dv.to_dev(self.grid_tables[1], torch.int32)
+            nat.call("sc_batch_set_hex8_grid", self.h, len(self.grid_tables[0]), self._halo.data_ptr(),
+                     self._elem8.data_ptr())
 
     def _lysmer(self, model, props, absorbing, k_div, order, N):
         etype = str(model.element_type)
@@ -146,14 +222,16 @@ class BatchedExplicit:
         self.l_s = dv.to_dev(sv.astype(np.float32), torch.float32)
 
     def config(self):
-        """(realisations per thread, threads per block, tuned ms per step) of the step kernel."""
-        rpt, tpb, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
-        nat.call("sc_batch_config", self.h, ctypes.byref(rpt), ctypes.byref(tpb), ctypes.byref(ms))
-        return rpt.value, tpb.value, ms.value
+        """(realisations per thread, threads per block, tuned ms per step, grid kernel) of the
+        step kernel; grid kernel is True for the uniform hexa8 grid kernel."""
+        rpt, tpb, ms, grid = ctypes.c_int(), ctypes.c_int(), ctypes.c_float(), ctypes.c_int()
+        nat.call("sc_batch_config", self.h, ctypes.byref(rpt), ctypes.byref(tpb), ctypes.byref(ms), ctypes.byref(grid))
+        return rpt.value, tpb.value, ms.value, bool(grid.value)
 
-    def set_shape(self, realisations_per_thread, threads_per_block):
-        """Override the tuned kernel shape (testing aid)."""
-        nat.call("sc_batch_set_shape", self.h, int(realisations_per_thread), int(threads_per_block))
+    def set_shape(self, realisations_per_thread, threads_per_block, grid=False):
+        """Override the tuned kernel and shape (testing aid)."""
+        fn = "sc_batch_set_grid_shape" if grid else "sc_batch_set_shape"
+        nat.call(fn, self.h, int(realisations_per_thread), int(threads_per_block))
 
     def set_force(self, table: ForceTable):
         eq = dv.to_dev(table.f_eq, torch.int64)

@@ -16,6 +16,8 @@
 // rate; the caller's FP64 u, v are converted in at the start of a run and out at its end.
 // w = u + beta v and v are also kept as FP32 ping-pong copies that neighbours read.  RPT and the nodes per block come from a short
 // timing of the candidates on scratch copies of the state when the handle is created.
+#include <vector>
+
 #include "sc_common.cuh"
 
 struct sc_batch_desc {
@@ -51,6 +53,7 @@ struct Args {
   double* out_v;       // [n_out][n_rec][R]
   int64_t n_out;
   unsigned* ticket;    // blocks finished in the current launch (last-block detection)
+  const unsigned char* vneed;  // slot -> 1 when a Lysmer row reads its velocity (FP32 copy kept)
 };
 
 template <int RPT>
@@ -165,7 +168,7 @@ __device__ inline bool batch_last_block(unsigned* ticket) {
   __shared__ bool am_last;
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) am_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  if (threadIdx.x == 0) am_last = (atomicAdd(ticket, 1u) == gridDim.x * gridDim.y - 1);
   __syncthreads();
   return am_last;
 }
@@ -233,7 +236,7 @@ __device__ __forceinline__ void node_update(const Args& g, int a, int r0, const 
 #pragma unroll
       for (int r = 0; r < RPT; ++r) wo[r] = vo[r] = 0.f;
       stf<RPT>(w_out + ir, wo);
-      stf<RPT>(vf_out + ir, vo);
+      if (g.vneed[i]) stf<RPT>(vf_out + ir, vo);
       continue;
     }
     float spring[RPT], dash[RPT];
@@ -253,10 +256,8 @@ __device__ __forceinline__ void node_update(const Args& g, int a, int r0, const 
       }
     }
     float2 vp[RPT], up[RPT];
-    float vown[RPT];
     ldp<RPT>(g.v2 + ir, vp);
     ldp<RPT>(g.u2 + ir, up);
-    ldf<RPT>(vf_in + ir, vown);
     const float fi = (float)g.f[i], mlf = g.ml32[i], imlf = g.iml32[i];
     const float aml = __fmul_rn(g.alpha32, mlf);
 #pragma unroll
@@ -264,7 +265,8 @@ __device__ __forceinline__ void node_update(const Args& g, int a, int r0, const 
       // FP32 acceleration (its inputs are FP32 products); _rn intrinsics keep the rounding
       // the same for every kernel shape
       const float kw = __fadd_rn(acc[c][r], spring[r]);
-      const float num = __fsub_rn(__fsub_rn(__fsub_rn(fi, kw), __fmul_rn(aml, vown[r])), dash[r]);
+      // own velocity: the pair's hi part, which is what the FP32 copy holds
+      const float num = __fsub_rn(__fsub_rn(__fsub_rn(fi, kw), __fmul_rn(aml, vp[r].x)), dash[r]);
       const float accel = __fmul_rn(num, imlf);
       pair_madd(vp[r], g.dth, accel, __fmul_rn(g.dtl, accel));                           // v += dt a
       pair_madd(up[r], g.dth, vp[r].x, fmaf(g.dth, vp[r].y, __fmul_rn(g.dtl, vp[r].x)));  // u += dt v
@@ -274,7 +276,7 @@ __device__ __forceinline__ void node_update(const Args& g, int a, int r0, const 
     stp<RPT>(g.v2 + ir, vp);
     stp<RPT>(g.u2 + ir, up);
     stf<RPT>(w_out + ir, wo);
-    stf<RPT>(vf_out + ir, vo);
+    if (g.vneed[i]) stf<RPT>(vf_out + ir, vo);
     if (rec_now) {
       const int rj = g.rec_map[i];
       if (rj >= 0) {
@@ -351,6 +353,159 @@ __global__ void __launch_bounds__(256) k_batch_step_mixed(Args g, const float* _
   step_epilogue(g, step);
 }
 
+// ------------------------------------------------------------------ uniform hexa8 grids
+// Meshes of one hexa8 element shape on a structured node lattice: lattice coordinates along
+// the elements' natural axes (xi, eta, zeta), an element's local node l at its first node's
+// lattice point plus the natural offset of l.  The lattice is cut into tiles of kTX x kTY x
+// kTZ points; halo [tile][kHN] lists the nodes of the tile grown by one point on every side
+// (-1 where the lattice has no node), point (hx, hy, hz) at hx + kHX (hy + kHY hz); elem8
+// [node][8] the element in which the node is local node la (-1 where none).  A block takes
+// one tile and 32 RPT consecutive realisations: it stages the halo's w in shared memory with
+// coalesced loads (about 4.5 loads per owned node where the incidence-list kernel gathers 64
+// node vectors), then a warp per owned node reads its 27 neighbours at fixed offsets into
+// registers, and the unit-E stiffness is a kernel parameter, so every FMA takes its K1 entry
+// from the constant bank.  Elements are visited in local-index order with the FMA sequence
+// of node_forces, which visits incidence lists sorted the same way: the results are bitwise
+// those of the incidence-list kernel.
+constexpr int kTX = 4, kTY = 4, kTZ = 2;
+constexpr int kHX = kTX + 2, kHY = kTY + 2, kHZ = kTZ + 2, kHN = kHX * kHY * kHZ;
+
+struct K1Hex8 {
+  float k[576];  // [3 la + c][3 lb + comp]
+};
+
+__host__ __device__ constexpr int hex8_nat(int l, int axis) {  // natural coordinate of local node l, 0 or 1
+  return axis == 0 ? ((l == 1 || l == 2 || l == 5 || l == 6) ? 1 : 0)
+                   : (axis == 1 ? ((l == 2 || l == 3 || l == 6 || l == 7) ? 1 : 0) : (l >= 4 ? 1 : 0));
+}
+// 27-neighbour index (dxi + 1) + 3 (deta + 1) + 9 (dzeta + 1) of lb seen from la, and the halo
+// offset of neighbour q
+__host__ __device__ constexpr int hex8_q(int la, int lb) {
+  return (hex8_nat(lb, 0) - hex8_nat(la, 0) + 1) + 3 * (hex8_nat(lb, 1) - hex8_nat(la, 1) + 1) +
+         9 * (hex8_nat(lb, 2) - hex8_nat(la, 2) + 1);
+}
+__host__ __device__ constexpr int q_off(int q) { return (q % 3 - 1) + kHX * ((q / 3) % 3 - 1 + kHY * (q / 9 - 1)); }
+
+template <int RPT>
+__device__ __forceinline__ void lds_f(const float* p, float (&v)[RPT]) {
+  if constexpr (RPT == 2) {
+    const float2 a = *reinterpret_cast<const float2*>(p);
+    v[0] = a.x;
+    v[1] = a.y;
+  } else {
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) v[q] = p[q];
+  }
+}
+
+// One step for all realisations on a uniform hexa8 grid: grid (tiles, realisation chunks of
+// 32 RPT), dynamic shared memory kHN * 3 * 32 RPT floats.
+template <int RPT>
+__global__ void __launch_bounds__(256) k_batch_step_hex8g(Args g, const __grid_constant__ K1Hex8 k1,
+                                                         const int* __restrict__ halo, const int* __restrict__ elem8,
+                                                         const float* __restrict__ w_in, float* __restrict__ w_out,
+                                                         const float* __restrict__ vf_in, float* __restrict__ vf_out) {
+  extern __shared__ __align__(16) float sw[];  // [kHN][3][RC]
+  constexpr int RC = 32 * RPT;
+  const int R = g.d.R;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int* ht = halo + (int64_t)blockIdx.x * kHN;
+  const int r0 = blockIdx.y * RC + lane * RPT;
+  const int step = *g.t + 1;
+  const bool rec_now = record_now(g, step);
+  // the halo's w for this chunk staged by asynchronous copies (zeros where there is no node
+  // and beyond R): 16-byte pieces when rows are 16-byte aligned (R % 4 == 0), else 4-byte
+  const int rc0 = blockIdx.y * RC;
+  const unsigned sbase = (unsigned)__cvta_generic_to_shared(sw);
+  if (R % 4 == 0) {
+    constexpr int PR = RC / 4;  // pieces per row
+    for (int pc = threadIdx.x; pc < kHN * 3 * PR; pc += blockDim.x) {
+      const int row = pc / PR, k = pc - row * PR;
+      const int node = __ldg(ht + row / 3), r = rc0 + 4 * k;
+      const int bytes = node < 0 || r >= R ? 0 : (R - r >= 4 ? 16 : 4 * (R - r));
+      const float* src = bytes ? w_in + ((int64_t)node * 3 + row % 3) * R + r : w_in;
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sbase + 4u * (row * RC + 4 * k)),
+                   "l"(src), "r"(bytes));
+    }
+  } else {
+    for (int pc = threadIdx.x; pc < kHN * 3 * RC; pc += blockDim.x) {
+      const int row = pc / RC, k = pc - row * RC;
+      const int node = __ldg(ht + row / 3), r = rc0 + k;
+      const int bytes = node < 0 || r >= R ? 0 : 4;
+      const float* src = bytes ? w_in + ((int64_t)node * 3 + row % 3) * R + r : w_in;
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sbase + 4u * (row * RC + k)), "l"(src),
+                   "r"(bytes));
+    }
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncthreads();
+  if (r0 < R) {
+    for (int n = warp; n < kTX * kTY * kTZ; n += nw) {
+      const int hb = (n % kTX + 1) + kHX * ((n / kTX) % kTY + 1 + kHY * (n / (kTX * kTY) + 1));
+      const int a = __ldg(ht + hb);
+      if (a < 0) continue;
+      // the node's pair state into L2 ahead of its update, and its elements' E
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int64_t ir = ((int64_t)a * 3 + c) * R + r0;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(g.u2 + ir)));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(g.v2 + ir)));
+      }
+      int el[8];
+      float Eall[8][RPT];
+#pragma unroll
+      for (int la = 0; la < 8; ++la) el[la] = __ldg(elem8 + (int64_t)a * 8 + la);
+#pragma unroll
+      for (int la = 0; la < 8; ++la) {
+        if (el[la] >= 0) {
+          ldf<RPT>(g.d.young + (int64_t)el[la] * R + r0, Eall[la]);
+        } else {
+#pragma unroll
+          for (int r = 0; r < RPT; ++r) Eall[la][r] = 0.f;
+        }
+      }
+      const float* sb = sw + hb * 3 * RC + lane * RPT;
+      float wv[27][3][RPT];
+#pragma unroll
+      for (int q = 0; q < 27; ++q)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) lds_f<RPT>(sb + (q_off(q) * 3 + c) * RC, wv[q][c]);
+      float acc[3][RPT];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) acc[c][r] = 0.f;
+#pragma unroll
+      for (int la = 0; la < 8; ++la) {
+        if (el[la] < 0) continue;
+        float t[3][RPT];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int r = 0; r < RPT; ++r) t[c][r] = 0.f;
+#pragma unroll
+        for (int lb = 0; lb < 8; ++lb) {
+          const int q = hex8_q(la, lb);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const int kb = (la * 3 + c) * 24 + lb * 3;
+            fma3<RPT>(t[c], k1.k[kb], k1.k[kb + 1], k1.k[kb + 2], wv[q][0], wv[q][1], wv[q][2]);
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) fma1<RPT>(acc[c], Eall[la], t[c]);
+      }
+      node_update<RPT>(g, a, r0, acc, w_in, w_out, vf_in, vf_out, step, rec_now);
+    }
+  }
+  step_epilogue(g, step);
+}
+
+__global__ void k_mark_slots(int64_t n, const int* __restrict__ idx, unsigned char* flag) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    flag[idx[q]] = 1;
+}
+
 __device__ inline float2 split2(double x) {
   const float h = (float)x;
   return make_float2(h, (float)(x - (double)h));
@@ -411,7 +566,12 @@ struct sc_batch {
   cudaGraph_t graph[2] = {nullptr, nullptr};
   unsigned blocks = 1;
   int rpt = 1, threads = 32, tpn = 32;  // shape chosen by the tuner
+  int grid = 0;                         // 1: the uniform hexa8 grid kernel
   float tuned_ms = 0.f;
+  unsigned char* vneed = nullptr;
+  int n_tiles = 0;
+  const int *halo = nullptr, *elem8 = nullptr;  // uniform hexa8 grid tables (caller's), or null
+  K1Hex8 k1{};
 };
 
 static void batch_drop_graphs(sc_batch* h) {
@@ -432,8 +592,23 @@ static void launch_rpt(int rpt, unsigned blocks, int threads, int tpn, cudaStrea
   }
 }
 
-static void batch_launch(const sc_batch* h, const Args& g, int rpt, int threads, int tpn, cudaStream_t st,
+template <int RPT>
+static void launch_hex8g(const sc_batch* h, const Args& g, int threads, cudaStream_t st, const float* wi, float* wo,
+                         const float* vi, float* vo) {
+  const unsigned by = (unsigned)((g.d.R + 32 * RPT - 1) / (32 * RPT));
+  const size_t smem = sizeof(float) * kHN * 3 * 32 * RPT;
+  k_batch_step_hex8g<RPT><<<dim3((unsigned)h->n_tiles, by), threads, smem, st>>>(g, h->k1, h->halo, h->elem8, wi, wo,
+                                                                                 vi, vo);
+}
+
+// grid = 1: the uniform hexa8 grid kernel (threads per block, realisations per thread; tpn unused)
+static void batch_launch(const sc_batch* h, const Args& g, int grid, int rpt, int threads, int tpn, cudaStream_t st,
                          const float* wi, float* wo, const float* vi, float* vo) {
+  if (grid) {
+    if (rpt == 2) launch_hex8g<2>(h, g, threads, st, wi, wo, vi, vo);
+    else launch_hex8g<1>(h, g, threads, st, wi, wo, vi, vo);
+    return;
+  }
   const int npb = threads / tpn;
   const int64_t want = ((int64_t)g.d.n_nodes + npb - 1) / npb;
   const unsigned blocks = (unsigned)(want < 152 * 32 ? want : 152 * 32);
@@ -490,40 +665,51 @@ static int batch_tune(sc_batch* h) {
     g.ticket = tk;
     g.f_ptr = nullptr;
     g.n_rec = 0;
+    // candidates: (grid kernel, realisations per thread, threads per block)
+    struct Cand {
+      int grid, rpt, threads, tpn;
+    };
+    std::vector<Cand> cands;
     const int rpts[4] = {1, 2, 4, 8};
     const int tpbs[3] = {128, 256, 64};
     const bool mixed = g0.d.node_nen != nullptr;  // one realisation, one thread per node
-    for (int ri = 0; ri < 4 && !rc; ++ri) {
+    for (int ri = 0; ri < 4; ++ri) {
       const int rpt = rpts[ri];
       if (R % rpt != 0 || (rpt >= 4 && R % 4 != 0)) continue;
       if (mixed && rpt != 1) continue;
       const int tpn = (R + rpt - 1) / rpt;
-      for (int bi = 0; bi < (mixed ? 3 : 2) && !rc; ++bi) {
-        if (tpn > tpbs[bi]) continue;
-        const int threads = (tpbs[bi] / tpn) * tpn;
-        float* wh = w;
-        float* wl = w + nsr;
-        float* vh = vf;
-        float* vl = vf + nsr;
-        for (int q = 0; q < 2; ++q) batch_launch(h, g, rpt, threads, tpn, st, wh, wl, vh, vl);
-        float ms_min = -1.f;
-        for (int q = 0; q < 5 && !rc; ++q) {
-          cudaEventRecord(e0, st);
-          batch_launch(h, g, rpt, threads, tpn, st, (q & 1) ? wl : wh, (q & 1) ? wh : wl, (q & 1) ? vl : vh,
-                       (q & 1) ? vh : vl);
-          cudaEventRecord(e1, st);
-          if ((rc = check_launch("batch tune"))) break;
-          if ((rc = check(cudaEventSynchronize(e1), "tune sync"))) break;
-          float ms = 0.f;
-          cudaEventElapsedTime(&ms, e0, e1);
-          if (ms_min < 0.f || ms < ms_min) ms_min = ms;
-        }
-        if (!rc && (best < 0.f || ms_min < best)) {
-          best = ms_min;
-          h->rpt = rpt;
-          h->threads = threads;
-          h->tpn = tpn;
-        }
+      for (int bi = 0; bi < (mixed ? 3 : 2); ++bi)
+        if (tpn <= tpbs[bi]) cands.push_back({0, rpt, (tpbs[bi] / tpn) * tpn, tpn});
+    }
+    if (h->halo)
+      for (int rpt = 1; rpt <= 2; ++rpt)
+        if (R % rpt == 0)
+          for (int threads : {256, 128}) cands.push_back({1, rpt, threads, 0});
+    for (size_t ci = 0; ci < cands.size() && !rc; ++ci) {
+      const Cand& c = cands[ci];
+      float* wh = w;
+      float* wl = w + nsr;
+      float* vh = vf;
+      float* vl = vf + nsr;
+      for (int q = 0; q < 2; ++q) batch_launch(h, g, c.grid, c.rpt, c.threads, c.tpn, st, wh, wl, vh, vl);
+      float ms_min = -1.f;
+      for (int q = 0; q < 5 && !rc; ++q) {
+        cudaEventRecord(e0, st);
+        batch_launch(h, g, c.grid, c.rpt, c.threads, c.tpn, st, (q & 1) ? wl : wh, (q & 1) ? wh : wl,
+                     (q & 1) ? vl : vh, (q & 1) ? vh : vl);
+        cudaEventRecord(e1, st);
+        if ((rc = check_launch("batch tune"))) break;
+        if ((rc = check(cudaEventSynchronize(e1), "tune sync"))) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms_min < 0.f || ms < ms_min) ms_min = ms;
+      }
+      if (!rc && (best < 0.f || ms_min < best)) {
+        best = ms_min;
+        h->grid = c.grid;
+        h->rpt = c.rpt;
+        h->threads = c.threads;
+        h->tpn = c.tpn;
       }
     }
   } while (0);
@@ -542,7 +728,8 @@ static int batch_build(sc_batch* h) {
   for (int k = 0; k < 2; ++k) {
     int rc = check(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal), "capture batch");
     if (rc) return rc;
-    batch_launch(h, h->g, h->rpt, h->threads, h->tpn, h->cap, h->w[k], h->w[k ^ 1], h->vf[k], h->vf[k ^ 1]);
+    batch_launch(h, h->g, h->grid, h->rpt, h->threads, h->tpn, h->cap, h->w[k], h->w[k ^ 1], h->vf[k],
+                 h->vf[k ^ 1]);
     cudaGraph_t gr;
     if ((rc = check(cudaStreamEndCapture(h->cap, &gr), "end batch"))) return rc;
     if ((rc = check(cudaGraphInstantiate(&h->exec[k], gr, 0), "instantiate batch"))) {
@@ -587,7 +774,15 @@ extern "C" int sc_batch_create(sc_batch** out, const sc_batch_desc* d, double* u
     if ((rc = check(cudaMallocAsync((void**)&h->v2, 8 * nsr, st), "malloc"))) break;
     if ((rc = check(cudaMallocAsync((void**)&h->ml32, 4 * ns, st), "malloc"))) break;
     if ((rc = check(cudaMallocAsync((void**)&h->iml32, 4 * ns, st), "malloc"))) break;
+    if ((rc = check(cudaMallocAsync((void**)&h->vneed, ns, st), "malloc"))) break;
     k_batch_consts<<<grid_for(ns, 256), 256, 0, st>>>(ns, d->ml, h->ml32, h->iml32);
+    // slots whose FP32 velocity copy a Lysmer row reads
+    cudaMemsetAsync(h->vneed, 0, ns, st);
+    int64_t n_l = 0;
+    if ((rc = check(cudaMemcpyAsync(&n_l, d->l_ptr + ns, 8, cudaMemcpyDeviceToHost, st), "lysmer size"))) break;
+    if ((rc = check(cudaStreamSynchronize(st), "sync"))) break;
+    if (n_l > 0) k_mark_slots<<<grid_for(n_l, 256), 256, 0, st>>>(n_l, d->l_col, h->vneed);
+    h->g.vneed = h->vneed;
     h->g.u2 = h->u2;
     h->g.v2 = h->v2;
     h->g.ml32 = h->ml32;
@@ -615,6 +810,43 @@ extern "C" int sc_batch_create(sc_batch** out, const sc_batch_desc* d, double* u
   return SC_OK;
 }
 
+// Enables the uniform hexa8 grid kernel (tables as described at k_batch_step_hex8g; the
+// incidence lists must be sorted by the node's local index in the element) and re-runs the
+// tuner over both kernels.
+extern "C" int sc_batch_set_hex8_grid(sc_batch* h, int n_tiles, const int* halo, const int* elem8) {
+  if (!h || n_tiles <= 0 || !halo || !elem8 || h->g.d.n_en != 8 || h->g.d.n_types != 1 || h->g.d.node_nen)
+    return SC_BAD_ARG;
+  if ((h->g.d.R + 63) / 64 > 65535) return SC_BAD_ARG;
+  cudaStream_t st = h->user;
+  int rc = check(cudaMemcpyAsync(h->k1.k, h->g.d.ke1, sizeof(h->k1.k), cudaMemcpyDeviceToHost, st), "k1");
+  if (!rc) rc = check(cudaStreamSynchronize(st), "sync");
+  if (!rc) rc = check(cudaFuncSetAttribute(k_batch_step_hex8g<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(sizeof(float) * kHN * 3 * 32)), "smem attribute");
+  if (!rc) rc = check(cudaFuncSetAttribute(k_batch_step_hex8g<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(sizeof(float) * kHN * 3 * 64)), "smem attribute");
+  if (rc) return rc;
+  h->n_tiles = n_tiles;
+  h->halo = halo;
+  h->elem8 = elem8;
+  batch_drop_graphs(h);
+  return batch_tune(h);
+}
+
+// Selects the uniform hexa8 grid kernel with 1 or 2 realisations per thread and 128 or 256
+// threads per block (testing aid; needs sc_batch_set_hex8_grid).
+extern "C" int sc_batch_set_grid_shape(sc_batch* h, int realisations_per_thread, int threads_per_block) {
+  if (!h || !h->halo) return SC_BAD_ARG;
+  const int rpt = realisations_per_thread;
+  if ((rpt != 1 && rpt != 2) || h->g.d.R % rpt != 0) return SC_BAD_ARG;
+  if (threads_per_block != 128 && threads_per_block != 256) return SC_BAD_ARG;
+  h->grid = 1;
+  h->rpt = rpt;
+  h->threads = threads_per_block;
+  h->tpn = 0;
+  batch_drop_graphs(h);
+  return SC_OK;
+}
+
 extern "C" int sc_batch_set_shape(sc_batch* h, int realisations_per_thread, int threads_per_block) {
   if (!h) return SC_BAD_ARG;
   const int R = h->g.d.R, rpt = realisations_per_thread;
@@ -622,6 +854,7 @@ extern "C" int sc_batch_set_shape(sc_batch* h, int realisations_per_thread, int 
   if (R % rpt != 0 || (rpt >= 4 && R % 4 != 0)) return SC_BAD_ARG;
   const int tpn = (R + rpt - 1) / rpt;
   if (threads_per_block < tpn || threads_per_block > 256 || threads_per_block % tpn != 0) return SC_BAD_ARG;
+  h->grid = 0;
   h->rpt = rpt;
   h->threads = threads_per_block;
   h->tpn = tpn;
@@ -629,11 +862,13 @@ extern "C" int sc_batch_set_shape(sc_batch* h, int realisations_per_thread, int 
   return SC_OK;
 }
 
-extern "C" int sc_batch_config(sc_batch* h, int* realisations_per_thread, int* threads_per_block, float* ms_per_step) {
+extern "C" int sc_batch_config(sc_batch* h, int* realisations_per_thread, int* threads_per_block, float* ms_per_step,
+                               int* grid_kernel) {
   if (!h) return SC_BAD_ARG;
   if (realisations_per_thread) *realisations_per_thread = h->rpt;
   if (threads_per_block) *threads_per_block = h->threads;
   if (ms_per_step) *ms_per_step = h->tuned_ms;
+  if (grid_kernel) *grid_kernel = h->grid;
   return SC_OK;
 }
 
@@ -696,7 +931,7 @@ extern "C" int sc_batch_destroy(sc_batch* h) {
   if (h->f) cudaFree(h->f);
   if (h->t) cudaFree(h->t);
   if (h->ticket) cudaFree(h->ticket);
-  void* more[] = {h->u2, h->v2, h->ml32, h->iml32};
+  void* more[] = {h->u2, h->v2, h->ml32, h->iml32, h->vneed};
   for (void* q : more)
     if (q) cudaFree(q);
   if (h->cap) cudaStreamDestroy(h->cap);

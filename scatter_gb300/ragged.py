@@ -321,7 +321,7 @@ class RaggedBatch:
         nat.call("sc_batch_set_force", self.h, n_t, t["f_ptr"].data_ptr(), t["f_slot"].data_ptr(),
                  t["f_val"].data_ptr())
         rpt, tpb, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
-        nat.call("sc_batch_config", self.h, ctypes.byref(rpt), ctypes.byref(tpb), ctypes.byref(ms))
+        nat.call("sc_batch_config", self.h, ctypes.byref(rpt), ctypes.byref(tpb), ctypes.byref(ms), None)
         self.tuned = (tpb.value, ms.value)
 
     def set_output(self, interval, n_out):

@@ -92,8 +92,9 @@ def test_batched_matches_per_realisation_fp64(cuda):
 
 
 def test_batched_shapes_agree_bitwise(cuda):
-    """Every kernel shape the tuner may pick (realisations per thread, threads per block)
-    gives bitwise the same histories: the per-realisation arithmetic is the same."""
+    """Every kernel and shape the tuner may pick (the incidence-list kernel with 1 to 8
+    realisations per thread, the uniform hexa8 grid kernel with 1 or 2) gives bitwise the same
+    histories: the per-realisation arithmetic and summation order are the same."""
     from scatter_gb300 import meshgen
     from scatter_gb300.batched import BatchedExplicit
     from scatter_gb300.force_external import ricker_table
@@ -108,9 +109,12 @@ def test_batched_shapes_agree_bitwise(cuda):
     table = ricker_table(m, int(top[len(top) // 2]), -1e4, 20.0, 0.002, time)
     rec = [int(m.eq_nb_dof[m.node_index()[n], 1]) for n in top[::5]]
     results = []
-    for rpt, tpb in ((1, 128), (1, 256), (2, 128), (4, 256), (8, 128)):
+    shapes = ((1, 128, False), (1, 256, False), (2, 128, False), (4, 256, False), (8, 128, False), (1, 128, True),
+              (1, 256, True), (2, 128, True), (2, 256, True))
+    for rpt, tpb, grid in shapes:
         b = BatchedExplicit(m, young, 0.3, 1900.0, [1, 0.02, 50, 0.02], [1, 1], 1e3, dt)
-        b.set_shape(rpt, tpb)
+        assert b.grid_tables is not None
+        b.set_shape(rpt, tpb, grid)
         b.set_force(table)
         b.set_output(1, rec, n_t)
         b.run(0, n_t - 1)

@@ -184,3 +184,54 @@ def test_matrix_free_lumped_mass_equals_assembled_row_sums():
     Mtx = Mt.reshape(k, 10, 3, 10, 3)[:, :, 0, :, 0]
     h = lumped_mass(Mtx, np.arange(k), ei, np.ones_like(em, dtype=bool), 1.0, hrz=True)
     assert h.min() > 0 and abs(h[:, 0].sum() / Mtx.sum() - 1) < 1e-12
+
+
+def test_batched_incidence_and_hex8_grid_tables():
+    """Host tables of the batched step: incidence lists ordered by the node's local index in
+    the element, and the uniform hexa8 grid tables (every element's node lb found in the tile
+    halo of its node la at the natural offset between them), None for meshes that are not such
+    grids."""
+    from scatter_gb300.batched import HEX8_NAT, HEX8_TILE, hex8_grid_tables, incidence_by_local_index
+    from scatter_gb300.system_matrix import model_arrays
+
+    m = meshgen.box_model(5, 3, 4, 0.5)
+    nodes, _, elem_idx, _ = model_arrays(m)
+    xyz = nodes[:, 1:].astype(float)
+    N, E = len(nodes), len(elem_idx)
+    ptr, inc = incidence_by_local_index(elem_idx, N)
+    assert ptr[-1] == E * 8
+    for a in (0, N // 2, N - 1):
+        els = inc[ptr[a]:ptr[a + 1]]
+        las = [int(np.nonzero(elem_idx[e] == a)[0][0]) for e in els]
+        assert las == sorted(las) and sorted(els.tolist()) == sorted(np.nonzero((elem_idx == a).any(1))[0].tolist())
+    halo, elem8 = hex8_grid_tables(xyz, elem_idx)
+    tx, ty, tz = HEX8_TILE
+    hx, hy = tx + 2, ty + 2
+    assert halo.shape[1] == hx * hy * (tz + 2)
+    # each node owned by exactly one tile (the halo's interior points)
+    inner = [(x + 1) + hx * ((y + 1) + hy * (z + 1)) for z in range(tz) for y in range(ty) for x in range(tx)]
+    owned = halo[:, inner].ravel()
+    owned = owned[owned >= 0]
+    assert len(owned) == N and len(np.unique(owned)) == N
+    where = {}
+    for t in range(len(halo)):
+        for p in inner:
+            if halo[t, p] >= 0:
+                where[int(halo[t, p])] = (t, p)
+    for e in range(E):
+        for la in range(8):
+            a = elem_idx[e, la]
+            assert elem8[a, la] == e
+            t, p = where[int(a)]
+            for lb in range(8):
+                d = HEX8_NAT[lb] - HEX8_NAT[la]
+                assert halo[t, p + d[0] + hx * (d[1] + hy * d[2])] == elem_idx[e, lb]
+    # boundary: a corner node has one element; its halo holds -1 outside the mesh
+    deg = np.bincount(elem_idx.ravel(), minlength=N)
+    corner = int(np.nonzero(deg == 1)[0][0])
+    assert (elem8[corner] >= 0).sum() == 1
+    assert (halo == -1).any()
+    # a reversed element breaks the common orientation
+    bad = elem_idx.copy()
+    bad[3] = bad[3][[1, 0, 3, 2, 5, 4, 7, 6]]
+    assert hex8_grid_tables(xyz, bad) is None
