@@ -42,7 +42,8 @@ struct Args {
   float2 *u2, *v2;      // the accumulators as (hi, lo) pairs, [slot][R]
   const float *ml32, *iml32;  // lumped mass and its reciprocal, FP32
   float dth, dtl, alpha32, beta32;  // dt as a pair; Rayleigh coefficients
-  double* f;  // dense force, slot space (shared by the realisations)
+  double* f;    // dense force, slot space (shared by the realisations)
+  float* f32;   // its FP32 copy, what the update reads (kept by the force swap)
   int* t;     // device step counter
   int n_t;
   const int64_t* f_ptr;
@@ -258,7 +259,7 @@ __device__ __forceinline__ void node_update(const Args& g, int a, int r0, const 
     float2 vp[RPT], up[RPT];
     ldp<RPT>(g.v2 + ir, vp);
     ldp<RPT>(g.u2 + ir, up);
-    const float fi = (float)g.f[i], mlf = g.ml32[i], imlf = g.iml32[i];
+    const float fi = g.f32[i], mlf = g.ml32[i], imlf = g.iml32[i];
     const float aml = __fmul_rn(g.alpha32, mlf);
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
@@ -295,10 +296,17 @@ __device__ __forceinline__ void step_epilogue(const Args& g, int step) {
     const int t = step - 1;
     if (g.f_ptr) {
       if (t >= 0 && t < g.n_t)
-        for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f[g.f_slot[k]] = 0.0;
+        for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) {
+          g.f[g.f_slot[k]] = 0.0;
+          g.f32[g.f_slot[k]] = 0.f;
+        }
       __syncthreads();
-      if (t + 1 < g.n_t)
+      if (t + 1 < g.n_t) {
         for (int64_t k = g.f_ptr[t + 1] + threadIdx.x; k < g.f_ptr[t + 2]; k += blockDim.x) g.f[g.f_slot[k]] += g.f_val[k];
+        __syncthreads();
+        for (int64_t k = g.f_ptr[t + 1] + threadIdx.x; k < g.f_ptr[t + 2]; k += blockDim.x)
+          g.f32[g.f_slot[k]] = (float)g.f[g.f_slot[k]];
+      }
     }
     if (threadIdx.x == 0) {
       *g.ticket = 0;
@@ -542,6 +550,8 @@ __global__ void k_batch_consts(int64_t n, const double* ml, float* ml32, float* 
 __global__ void k_batch_force0(Args g, int t) {
   if (!g.f_ptr || t < 0 || t >= g.n_t) return;
   for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f[g.f_slot[k]] += g.f_val[k];
+  __syncthreads();
+  for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f32[g.f_slot[k]] = (float)g.f[g.f_slot[k]];
 }
 
 __global__ void k_set_int(int* p, int v) { *p = v; }
@@ -558,6 +568,7 @@ struct sc_batch {
   float *w[2] = {nullptr, nullptr}, *vf[2] = {nullptr, nullptr};
   int* rec_map = nullptr;
   double* f = nullptr;
+  float* f32 = nullptr;
   int* t = nullptr;
   unsigned* ticket = nullptr;
   float2 *u2 = nullptr, *v2 = nullptr;
@@ -768,6 +779,7 @@ extern "C" int sc_batch_create(sc_batch** out, const sc_batch_desc* d, double* u
     if (rc) break;
     if ((rc = check(cudaMallocAsync((void**)&h->rec_map, 4 * ns, st), "malloc"))) break;
     if ((rc = check(cudaMallocAsync((void**)&h->f, 8 * ns, st), "malloc"))) break;
+    if ((rc = check(cudaMallocAsync((void**)&h->f32, 4 * ns, st), "malloc"))) break;
     if ((rc = check(cudaMallocAsync((void**)&h->t, sizeof(int), st), "malloc"))) break;
     if ((rc = check(cudaMallocAsync((void**)&h->ticket, sizeof(unsigned), st), "malloc"))) break;
     if ((rc = check(cudaMallocAsync((void**)&h->u2, 8 * nsr, st), "malloc"))) break;
@@ -793,9 +805,11 @@ extern "C" int sc_batch_create(sc_batch** out, const sc_batch_desc* d, double* u
     h->g.beta32 = (float)d->beta;
     cudaMemsetAsync(h->rec_map, 0xff, 4 * ns, st);
     cudaMemsetAsync(h->f, 0, 8 * ns, st);
+    cudaMemsetAsync(h->f32, 0, 4 * ns, st);
     cudaMemsetAsync(h->t, 0, sizeof(int), st);
     cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), st);
     h->g.f = h->f;
+    h->g.f32 = h->f32;
     h->g.t = h->t;
     h->g.ticket = h->ticket;
     h->g.rec_map = h->rec_map;
@@ -909,6 +923,7 @@ extern "C" int sc_batch_run(sc_batch* h, int t_begin, int t_end) {
   k_batch_init<<<grid_for((int64_t)h->g.d.n_nodes * 3 * h->g.d.R, 256, 152 * 32), 256, 0, st>>>(h->g, h->w[0],
                                                                                                  h->vf[0]);
   cudaMemsetAsync(h->f, 0, 8 * (int64_t)h->g.d.n_nodes * 3, st);
+  cudaMemsetAsync(h->f32, 0, 4 * (int64_t)h->g.d.n_nodes * 3, st);
   k_batch_force0<<<1, 256, 0, st>>>(h->g, t_begin);
   k_set_int<<<1, 1, 0, st>>>(h->t, t_begin);
   if ((rc = check_launch("batch prepare"))) return rc;
@@ -929,6 +944,7 @@ extern "C" int sc_batch_destroy(sc_batch* h) {
   }
   if (h->rec_map) cudaFree(h->rec_map);
   if (h->f) cudaFree(h->f);
+  if (h->f32) cudaFree(h->f32);
   if (h->t) cudaFree(h->t);
   if (h->ticket) cudaFree(h->ticket);
   void* more[] = {h->u2, h->v2, h->ml32, h->iml32, h->vneed};
