@@ -259,7 +259,7 @@ def run_gb300(args):
                       "n_eq": n, "nnz": nnz, "elements": int(len(model.elem)), "receivers": len(rec_eq),
                       "parallelism": f"replicas x{ws}",
                       "l2": "inputs larger than L2 (CSR values+cols 5.1 GB), no flush",
-                      "solver": "Newmark beta=1/4 gamma=1/2; per step PCG (FSAI preconditioner, FP32 factor), "
+                      "solver": "Newmark beta=1/4 gamma=1/2; per step PCG (FSAI preconditioner, FP16 factor), "
                                 "quadratic warm start, rtol 1e-12; node-block operator, SpMV products in FP32 "
                                 "pairs, residual, dot products and state FP64"},
            "cg_iters_per_step": iters / K_steps, "cg_iters_max": it_max,

@@ -202,7 +202,8 @@ int sc_rf_lognormal(int n_pts, const float* xyz, int R, int n_modes, const float
  * as one scalar per node pair, and Rayleigh damping C = Cabs + alpha M + beta K with the
  * Lysmer dashpots Cabs as a small slot-space CSR (scatter/system_matrix.py:166-198,375).
  * Each step solves A x = f - C vp - K up by PCG preconditioned with a factorised sparse
- * approximate inverse G^T G of A (FP32 factor on the lower node pattern, built on the GPU),
+ * approximate inverse G^T G of A (factor on the lower node pattern, built on the GPU in FP32 and
+ * applied from FP16 planes scaled by a power of two),
  * warm-started from the quadratic extrapolation of the acceleration history, to
  * ||r|| <= rtol ||rhs||.  eqmap [n_nodes][dim] (-1 fixed); rowptr/cols/K/M/C the eq-space
  * CSR from sc_csr_pattern + sc_assemble_values (+ Lysmer / Rayleigh); cab_* the Lysmer

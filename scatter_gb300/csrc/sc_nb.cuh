@@ -5,6 +5,8 @@
 #include <math.h>
 #include <stdlib.h>
 
+#include <cuda_fp16.h>
+
 #include "sc_common.cuh"
 
 namespace sc {
@@ -43,7 +45,7 @@ struct Args {
   const int *sf_col, *sl_col, *su_col;
   int64_t sf_n, sl_n, su_n;
   const double *KS, *AS, *MSS;
-  const float *GS, *GTS;
+  const __half *GS, *GTS;  // FSAI factor planes, FP16, scaled by a power of two (max |entry| in [0.5, 1))
   const float2* APS;       // A as FP32 (hi, lo) pairs (hi + lo = A to 48 bits) for the pair-arithmetic SpMV
   const float2* KPS;       // K as FP32 pairs, for the explicit step and the adjoint (built on first use)
   float2* p2;              // p as (hi, lo) FP32 pairs, written with p
@@ -137,6 +139,13 @@ __device__ __forceinline__ void ld4(const float* p, float (&v)[4], int keep) {
   const float4* q = reinterpret_cast<const float4*>(p);
   const float4 a = keep ? __ldg(q) : __ldcs(q);
   v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void ld4(const __half* p, float (&v)[4], int keep) {
+  const uint2* q = reinterpret_cast<const uint2*>(p);
+  const uint2 a = keep ? __ldg(q) : __ldcs(q);
+  const float2 lo = __half22float2(*reinterpret_cast<const __half2*>(&a.x));
+  const float2 hi = __half22float2(*reinterpret_cast<const __half2*>(&a.y));
+  v[0] = lo.x; v[1] = lo.y; v[2] = hi.x; v[3] = hi.y;
 }
 __device__ __forceinline__ void ld4(const float2* p, float2 (&v)[4], int keep) {
   const float4* q = reinterpret_cast<const float4*>(p);

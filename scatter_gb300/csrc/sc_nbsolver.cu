@@ -20,6 +20,7 @@
 // Kernels: one warp per node row (lanes over the row's blocks) for every block product;
 // per-block partial sums reduced by the last block (ticket, fixed order, no spin-waits);
 // one CUDA graph per step with a device-side WHILE conditional around the PCG body.
+#include <string.h>
 #include <math.h>
 #include <stdlib.h>
 
@@ -181,7 +182,7 @@ __global__ void __launch_bounds__(kThreads) k_residual(Args g) {
   }
 }
 
-// t = G r  (lower pattern, FP32 factor, FP32 result)
+// t = G r  (lower pattern, FP16 factor planes, FP32 products and result)
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_prec_lower(Args g) {
   SELL_ROW_LOOP(g.sl_ptr) {
@@ -774,6 +775,30 @@ __global__ void k_sell_permute(int planes, int64_t n_out, int64_t n_in, const in
   }
 }
 
+// FSAI planes: permuted into the sliced-ELL order and rounded to FP16 after scaling by a
+// power of two (CG is invariant under scaling the preconditioner; the power of two keeps the
+// iterates' bits and keeps every entry inside FP16's range whatever the units)
+__global__ void k_sell_permute_half(int planes, int64_t n_out, int64_t n_in, const int64_t* src, const float* in,
+                                    __half* out, float scale) {
+  for (int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < n_out;
+       pos += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = src[pos];
+    for (int c = 0; c < planes; ++c)
+      out[(int64_t)c * n_out + pos] = __float2half_rn(k >= 0 ? scale * in[(int64_t)c * n_in + k] : 0.f);
+  }
+}
+
+// largest |x| (as the bits of a non-negative float, which order like the values)
+__global__ void k_absmax_bits(int64_t n, const float* __restrict__ x, unsigned* out) {
+  unsigned m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float a = fabsf(x[i]);
+    if (a <= 3.0e38f) m = max(m, __float_as_uint(a));  // finite values only
+  }
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
 __global__ void k_init_scal(Scal* s, double tol2, int max_it) {
   s->rz = s->pw = s->rr = s->bb = s->alpha = s->beta = 0.0;
   s->tol2 = tol2;
@@ -888,7 +913,7 @@ void drop_graph(sc_nb_newmark* h) {
 // Sliced-ELL copies of K, A, M (full pattern), G (lower) and G^T (upper) for the per-step
 // kernels; allocated here (setup) from the stream-ordered pool and freed by sc_nb_destroy.
 static int build_sell(sc_nb_newmark* h, const double* KB, const double* AB, const double* MS, const float* GB,
-                      const float* GTB) {
+                      const float* GTB, float gscale) {
   Args& g = h->g;
   cudaStream_t st = h->user;
   const int D2 = g.D * g.D;
@@ -931,9 +956,9 @@ static int build_sell(sc_nb_newmark* h, const double* KB, const double* AB, cons
       g.sf_ptr = ptr; g.sf_col = col; g.sf_n = total; g.KS = ks; g.AS = as; g.MSS = ms;
       g.APS = ap;
     } else {
-      float* gs = nullptr;
-      if ((rc = alloc((void**)&gs, 4 * D2 * total))) break;
-      k_sell_permute<float><<<pb, 256, 0, st>>>(D2, total, g.nnzb, src, kind == 1 ? GB : GTB, gs);
+      __half* gs = nullptr;
+      if ((rc = alloc((void**)&gs, 2 * D2 * total))) break;
+      k_sell_permute_half<<<pb, 256, 0, st>>>(D2, total, g.nnzb, src, kind == 1 ? GB : GTB, gs, gscale);
       if (kind == 1) { g.sl_ptr = ptr; g.sl_col = col; g.sl_n = total; g.GS = gs; }
       else { g.su_ptr = ptr; g.su_col = col; g.su_n = total; g.GTS = gs; }
     }
@@ -1060,8 +1085,8 @@ extern "C" int sc_nb_create(sc_nb_newmark** out, int n_nodes, int dim, const int
   do {
     if ((rc = check(cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking), "stream"))) break;
     if ((rc = check(cudaStreamCreateWithFlags(&h->cap2, cudaStreamNonBlocking), "stream"))) break;
-    if ((rc = check(cudaMallocAsync((void**)&dflag, 2 * sizeof(int), st), "malloc"))) break;
-    cudaMemsetAsync(dflag, 0, 2 * sizeof(int), st);
+    if ((rc = check(cudaMallocAsync((void**)&dflag, 3 * sizeof(int), st), "malloc"))) break;
+    cudaMemsetAsync(dflag, 0, 3 * sizeof(int), st);
     cudaMemsetAsync(g.f, 0, 8 * ns, st);
     cudaMemsetAsync(g.a1, 0, 8 * ns, st);
     cudaMemsetAsync(g.a2, 0, 8 * ns, st);
@@ -1080,8 +1105,18 @@ extern "C" int sc_nb_create(sc_nb_newmark** out, int n_nodes, int dim, const int
       k_transpose_g<2><<<h->node_blocks, kThreads, 0, st>>>(g, GB, GTB);
     }
     k_init_scal<<<1, 1, 0, st>>>(g.s, rtol * rtol, max_iter);
+    k_absmax_bits<<<grid_for((int64_t)D2 * nnzb, 256, 152 * 8), 256, 0, st>>>((int64_t)D2 * nnzb, GB,
+                                                                               (unsigned*)(dflag + 2));
     if ((rc = check_launch("nb setup"))) break;
-    if ((rc = build_sell(h, KB, AB, MS, GB, GTB))) break;
+    unsigned gmax_bits = 0;
+    if ((rc = check(cudaMemcpyAsync(&gmax_bits, dflag + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "memcpy")))
+      break;
+    if ((rc = check(cudaStreamSynchronize(st), "sync"))) break;
+    float gmax = 0.f;
+    memcpy(&gmax, &gmax_bits, sizeof(float));
+    // the power of two that brings the largest FSAI entry into [0.5, 1)
+    const float gscale = gmax > 0.f ? ldexpf(1.f, -(ilogbf(gmax) + 1)) : 1.f;
+    if ((rc = build_sell(h, KB, AB, MS, GB, GTB, gscale))) break;
     int hf[2] = {0, 0};
     if ((rc = check(cudaMemcpyAsync(hf, dflag, 2 * sizeof(int), cudaMemcpyDeviceToHost, st), "memcpy"))) break;
     if ((rc = check(cudaStreamSynchronize(st), "sync"))) break;

@@ -68,7 +68,7 @@ def test_node_block_operators(cuda, kind, name):
         assert rel_l2(s.apply("Cabs", x), Cabs @ x) <= 1e-13
         # Rayleigh structure used by the residual: C = Cabs + alpha M + beta K
         assert rel_l2(Cabs @ x + g.alpha * (M @ x) + g.beta * (K @ x), C @ x) <= 1e-12
-    # preconditioner: symmetric positive definite (FP32 factor)
+    # preconditioner: symmetric positive definite (FP16 factor planes, FP32 products)
     z = rng.standard_normal(g.n_eq)
     Px, Pz = s.apply("P", x), s.apply("P", z)
     assert abs(z @ Px - x @ Pz) <= 1e-5 * abs(x @ Px)
