@@ -172,7 +172,7 @@ def run_gb300(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from scatter_gb300 import _native
+    from scatter_gb300 import _native, replicas
     from scatter_gb300.solvers import NodeBlockNewmark
     from scatter_gb300.system_matrix import GenerateMatrix
 
@@ -204,8 +204,7 @@ def run_gb300(args):
     solver.run(0, W)
     rc, it_w, _ = solver.status()
     torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -214,18 +213,15 @@ def run_gb300(args):
         solver.run(W, W + K_steps)
         e1.record()
         torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     ms = e0.elapsed_time(e1)
     rc, it_all, it_max = solver.status()
     if rc != 0:
         raise SystemExit(f"solver status {rc} during the timed region")
     iters = it_all - it_w
-    if ws > 1:
-        tt = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
-    value = ws * n * K_steps / (ms / 1e3)
+    # every rank advances its own replica: the job's rate is all ranks' DOF-steps over the
+    # longest rank's time
+    ms, value = replicas.job_rate(ms, n * K_steps, device="cuda")
 
     # dominant kernel: the PCG block SpMV, timed standalone on the solver's stream
     ms_spmv, bytes_spmv = solver.time_spmv(20)
