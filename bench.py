@@ -381,6 +381,7 @@ def batched_run(k, w, R=256):
     s = NodeBlockNewmark(g, DT, precond="jacobi")
     s.set_force(table)
     s.set_output(1, rec_eq, n_t, what=("v",))
+    single_tpr, _ = s.tune_explicit()  # the single solve at its own best shape
     s.run_explicit(0, w)
     torch.cuda.synchronize()
     e0, e1 = _events()
@@ -401,7 +402,8 @@ def batched_run(k, w, R=256):
                             "incidence lists (k_batch_step)", "realisations_per_thread": rpt,
                             "threads_per_block": tpb, "tuned_ms": tuned_ms},
             "workload": "256 log-normal E realisations, box 40x20x10 m hexa8 0.5 m, Lysmer, Ricker 20 Hz, dt 5e-5",
-            "single": "plain FP64 explicit GPU path (node-block graph), realisation 0, same steps"}
+            "single": "plain FP64-class explicit GPU path (node-block graph, threads per row tuned: "
+                      f"{single_tpr}), realisation 0, same steps"}
 
 
 def ragged_run(k, w, n_meshes=64, seed=4, hexa_edges=(10, 80), tetra_edges=(5, 40)):
@@ -640,19 +642,24 @@ def run_reference(args):
 
     s = cpu.NewmarkCPU(M, C, K, DT)
     budget = args.cpu_seconds
+    # untimed warm-up: the requested W steps, within half the time budget (at least one)
     t1 = time.perf_counter()
     s.run(0, 1, table.f_ptr, table.f_eq, table.f_val, rec_eq)
     one = time.perf_counter() - t1
+    w_steps = int(max(1, min(args.warmup, budget / 2 / max(one, 1e-6))))
+    if w_steps > 1:
+        s.run(1, w_steps - 1, table.f_ptr, table.f_eq, table.f_val, rec_eq)  # (first step, step count)
     steps = int(max(2, min(args.steps, budget / max(one, 1e-6))))
     t1 = time.perf_counter()
-    s.run(1, steps, table.f_ptr, table.f_eq, table.f_val, rec_eq)
+    s.run(w_steps, steps, table.f_ptr, table.f_eq, table.f_val, rec_eq)
     el_s = time.perf_counter() - t1
     value = n * steps / el_s
     cb = {"value": value, "unit": "DOF-steps/s", "cores": cpu.threads(), "kind": "port",
-          "sample": f"{steps} Newmark steps (1..{steps}) of the same workload from rest; oracle numpy assembly "
+          "sample": f"{steps} Newmark steps ({w_steps}..{w_steps + steps - 1}) of the same workload after {w_steps} "
+                    f"untimed steps from rest; oracle numpy assembly "
                     f"({setup:.0f} s, untimed) + C Jacobi-PCG loop on {cpu.threads()} threads, {el_s:.1f} s"}
     print(json.dumps({"metric": METRIC, "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": steps,
-                      "warmup": 1, "ms_per_step": el_s / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+                      "warmup": w_steps, "ms_per_step": el_s / steps * 1e3, "higher_is_better": True, "scaling": "weak",
                       "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded structured mesh)",
                       "config": {"workload": "plain Newmark FP64, box 60x40x30 m hexa8 0.5 m (120x80x60 el), "
                                              "2 layers, Lysmer sides+base, moving 100 kN at 40 km/h, dt 5e-5",
