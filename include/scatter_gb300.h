@@ -218,6 +218,14 @@ int sc_nb_create(sc_nb_newmark** h, int n_nodes, int dim, const int* eqmap, cons
                  const double* C, int64_t n_cab, const int64_t* cab_ptr, const int* cab_col, const double* cab_val,
                  double alpha, double beta, double dt, double rtol, int max_iter, int precond, double* u, double* v,
                  double* a, void* workspace, int64_t workspace_bytes, void* stream);
+/* Warm start of each Newmark step (no reference counterpart): the PCG starts from the
+ * polynomial extrapolation of order p of the previous accelerations,
+ * x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k} (p = 2: 3 a_n - 3 a_{n-1} + a_{n-2}).  order 1..8
+ * fixes p; 0 (the default) adapts it on the device: starting from 2 it moves to a neighbouring
+ * order while the mean PCG iterations over windows of 16 steps fall, steps back when they
+ * rise, and holds 8 windows before probing again.  The order changes the iteration count,
+ * not the answer, which meets the same tolerance. */
+int sc_nb_set_predictor(sc_nb_newmark* h, int order);
 /* options bit 0: run the PCG SpMV in FP64 instead of the default FP32-pair arithmetic
  * (A as hi + lo FP32 pairs, exact TwoProd/TwoSum accumulation, ~2^-46 relative per product;
  * the residual, dot products and state stay FP64).  bit 1: run the explicit scheme in FP64

@@ -14,15 +14,22 @@ namespace nb {
 
 constexpr int kThreads = 256;
 constexpr int kMaxFsai = 64;  // FSAI row pattern capacity (slots); larger rows fall back to Jacobi
+constexpr int kHistMax = 8;   // acceleration history kept for the warm start
+// warm-start order control (pred_order 0 = adaptive): start at kPredStart, then compare the
+// mean PCG iterations of windows of kPredWin steps, keep climbing while a probed neighbour
+// order is better, step back when it is worse and hold there kPredHold windows
+constexpr int kPredStart = 2, kPredWin = 16, kPredHold = 8;
 
 struct Scal {
   double rz, pw, rr, bb, alpha, beta, tol2, pad0;
   long long total_iters;
   int it, max_it, max_seen, status, t, fsai_fallback;
   unsigned int ticket;
-  int hist;  // valid previous accelerations (0..2) for the warm start
+  int hist;  // valid previous accelerations (0..kHistMax) for the warm start
   int done;  // eager mode: set when the PCG loop should stop
-  unsigned int pad2[1];
+  // adaptive warm-start order: current order, probing direction, window and hold counters
+  int pord, pdir, win_n, win_it, probing, hold;
+  double ref_avg;  // mean iterations per step of the reference window
 };
 
 struct Args {
@@ -55,7 +62,9 @@ struct Args {
   double alpha_r, beta_r;  // Rayleigh coefficients
   double aM, aK, aC;       // A = aM M + aK K + aC Cabs
   double dt;
-  double *u, *v, *a, *a1, *a2;
+  double *u, *v, *a;
+  double* ah[kHistMax];  // previous accelerations a_{n-1} .. a_{n-kHistMax} (ah[0] most recent)
+  int pred_order;        // order of the warm start's extrapolation (1..kHistMax), 0: adaptive (Scal::pord)
   double *q1, *q2, *y1, *x0, *x, *r, *z, *p, *w, *f;
   float* t32;
   float* r32;  // FP32 copy of r, written with r: the lower FSAI half gathers it (no FP64 conversion per gather)

@@ -14,7 +14,9 @@
 //   b  = f - C vp - K up = f - K q1 - M q2 - Cabs y1
 //   q1 = up + beta y1, q2 = alpha y1, y1 = vp (+ the usual predictor terms, see k_predict)
 // Each step solves A x = b for the new acceleration by PCG with preconditioner G^T G,
-// warm-started from the quadratic extrapolation 3a_n - 3a_{n-1} + a_{n-2}, stopped at
+// warm-started from the polynomial extrapolation of the accelerations of order p
+// (x0 = sum_k (-1)^k C(p+1, k+1) a_{n-k}, e.g. 3a_n - 3a_{n-1} + a_{n-2} for p = 2; p is
+// fixed by the caller or, by default, adapted to the iteration counts, see k_advance), stopped at
 // ||r|| <= rtol ||b||; then u, v, a are updated exactly as the reference's update.
 //
 // Kernels: one warp per node row (lanes over the row's blocks) for every block product;
@@ -60,9 +62,16 @@ __global__ void k_predict(Args g) {
     g.q1[i] = up + g.beta_r * vp;
     g.q2[i] = g.alpha_r * vp;
     g.y1[i] = vp;
-    double x0 = ai;
-    if (hist >= 2) x0 = 3.0 * ai - 3.0 * g.a1[i] + g.a2[i];
-    else if (hist == 1) x0 = 2.0 * ai - g.a1[i];
+    // x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k}, p = min(history, order); the binomial
+    // coefficients are exact in FP64 and the terms are summed in a fixed order
+    const int ord = g.pred_order > 0 ? g.pred_order : g.s->pord;
+    const int p = hist < ord ? hist : ord;
+    double x0 = (p + 1) * ai;
+    double cb = p + 1;  // C(p+1, k+1)
+    for (int k = 1; k <= p; ++k) {
+      cb = cb * (p + 1 - k) / (k + 1);
+      x0 += ((k & 1) ? -cb : cb) * g.ah[k - 1][i];
+    }
     if (g.fixed[i]) x0 = 0.0;
     g.x0[i] = x0;
     if (g.spmv_pair) g.p2[i] = split_pair(x0);  // p2 is scratch until p is first written
@@ -489,14 +498,17 @@ __global__ void k_direction(Args g) {
 // u = up + dt^2/4 x ; v = vp + dt/2 x ; shift the acceleration history ; record ; t += 1
 __global__ void k_finalize(Args g) {
   const double dt = g.dt, h = 0.5 * dt, qq = 0.25 * dt * dt;
+  // history kept: the fixed order's entries, or one beyond the adaptive order (it moves by
+  // at most one per window)
+  const int depth = g.pred_order > 0 ? g.pred_order : min(kHistMax, g.s->pord + 1);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
     const double x = g.x[i], ai = g.a[i], vi = g.v[i];
     const double up = g.u[i] + dt * vi + qq * ai;
     const double vp = vi + h * ai;
     g.u[i] = fma(qq, x, up);
     g.v[i] = fma(h, x, vp);
-    g.a2[i] = g.a1[i];
-    g.a1[i] = ai;
+    for (int k = depth - 1; k > 0; --k) g.ah[k][i] = g.ah[k - 1][i];
+    g.ah[0][i] = ai;
     g.a[i] = x;
   }
 }
@@ -516,13 +528,54 @@ __global__ void k_record(Args g) {
   }
 }
 
+__global__ void k_cap_hist(Scal* s, int n) {
+  if (s->hist > n) s->hist = n;
+}
+
 __global__ void k_advance(Args g) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     Scal* s = g.s;
     s->total_iters += s->it;
     if (s->it > s->max_seen) s->max_seen = s->it;
     s->t += 1;
-    if (s->hist < 2) s->hist += 1;
+    if (s->hist < kHistMax) s->hist += 1;
+    if (g.pred_order == 0 && ++s->win_n == kPredWin) {
+      // adaptive warm-start order, from the mean iterations of the window just ended
+      const double avg = (double)(s->win_it + s->it) / kPredWin;
+      s->win_n = 0;
+      s->win_it = 0;
+      if (s->probing) {
+        if (avg <= s->ref_avg) {  // the probed order is no worse: keep it, probe further
+          s->ref_avg = avg;
+          const int np = s->pord + s->pdir;
+          if (np >= 1 && np <= kHistMax) {
+            s->pord = np;
+          } else {
+            s->probing = 0;
+            s->pdir = -s->pdir;
+            s->hold = kPredHold;
+          }
+        } else {  // worse: back to the better order, hold, probe the other side next
+          s->pord -= s->pdir;
+          s->pdir = -s->pdir;
+          s->probing = 0;
+          s->hold = kPredHold;
+        }
+      } else if (s->hold > 0) {
+        s->hold -= 1;
+      } else {  // this window is the reference: probe the neighbour in the current direction
+        s->ref_avg = avg;
+        const int np = s->pord + s->pdir;
+        if (np >= 1 && np <= kHistMax) {
+          s->pord = np;
+          s->probing = 1;
+        } else {
+          s->pdir = -s->pdir;
+        }
+      }
+    } else if (g.pred_order == 0) {
+      s->win_it += s->it;
+    }
   }
 }
 
@@ -811,6 +864,10 @@ __global__ void k_init_scal(Scal* s, double tol2, int max_it) {
   s->fsai_fallback = 0;
   s->ticket = 0;
   s->hist = 0;
+  s->pord = kPredStart;
+  s->pdir = 1;
+  s->win_n = s->win_it = s->probing = s->hold = 0;
+  s->ref_avg = 0.0;
 }
 
 }  // namespace nb
@@ -991,7 +1048,7 @@ extern "C" int64_t sc_nb_workspace_bytes(int n_nodes, int dim, int64_t nnzb) {
   b += 2 * align256(8 * D2 * nnzb);           // KB, AB
   b += align256(8 * nnzb);                    // MS
   b += 2 * align256(4 * D2 * nnzb);           // GB, GTB
-  b += 13 * align256(8 * ns);                 // a1 a2 q1 q2 y1 x0 x r z p w f (+1 spare)
+  b += (kHistMax + 11) * align256(8 * ns);    // history ah[kHistMax], q1 q2 y1 x0 x r z p w f, p2
   b += 2 * align256(4 * ns);                  // t32, r32
   b += align256(8 * 4 * 152 * 16);            // partials
   b += align256(sizeof(Scal));
@@ -1054,8 +1111,8 @@ extern "C" int sc_nb_create(sc_nb_newmark** out, int n_nodes, int dim, const int
   g.MS = MS;
   g.GB = GB;
   g.GTB = GTB;
-  g.a1 = (double*)take(8 * ns);
-  g.a2 = (double*)take(8 * ns);
+  for (int k = 0; k < kHistMax; ++k) g.ah[k] = (double*)take(8 * ns);
+  g.pred_order = 0;  // adaptive
   g.q1 = (double*)take(8 * ns);
   g.q2 = (double*)take(8 * ns);
   g.y1 = (double*)take(8 * ns);
@@ -1088,8 +1145,7 @@ extern "C" int sc_nb_create(sc_nb_newmark** out, int n_nodes, int dim, const int
     if ((rc = check(cudaMallocAsync((void**)&dflag, 3 * sizeof(int), st), "malloc"))) break;
     cudaMemsetAsync(dflag, 0, 3 * sizeof(int), st);
     cudaMemsetAsync(g.f, 0, 8 * ns, st);
-    cudaMemsetAsync(g.a1, 0, 8 * ns, st);
-    cudaMemsetAsync(g.a2, 0, 8 * ns, st);
+    for (int k = 0; k < kHistMax; ++k) cudaMemsetAsync(g.ah[k], 0, 8 * ns, st);
     cudaMemsetAsync(GB, 0, 4 * D2 * nnzb, st);
     k_setup_nodes<<<grid_for(n_nodes, 128), 128, 0, st>>>(n_nodes, dim, eqmap, adj_ptr, adj, diag, fixed, dflag);
     if (dim == 3)
@@ -1140,6 +1196,18 @@ extern "C" int sc_nb_create(sc_nb_newmark** out, int n_nodes, int dim, const int
   return SC_OK;
 }
 
+// Polynomial order (1..kHistMax; 0: adaptive, the default) of the extrapolated accelerations
+// that start each step's PCG: it changes the iteration count, not the converged answer.
+extern "C" int sc_nb_set_predictor(sc_nb_newmark* h, int order) {
+  if (!h || order < 0 || order > kHistMax) return SC_BAD_ARG;
+  // only the previous fixed order's entries of the history are current (adaptive keeps all)
+  if (h->g.pred_order > 0 && (order == 0 || order > h->g.pred_order))
+    k_cap_hist<<<1, 1, 0, h->user>>>(h->g.s, h->g.pred_order);
+  h->g.pred_order = order;
+  drop_graph(h);
+  return check_launch("predictor order");
+}
+
 extern "C" int sc_nb_set_options(sc_nb_newmark* h, int options) {
   if (!h) return SC_BAD_ARG;
   h->g.spmv_pair = (options & 1) ? 0 : 1;
@@ -1180,7 +1248,7 @@ extern "C" int sc_nb_set_output(sc_nb_newmark* h, int out_interval, int n_rec, c
 
 // t_begin: state index of u/v/a on entry (the force entries of step t_begin are assumed in f
 // when t_begin > 0; at t_begin == 0 they are written here).  The warm start uses the
-// acceleration history (a1, a2) once steps of this solver have filled it.
+// acceleration history once steps of this solver have filled it.
 // One step with eager launches (no graph): the same kernels, the PCG loop driven by the host
 // reading Scal::done after each iteration.  Used for profiling (kernels inside graphs with
 // conditional nodes cannot be captured by the profiler); selected by SCATTER_GB300_EAGER=1.

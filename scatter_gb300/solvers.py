@@ -204,6 +204,11 @@ class NodeBlockNewmark:
         # bit 0: PCG SpMV in FP64 instead of FP32 pairs; bit 1: explicit K w in FP64
         nat.call("sc_nb_set_options", self.h, {"pair": 0, "fp64": 1}[spmv] | {"pair": 0, "fp64": 2}[explicit])
 
+    def set_predictor(self, order):
+        """Order (1..8) of the extrapolated accelerations each step's PCG starts from; 0 (the
+        default) adapts the order to the iteration counts."""
+        nat.call("sc_nb_set_predictor", self.h, int(order))
+
     def set_force(self, table: ForceTable):
         eq = dv.to_dev(table.f_eq, torch.int64)
         slot = self.eq2slot[eq].to(torch.int32) if eq.numel() else eq.to(torch.int32)
