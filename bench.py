@@ -256,7 +256,7 @@ def run_gb300(args):
                       "parallelism": f"replicas x{ws}",
                       "l2": "inputs larger than L2 (CSR values+cols 5.1 GB), no flush",
                       "solver": "Newmark beta=1/4 gamma=1/2; per step PCG (FSAI preconditioner, FP16 factor), "
-                                "quadratic warm start, rtol 1e-12; node-block operator, SpMV products in FP32 "
+                                "warm start extrapolating the accelerations, order adapted on the device, rtol 1e-12; node-block operator, SpMV products in FP32 "
                                 "pairs, residual, dot products and state FP64"},
            "cg_iters_per_step": iters / K_steps, "cg_iters_max": it_max,
            "setup_s": {"host_mesh_and_loads": round(t_host, 2), "gpu_assembly_lysmer_rayleigh": round(t_assembly, 3),

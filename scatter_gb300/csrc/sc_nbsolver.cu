@@ -55,6 +55,20 @@ __global__ void k_force(Args g) {
 __global__ void k_predict(Args g) {
   const double dt = g.dt, h = 0.5 * dt, qq = 0.25 * dt * dt;
   const int hist = g.s->hist;
+  // warm-start order p = min(history, order) and its coefficients (-1)^k C(p+1, k+1), exact
+  // integers, computed once per thread
+  const int ord = g.pred_order > 0 ? g.pred_order : g.s->pord;
+  const int p = hist < ord ? hist : ord;
+  double cf[kHistMax + 1];
+  {
+    long long c = p + 1;
+    cf[0] = (double)c;
+#pragma unroll
+    for (int k = 1; k <= kHistMax; ++k) {
+      if (k <= p) c = c * (p + 1 - k) / (k + 1);
+      cf[k] = k <= p ? ((k & 1) ? -(double)c : (double)c) : 0.0;
+    }
+  }
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
     const double ai = g.a[i], vi = g.v[i];
     const double vp = vi + h * ai;
@@ -62,16 +76,11 @@ __global__ void k_predict(Args g) {
     g.q1[i] = up + g.beta_r * vp;
     g.q2[i] = g.alpha_r * vp;
     g.y1[i] = vp;
-    // x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k}, p = min(history, order); the binomial
-    // coefficients are exact in FP64 and the terms are summed in a fixed order
-    const int ord = g.pred_order > 0 ? g.pred_order : g.s->pord;
-    const int p = hist < ord ? hist : ord;
-    double x0 = (p + 1) * ai;
-    double cb = p + 1;  // C(p+1, k+1)
-    for (int k = 1; k <= p; ++k) {
-      cb = cb * (p + 1 - k) / (k + 1);
-      x0 += ((k & 1) ? -cb : cb) * g.ah[k - 1][i];
-    }
+    // x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k}, terms summed in a fixed order
+    double x0 = cf[0] * ai;
+#pragma unroll
+    for (int k = 1; k <= kHistMax; ++k)
+      if (k <= p) x0 += cf[k] * g.ah[k - 1][i];
     if (g.fixed[i]) x0 = 0.0;
     g.x0[i] = x0;
     if (g.spmv_pair) g.p2[i] = split_pair(x0);  // p2 is scratch until p is first written
