@@ -99,3 +99,45 @@ def test_eager_mode_matches_graph_mode(cuda):
             os.environ.pop("SCATTER_GB300_EAGER", None)
     np.testing.assert_array_equal(outs[0][0], outs[1][0])
     assert outs[0][1] == outs[1][1]
+
+
+def test_warm_start_order_changes_iterations_not_the_answer(cuda):
+    """Fixed warm-start orders 1..8 and the adaptive default reach the same displacements
+    (the PCG tolerance), and the adaptive order needs fewer PCG iterations than order 2 on a
+    smooth load history."""
+    from scatter_gb300 import meshgen
+    from scatter_gb300.force_external import ricker_table
+    from scatter_gb300.solvers import NodeBlockNewmark
+    from scatter_gb300.system_matrix import GenerateMatrix
+
+    mats = {"lower": {"density": 2000.0, "Young": 150e6, "poisson": 0.25},
+            "upper": {"density": 1800.0, "Young": 30e6, "poisson": 0.3}}
+    m = meshgen.box_model(10, 6, 6, 0.5, layers=[(0.0, "lower"), (1.5, "upper")], bottom="020", x_faces="200",
+                          z_faces="002")
+    g = GenerateMatrix(m.number_eq, 2)
+    g.generate_stiffness_and_mass(m, mats)
+    g.absorbing_boundaries(m, mats, [1, 1], 1e3)
+    g.damping_Rayleigh([1, 0.02, 50, 0.02])
+    dt, n_t = 5e-5, 401
+    time = np.arange(n_t) * dt
+    top = m.top_nodes()
+    table = ricker_table(m, int(top[len(top) // 2]), -1e4, 40.0, 0.004, time)
+    rec = np.asarray([int(m.eq_nb_dof[m.node_index()[n], 1]) for n in top[::3]], dtype=np.int64)
+    runs = {}
+    for order in (0, 1, 2, 4, 6, 8):
+        s = NodeBlockNewmark(g, dt)
+        if order:
+            s.set_predictor(order)
+        s.set_force(table)
+        s.set_output(1, rec, n_t, what=("u",))
+        s.initial_acceleration()
+        s.run(0, n_t - 1)
+        rc, iters, _ = s.status()
+        assert rc == 0
+        runs[order] = (s.outputs()["u"].copy(), iters)
+        s.close()
+    ref = runs[2][0]
+    assert np.abs(ref).max() > 0
+    for order, (u, _) in runs.items():
+        assert rel_l2(u, ref) <= 1e-10, order
+    assert runs[0][1] < runs[2][1]
