@@ -540,10 +540,10 @@ def adjoint_run(n_steps=4000, checkpoint=200, n_fd=20):
             worst = max(worst, err)
             checks.append([kind, int(e), float(grad[e]), float(fd)])
     return {"adjoint_over_forward": ms_a / ms_f, "forward_ms": ms_f, "gradient_ms": ms_a,
-            "gradient_phases_ms": {"forward_with_checkpoints": phases[0], "recompute": phases[1],
-                                   "backward": phases[2], "reverse_sweep_wall": phases[3]},
-            "reverse_sweep": "recompute of segment s-1 on a second stream beside the backward of segment s; "
-                             "element gradients once per segment", "explicit_kernel_ms": kernel_ms, "misfit": J,
+            "gradient_phases_ms": {"forward_with_checkpoints": phases[0], "recompute_last_segment": phases[1],
+                                   "backward_with_recompute": phases[2], "reverse_sweep": phases[3]},
+            "reverse_sweep": "each backward step fused with a recompute step of the previous segment (one kernel "
+                             "per pair of steps); element gradients once per segment", "explicit_kernel_ms": kernel_ms, "misfit": J,
             "misfit_check": 0.5 * float(((v0[1:] - target[1:]) ** 2).sum()), "n_eq": int(m.number_eq),
             "elements": n_el, "steps": n_steps, "checkpoint": checkpoint, "fd_max_rel_err": worst, "fd_checks": len(checks),
             "timing": "forward: CUDA events around the explicit run; gradient: host wall clock around the whole "

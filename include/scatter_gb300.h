@@ -269,11 +269,11 @@ int sc_nb_time_explicit(sc_nb_newmark* h, int reps, float* ms_per_step);
  * force table), and dJ/dE_e, dJ/drho_e for per-element Young's modulus and density, with
  *   K = sum_e E_e K1_e + Lysmer springs, M_L = sum_e rho_e ml1_e, Lysmer dashpots ~ sqrt(rho_e E_e)
  * (the operators the handle was built from must be these at the given young/rho).  Forward
- * with FP32-pair checkpoints every `checkpoint` steps; per segment (last first) a recompute
- * on a second stream, overlapping the backward recursion of the segment after it; one CUDA
- * graph per recompute step and per backward step, and one element-gradient kernel per
- * segment; gradients accumulated per element in step order (deterministic, independent of
- * the checkpoint interval).  Descriptor fields:
+ * with FP32-pair checkpoints every `checkpoint` steps; the reverse sweep (last segment
+ * first) runs each backward step fused with a recompute step of the segment before it (one
+ * kernel per pair of steps) and one element-gradient kernel per segment, all on the handle's
+ * stream; gradients accumulated per element in step order (deterministic, independent of the
+ * checkpoint interval).  Descriptor fields:
  *   elem [n_elem][n_en] node indices; ke_type [n_elem] -> ke1 [types][3 n_en][3 n_en] FP32
  *   unit-E element stiffness; young, rho [n_elem]; ml1 [n_elem][n_en][3] FP32 unit lumped mass
  *   (free columns); l_eptr [n_elem+1], l_row, l_col (slots), l_c, l_s (FP32): the element's
@@ -282,8 +282,9 @@ int sc_nb_time_explicit(sc_nb_newmark* h, int reps, float* ms_per_step);
 typedef struct sc_adj_desc sc_adj_desc;
 int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* desc, double* J_host, double* grad_E, double* grad_rho);
 /* device time of the last sc_nb_adjoint call's phases, ms: [0] forward with checkpoints,
- * [1] recompute and [2] backward, each summed over the segments (they overlap on two
- * streams), [3] the wall time of the reverse sweep (from the end of the forward) */
+ * [1] recompute of the last segment (alone), [2] the rest of the reverse sweep (backward
+ * steps fused with the previous segment's recompute, element gradients), [3] the whole
+ * reverse sweep, [1] + [2] */
 int sc_nb_adjoint_timings(sc_nb_newmark* h, float* ms4);
 /* testing aid: y = Op x in slot space; which = 0: A, 1: K, 2: consistent mass, 3: the
  * preconditioner G^T G, 4: Lysmer dashpots.  Synchronous; call between steps. */

@@ -142,9 +142,9 @@ class _Prepared:
         return J.value, dv.host(gE), dv.host(gR)
 
     def timings(self):
-        """Device ms of the last gradient's phases: forward with checkpoints, recompute and
-        backward (each summed over the segments; the two overlap on two streams), and the wall
-        time of the reverse sweep."""
+        """Device ms of the last gradient's phases: forward with checkpoints, recompute of the
+        last segment, the rest of the reverse sweep (backward steps fused with the previous
+        segment's recompute, element gradients), and the whole reverse sweep."""
         ms = (ctypes.c_float * 4)()
         nat.call("sc_nb_adjoint_timings", self.solver.h, ms)
         return tuple(float(x) for x in ms)

@@ -721,6 +721,122 @@ __global__ void __launch_bounds__(kThreads) k_adj_rows(Args g, PairStep p, sc_ad
   }
 }
 
+// A recompute step of one segment and a backward step of the next one, fused: one pass over
+// the K pair planes serves K w (the explicit step n -> n+1 of the recompute, storing the
+// element gradient's inputs, recording no receivers) and K y (the backward rows of step nb).
+// Each half's arithmetic is that of k_explicit_pair / k_adj_rows, in the same order, so the
+// results are bitwise theirs.  The last block swaps the recompute's force entries and advances
+// both step counters.
+template <int D, int TPR>
+__global__ void __launch_bounds__(kThreads) k_adj_fused(Args g, PairStep p, SegStore st, sc_adj_desc d, AdjState a,
+                                                        int cur) {
+  const int step = g.s->t + 1;
+  const int64_t kn = (int64_t)(step - 1 - *st.t0) * g.n_s;
+  const int nb = *a.n_dev;
+  float* ys = a.ys + (int64_t)(nb - *a.seg_t0) * g.n_s;
+  const float2* y = cur ? a.y[1] : a.y[0];
+  float2* yn = cur ? a.y[0] : a.y[1];
+  const int sub = threadIdx.x % TPR;
+  SELL_ROW_LOOP_T(TPR) {
+    SELL_ROW_BEGIN(g.sf_ptr)
+    float hf[D], lf[D], hb[D], lb[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) hf[c] = lf[c] = hb[c] = lb[c] = 0.f;
+    for (int64_t q = sub; q < nq; q += TPR) {
+      const int64_t pos = p0 + 128 * q;
+      int cl[4];
+      cols4(g.sf_col, pos, cl, g.keep_l2);
+      float2 wa[4][D], ya[4][D];
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+#pragma unroll
+        for (int dd = 0; dd < D; ++dd) {
+          wa[e][dd] = p.w_in[(int64_t)cl[e] * D + dd];
+          ya[e][dd] = y[(int64_t)cl[e] * D + dd];
+        }
+#pragma unroll
+      for (int c = 0; c < D; ++c)
+#pragma unroll
+        for (int dd = 0; dd < D; ++dd) {
+          float2 k4[4];
+          ld4(g.KPS + (int64_t)(c * D + dd) * g.sf_n + pos, k4, g.keep_l2);
+#pragma unroll
+          for (int e = 0; e < 4; ++e) pair_fma(k4[e].x, k4[e].y, wa[e][dd], hf[c], lf[c]);
+#pragma unroll
+          for (int e = 0; e < 4; ++e) pair_fma(k4[e].x, k4[e].y, ya[e][dd], hb[c], lb[c]);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      group_pair_sum<TPR>(hf[c], lf[c]);
+      group_pair_sum<TPR>(hb[c], lb[c]);
+    }
+    if (row >= g.n_nodes) continue;
+    for (int c = (TPR >= D ? sub : 0); c < D; c += (TPR >= D ? D : 1)) {
+      if (TPR > 1 && TPR < D && c % TPR != sub) continue;
+      const int64_t i = row * D + c;
+      // recompute: the explicit step, storing the element gradient's inputs of state n
+      if (g.fixed[i]) {
+        p.v_out[i] = p.w_out[i] = make_float2(0.f, 0.f);
+        st.wp[kn + i] = make_float2(0.f, 0.f);
+        st.v32[kn + i] = st.a32[kn + i] = 0.f;
+      } else {
+        float2 cab = make_float2(0.f, 0.f);
+        for (int64_t k = g.cab_ptr[i]; k < g.cab_ptr[i + 1]; ++k) cab = p_add(cab, p_mul(p.cab[k], p.v_in[g.cab_col[k]]));
+        const float2 vi = p.v_in[i];
+        const float2 kw = p_renorm(pick<D>(hf, c), pick<D>(lf, c));
+        const float2 num = p_sub(p_sub(p_sub(p.f[i], kw), p_mul(p.aml[i], vi)), cab);
+        const float2 acc = p_mul(num, p.iml[i]);
+        const float2 vn = p_add(vi, p_mul(p.dt, acc));
+        const float2 un = p_add(p.u[i], p_mul(p.dt, vn));
+        p.v_out[i] = vn;
+        p.u[i] = un;
+        p.w_out[i] = w_of(un, vn, p.beta);
+        st.wp[kn + i] = p.w_in[i];
+        st.v32[kn + i] = vi.x;
+        st.a32[kn + i] = acc.x;
+      }
+      // backward rows of step nb
+      const float2 yi = y[i];
+      ys[i] = __fadd_rn(yi.x, yi.y);
+      if (g.fixed[i]) {
+        a.mu_u[i] = a.mu_v[i] = yn[i] = make_float2(0.f, 0.f);
+        continue;
+      }
+      const float2 ky = p_renorm(pick<D>(hb, c), pick<D>(lb, c));
+      float2 cy = make_float2(0.f, 0.f);
+      for (int64_t q = g.cab_ptr[i]; q < g.cab_ptr[i + 1]; ++q) cy = p_add(cy, p_mul(p.cab[q], y[g.cab_col[q]]));
+      const float2 mu_u = a.mu_u[i], mu_v = a.mu_v[i];
+      const float2 gg = p_add(mu_v, p_mul(p.dt, mu_u));
+      const float2 mu = p_sub(mu_u, p_mul(p.dt, ky));
+      float2 mv = p_sub(gg, p_mul(p.dt, p_add(p_add(p_mul(p.beta, ky), cy), p_mul(p.aml[i], yi))));
+      const int rj = a.rec_map[i];
+      if (rj >= 0 && nb >= 1)
+        mv = p_add(mv, p_of(a.out_v[(int64_t)nb * d.n_rec + rj] - d.target[(int64_t)nb * d.n_rec + rj]));
+      a.mu_u[i] = mu;
+      a.mu_v[i] = mv;
+      yn[i] = p_mul(p_add(mv, p_mul(p.dt, mu)), p.iml[i]);
+    }
+  }
+  if (last_block(&g.s->ticket)) {
+    const int t = step - 1;
+    if (g.f_ptr) {
+      if (t >= 0 && t < g.n_t)
+        for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x)
+          p.f[g.f_slot[k]] = make_float2(0.f, 0.f);
+      __syncthreads();
+      if (t + 1 < g.n_t)
+        for (int64_t k = g.f_ptr[t + 1] + threadIdx.x; k < g.f_ptr[t + 2]; k += blockDim.x)
+          p.f[g.f_slot[k]] = p_of(g.f_val[k]);
+    }
+    if (threadIdx.x == 0) {
+      g.s->ticket = 0;
+      g.s->t = step;
+      *a.n_dev = nb - 1;
+    }
+  }
+}
+
 constexpr int kAdjElemThreads = 128;
 
 // Element gradients of one segment, steps t1 - 1 down to t0, once its backward steps are
@@ -903,16 +1019,31 @@ void launch_grad_seg(const sc_nb_newmark* h, cudaStream_t st, const sc_adj_desc&
   }
 }
 
+template <int TPR>
+void launch_adj_fused_t(const sc_nb_newmark* h, cudaStream_t st, int kk, const SegStore& store, const sc_adj_desc& d,
+                        const AdjState& a, int cur) {
+  k_adj_fused<3, TPR><<<h->tpr_blocks, kThreads, 0, st>>>(h->g, pair_step(h, kk), store, d, a, cur);
+}
+void launch_adj_fused(const sc_nb_newmark* h, cudaStream_t st, int kk, const SegStore& store, const sc_adj_desc& d,
+                      const AdjState& a, int cur) {
+  switch (h->tpr) {
+    case 4: launch_adj_fused_t<4>(h, st, kk, store, d, a, cur); break;
+    case 2: launch_adj_fused_t<2>(h, st, kk, store, d, a, cur); break;
+    default: launch_adj_fused_t<1>(h, st, kk, store, d, a, cur); break;
+  }
+}
+
 }  // namespace
 
 // Forward from rest with pair checkpoints every `checkpoint` steps, then the reverse sweep
-// over the segments, last first.  Two streams: the handle's stream runs the forward and the
-// backward; a second stream recomputes segment s - 1 from its checkpoint (the explicit step
-// storing the element gradient's inputs into one of two segment buffers) while the backward
-// reverses segment s from the other buffer (one row kernel per step, then one element
-// gradient kernel for the whole segment).  The forward and the recompute run the same kernels
-// from the same pair state, so the recomputed states are bitwise the forward's.  Requires the
-// pair arithmetic (the default).
+// over the segments, last first, on the handle's stream: the last segment is recomputed from
+// its checkpoint (the explicit step storing the element gradient's inputs into one of two
+// segment buffers); then for each segment s the backward steps of s run fused with the
+// recompute steps of s - 1 into the other buffer (one kernel per pair of steps, one pass over
+// the K planes for both), the rest of either alone, then one element-gradient kernel for the
+// whole of s.  The forward and the recompute run the same arithmetic from the same pair state,
+// so the recomputed states are bitwise the forward's.  Requires the pair arithmetic (the
+// default).
 extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_host, double* grad_E,
                              double* grad_rho) {
   if (!h || !dp || !grad_E || !grad_rho) return SC_BAD_ARG;
@@ -922,11 +1053,12 @@ extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_
       !d.young || !d.rho || !d.ml1 || !d.l_eptr || h->g.D != 3 || !h->explicit_pair)
     return SC_BAD_ARG;
   Args& g = h->g;
-  cudaStream_t st = h->user;  // forward and backward
-  cudaStream_t rs = nullptr;  // recompute
+  cudaStream_t st = h->user;
   const int N = d.n_steps, C = d.checkpoint < d.n_steps ? d.checkpoint : d.n_steps, nseg = (N + C - 1) / C;
   const int nbuf = nseg > 1 ? 2 : 1;
   auto buf = [&](int sgi) { return nbuf == 2 ? (sgi & 1) : 0; };
+  auto seg0 = [&](int sgi) { return sgi * C; };
+  auto seg1 = [&](int sgi) { return sgi * C + C < N ? sgi * C + C : N; };
   const int64_t ns = g.n_s;
   // the caller's output configuration, restored at the end
   const int o_int = g.out_interval, o_nrec = g.n_rec;
@@ -940,12 +1072,8 @@ extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_
   int* t0_dev = nullptr;  // the segment start of each buffer
   int rc = SC_OK;
   auto M = [&](void** p, size_t b) { return check(cudaMallocAsync(p, b, st), "adjoint malloc"); };
-  cudaGraphExec_t rec_exec[2][2] = {}, bwd_exec[2][2] = {};
-  cudaGraph_t rec_graph[2][2] = {}, bwd_graph[2][2] = {};
-  cudaEvent_t ev_fwd = nullptr, ev_rs_end = nullptr, rec_done[2] = {}, bwd_done[2] = {};
-  // phase timers: [0, 1] forward; per segment [2 + 4 s, 3 + 4 s] recompute (second stream) and
-  // [4 + 4 s, 5 + 4 s] backward
-  std::vector<cudaEvent_t> tev;
+  // phase timers: forward [0, 1]; the last segment's recompute [1, 2]; the rest of the sweep [2, 3]
+  cudaEvent_t tev[4] = {};
   do {
     if ((rc = M((void**)&ck_u, 8 * ns * nseg)) || (rc = M((void**)&ck_v, 8 * ns * nseg)) ||
         (rc = M((void**)&s.mu_u, 8 * ns)) || (rc = M((void**)&s.mu_v, 8 * ns)) || (rc = M((void**)&s.y[0], 8 * ns)) ||
@@ -965,11 +1093,6 @@ extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_
     }
     if (rc) break;
     if ((rc = check(cudaMallocHost((void**)&t_host, 8 * (size_t)nseg), "adjoint pinned"))) break;
-    if ((rc = check(cudaStreamCreateWithFlags(&rs, cudaStreamNonBlocking), "adjoint stream"))) break;
-    for (cudaEvent_t* ev : {&ev_fwd, &ev_rs_end, &rec_done[0], &rec_done[1], &bwd_done[0], &bwd_done[1]})
-      if ((rc = check(cudaEventCreateWithFlags(ev, cudaEventDisableTiming), "adjoint event"))) break;
-    if (rc) break;
-    tev.assign(2 + 4 * (size_t)nseg, nullptr);
     for (auto& ev : tev)
       if ((rc = check(cudaEventCreate(&ev), "adjoint timer"))) break;
     if (rc) break;
@@ -989,110 +1112,74 @@ extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_
     force_reset(h, 0);
     cudaEventRecord(tev[0], st);
     for (int sgi = 0; sgi < nseg && !rc; ++sgi) {
-      const int t0 = sgi * C, t1 = t0 + C < N ? t0 + C : N;
       cudaMemcpyAsync(ck_u + sgi * ns, h->u2, 8 * ns, cudaMemcpyDeviceToDevice, st);
       cudaMemcpyAsync(ck_v + sgi * ns, h->v2[0], 8 * ns, cudaMemcpyDeviceToDevice, st);
-      rc = explicit_steps(h, t0, t1);
+      rc = explicit_steps(h, seg0(sgi), seg1(sgi));
     }
     if (rc) break;
     cudaEventRecord(tev[1], st);
     k_adj_misfit<<<1, 1024, 0, st>>>(s.out_v, d.target, d.n_rec, N, s.J);
-    // recompute graphs (per buffer and ping-pong parity): the explicit step storing the
-    // element gradient's inputs, recording no receivers (the forward's records stand)
-    g.n_rec = 0;
-    for (int b = 0; b < nbuf && !rc; ++b)
-      for (int kk = 0; kk < 2 && !rc; ++kk) {
-        if ((rc = check(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal), "capture rec"))) break;
-        launch_pair<3>(h, h->cap, kk, SegStore{a[b].wp, a[b].v32, a[b].a32, a[b].seg_t0});
-        if ((rc = check(cudaStreamEndCapture(h->cap, &rec_graph[b][kk]), "end rec"))) break;
-        rc = check(cudaGraphInstantiate(&rec_exec[b][kk], rec_graph[b][kk], 0), "inst rec");
-      }
-    g.n_rec = d.n_rec;
-    // backward graphs: the row kernel per buffer and parity
-    for (int b = 0; b < nbuf && !rc; ++b)
-      for (int kk = 0; kk < 2 && !rc; ++kk) {
-        if ((rc = check(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal), "capture bwd"))) break;
-        launch_adj_rows(h, h->cap, d, a[b], kk);
-        if ((rc = check(cudaStreamEndCapture(h->cap, &bwd_graph[b][kk]), "end bwd"))) break;
-        rc = check(cudaGraphInstantiate(&bwd_exec[b][kk], bwd_graph[b][kk], 0), "inst bwd");
-      }
-    if (rc) break;
     k_adj_init<<<h->vec_blocks, 256, 0, st>>>(g, pair_step(h, 0), s, d.target, d.n_rec, N);
-    cudaEventRecord(ev_fwd, st);
-    cudaStreamWaitEvent(rs, ev_fwd, 0);
-    // recompute of segment sgi on the second stream into its buffer
-    auto recompute = [&](int sgi) {
+    // the recompute records no receivers (the forward's records stand)
+    g.n_rec = 0;
+    // restore segment sgi's checkpoint as the recompute's state, its start in its buffer
+    auto recompute_setup = [&](int sgi) {
       const int b = buf(sgi);
-      const int t0 = sgi * C, t1 = t0 + C < N ? t0 + C : N;
-      t_host[sgi] = t0;
-      cudaMemcpyAsync(h->u2, ck_u + sgi * ns, 8 * ns, cudaMemcpyDeviceToDevice, rs);
-      cudaMemcpyAsync(h->v2[0], ck_v + sgi * ns, 8 * ns, cudaMemcpyDeviceToDevice, rs);
-      cudaMemcpyAsync(a[b].seg_t0, t_host + sgi, 4, cudaMemcpyHostToDevice, rs);
-      k_w_pairs<<<h->vec_blocks, 256, 0, rs>>>(ns, h->u2, h->v2[0], host_pair(g.beta_r), h->w2[0]);
-      force_reset(h, t0, rs);
-      k_set_t<<<1, 1, 0, rs>>>(g.s, t0);
-      cudaEventRecord(tev[2 + 4 * sgi], rs);
-      int r = check_launch("recompute set-up"), kk = 0;
-      for (int t = t0; t < t1 && !r; ++t, kk ^= 1) r = check(cudaGraphLaunch(rec_exec[b][kk], rs), "rec launch");
-      cudaEventRecord(tev[3 + 4 * sgi], rs);
-      cudaEventRecord(rec_done[b], rs);
-      return r;
+      t_host[sgi] = seg0(sgi);
+      cudaMemcpyAsync(h->u2, ck_u + sgi * ns, 8 * ns, cudaMemcpyDeviceToDevice, st);
+      cudaMemcpyAsync(h->v2[0], ck_v + sgi * ns, 8 * ns, cudaMemcpyDeviceToDevice, st);
+      cudaMemcpyAsync(a[b].seg_t0, t_host + sgi, 4, cudaMemcpyHostToDevice, st);
+      k_w_pairs<<<h->vec_blocks, 256, 0, st>>>(ns, h->u2, h->v2[0], host_pair(g.beta_r), h->w2[0]);
+      force_reset(h, seg0(sgi), st);
+      k_set_t<<<1, 1, 0, st>>>(g.s, seg0(sgi));
     };
-    rc = recompute(nseg - 1);
+    auto store_of = [&](int sgi) {
+      const AdjState& ab = a[buf(sgi)];
+      return SegStore{ab.wp, ab.v32, ab.a32, ab.seg_t0};
+    };
+    recompute_setup(nseg - 1);
+    int kk = 0;  // ping-pong parity of the recompute's state buffers
+    for (int t = seg0(nseg - 1); t < seg1(nseg - 1); ++t, kk ^= 1) launch_pair<3>(h, st, kk, store_of(nseg - 1));
+    cudaEventRecord(tev[2], st);
     int yk = 0;  // y[yk] holds the y of the next step to reverse
-    for (int sgi = nseg - 1; sgi >= 0 && !rc; --sgi) {
-      const int b = buf(sgi);
-      const int t0 = sgi * C, t1 = t0 + C < N ? t0 + C : N;
-      if (sgi >= 1) {
-        // segment sgi - 1 goes to the buffer the backward of segment sgi + 1 read
-        if (sgi + 1 < nseg) cudaStreamWaitEvent(rs, bwd_done[buf(sgi - 1)], 0);
-        if ((rc = recompute(sgi - 1))) break;
-      }
-      cudaStreamWaitEvent(st, rec_done[b], 0);
-      t_host[nseg + sgi] = t1 - 1;
+    for (int sgi = nseg - 1; sgi >= 0; --sgi) {
+      const AdjState& ab = a[buf(sgi)];
+      const int len_b = seg1(sgi) - seg0(sgi), len_r = sgi >= 1 ? seg1(sgi - 1) - seg0(sgi - 1) : 0;
+      t_host[nseg + sgi] = seg1(sgi) - 1;
       cudaMemcpyAsync(s.n_dev, t_host + nseg + sgi, 4, cudaMemcpyHostToDevice, st);
-      cudaEventRecord(tev[4 + 4 * sgi], st);
-      for (int t = t1 - 1; t >= t0 && !rc; --t, yk ^= 1) rc = check(cudaGraphLaunch(bwd_exec[b][yk], st), "bwd launch");
-      launch_grad_seg(h, st, d, a[b], t0, t1);
-      cudaEventRecord(tev[5 + 4 * sgi], st);
-      cudaEventRecord(bwd_done[b], st);
-    }
-    if (!rc) rc = check_launch("adjoint sweep");
-    cudaEventRecord(ev_rs_end, rs);
-    cudaStreamWaitEvent(st, ev_rs_end, 0);
-    if (!rc && J_host) rc = check(cudaMemcpyAsync(J_host, s.J, 8, cudaMemcpyDeviceToHost, st), "J");
-    if (!rc) rc = check(cudaStreamSynchronize(st), "sync adjoint");
-    if (!rc) {
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, tev[0], tev[1]);
-      h->adj_ms[0] = ms;
-      h->adj_ms[1] = h->adj_ms[2] = 0.f;
-      for (int sgi = 0; sgi < nseg; ++sgi) {
-        cudaEventElapsedTime(&ms, tev[2 + 4 * sgi], tev[3 + 4 * sgi]);
-        h->adj_ms[1] += ms;
-        cudaEventElapsedTime(&ms, tev[4 + 4 * sgi], tev[5 + 4 * sgi]);
-        h->adj_ms[2] += ms;
+      if (sgi >= 1) {
+        recompute_setup(sgi - 1);
+        kk = 0;
       }
-      cudaEventElapsedTime(&ms, tev[1], tev[5]);
-      h->adj_ms[3] = ms;
+      for (int j = 0; j < len_b; ++j, yk ^= 1) {
+        if (j < len_r) {
+          launch_adj_fused(h, st, kk, store_of(sgi - 1), d, ab, yk);
+          kk ^= 1;
+        } else {
+          launch_adj_rows(h, st, d, ab, yk);
+        }
+      }
+      for (int j = len_b; j < len_r; ++j, kk ^= 1) launch_pair<3>(h, st, kk, store_of(sgi - 1));
+      launch_grad_seg(h, st, d, ab, seg0(sgi), seg1(sgi));
+      if ((rc = check_launch("adjoint sweep"))) break;
     }
+    if (rc) break;
+    cudaEventRecord(tev[3], st);
+    if (J_host && (rc = check(cudaMemcpyAsync(J_host, s.J, 8, cudaMemcpyDeviceToHost, st), "J"))) break;
+    if ((rc = check(cudaStreamSynchronize(st), "sync adjoint"))) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, tev[0], tev[1]);
+    h->adj_ms[0] = ms;
+    cudaEventElapsedTime(&ms, tev[1], tev[2]);
+    h->adj_ms[1] = ms;
+    cudaEventElapsedTime(&ms, tev[2], tev[3]);
+    h->adj_ms[2] = ms;
+    cudaEventElapsedTime(&ms, tev[1], tev[3]);
+    h->adj_ms[3] = ms;
   } while (0);
   g.n_rec = d.n_rec;
   cudaStreamSynchronize(st);
-  if (rs) {
-    cudaStreamSynchronize(rs);
-    cudaStreamDestroy(rs);
-  }
-  for (int b = 0; b < 2; ++b)
-    for (int kk = 0; kk < 2; ++kk) {
-      if (rec_exec[b][kk]) cudaGraphExecDestroy(rec_exec[b][kk]);
-      if (rec_graph[b][kk]) cudaGraphDestroy(rec_graph[b][kk]);
-      if (bwd_exec[b][kk]) cudaGraphExecDestroy(bwd_exec[b][kk]);
-      if (bwd_graph[b][kk]) cudaGraphDestroy(bwd_graph[b][kk]);
-    }
   for (auto ev : tev)
-    if (ev) cudaEventDestroy(ev);
-  for (cudaEvent_t ev : {ev_fwd, ev_rs_end, rec_done[0], rec_done[1], bwd_done[0], bwd_done[1]})
     if (ev) cudaEventDestroy(ev);
   void* frees[] = {ck_u,  ck_v,     s.mu_u, s.mu_v,  s.y[0], s.y[1], s.out_v, s.n_dev, s.ticket_r, t0_dev, s.rec_map,
                    s.J,   s.iE,     s.iR,   a[0].wp, a[0].v32, a[0].a32, a[0].ys, a[1].wp, a[1].v32, a[1].a32, a[1].ys};
@@ -1103,8 +1190,9 @@ extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_
   return rc;
 }
 
-// [0] forward with checkpoints, [1] recompute (summed over segments), [2] backward (summed),
-// [3] the reverse sweep's wall time (recompute and backward overlap on two streams)
+// [0] forward with checkpoints; [1] recompute of the last segment (alone); [2] the rest of the
+// reverse sweep (backward steps fused with the previous segment's recompute, element
+// gradients); [3] the reverse sweep's wall time, [1] + [2]
 extern "C" int sc_nb_adjoint_timings(sc_nb_newmark* h, float* ms4) {
   if (!h || !ms4) return SC_BAD_ARG;
   for (int i = 0; i < 4; ++i) ms4[i] = h->adj_ms[i];
