@@ -221,7 +221,7 @@ int sc_nb_create(sc_nb_newmark** h, int n_nodes, int dim, const int* eqmap, cons
 /* Warm start of each Newmark step (no reference counterpart): the PCG starts from the
  * polynomial extrapolation of order p of the previous accelerations,
  * x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k} (p = 2: 3 a_n - 3 a_{n-1} + a_{n-2}).  order 1..8
- * fixes p; 0 (the default) adapts it on the device: starting from 2 it moves to a neighbouring
+ * fixes p; 0 (the default) adapts it on the device: starting from 4 it moves to a neighbouring
  * order while the mean PCG iterations over windows of 16 steps fall, steps back when they
  * rise, and holds 8 windows before probing again.  The order changes the iteration count,
  * not the answer, which meets the same tolerance. */
