@@ -124,3 +124,49 @@ def test_batched_shapes_agree_bitwise(cuda):
     for vb, ub in results[1:]:
         np.testing.assert_array_equal(vb, results[0][0])
         np.testing.assert_array_equal(ub, results[0][1])
+
+
+def test_batched_grid_kernel_on_a_notched_mesh(cuda):
+    """The tiled uniform-grid kernel on a box with a block of elements cut out of a top
+    corner (halo points without nodes, nodes with fewer than 8 elements) gives bitwise the
+    incidence-list kernel's histories."""
+    from scatter_gb300 import meshgen
+    from scatter_gb300.batched import BatchedExplicit
+    from scatter_gb300.force_external import ricker_table
+    from scatter_gb300.mesher import ReadMesh
+    from scatter_gb300.random_fields import element_centroids, lognormal_fields
+
+    nx, ny, nz, h = 8, 5, 6, 0.5
+    nodes, elem, _ = meshgen.box_hexa8(nx, ny, nz, h)
+    X = nodes[:, 1:]
+    idx = {int(n): k for k, n in enumerate(nodes[:, 0])}
+    cen = np.stack([X[[idx[int(n)] for n in e]].mean(axis=0) for e in elem])
+    lo = X.min(axis=0)
+    keep = ~((cen[:, 0] > lo[0] + 2.0) & (cen[:, 1] > lo[1] + 1.5) & (cen[:, 2] > lo[2] + 1.0))
+    elem = elem[keep]
+    used = np.isin(nodes[:, 0], np.unique(elem))
+    m = ReadMesh.from_arrays(nodes[used], elem, "hexa8", [[3, 1, "solid"]], np.ones(len(elem), dtype=np.int64))
+    m.read_bc(meshgen.box_boundaries(nx * h, ny * h, nz * h, "111", "100", "001"))  # no Lysmer faces
+    m.mapping()
+    m.connectivities()
+    R = 8
+    young = lognormal_fields(element_centroids(m), seed=9, R=R, lengths=(2.0, 1.0, 2.0), mean=50e6, sd=12.5e6)
+    dt, n_t = 5e-5, 100
+    time = np.linspace(0, dt * (n_t - 1), n_t)
+    top = m.top_nodes()
+    table = ricker_table(m, int(top[0]), -1e4, 40.0, 0.002, time)
+    rec = [int(m.eq_nb_dof[m.node_index()[n], 1]) for n in top[::2]]
+    results = []
+    for rpt, tpb, grid in ((4, 256, False), (1, 256, True), (2, 256, True)):
+        b = BatchedExplicit(m, young, 0.3, 1900.0, [1, 0.02, 50, 0.02], [1, 1], 1e3, dt)
+        assert b.grid_tables is not None
+        b.set_shape(rpt, tpb, grid)
+        b.set_force(table)
+        b.set_output(1, rec, n_t)
+        b.run(0, n_t - 1)
+        results.append((b.velocities(), b.state()[0]))
+        b.close()
+    assert np.abs(results[0][0]).max() > 0
+    for vb, ub in results[1:]:
+        np.testing.assert_array_equal(vb, results[0][0])
+        np.testing.assert_array_equal(ub, results[0][1])

@@ -235,3 +235,47 @@ def test_batched_incidence_and_hex8_grid_tables():
     bad = elem_idx.copy()
     bad[3] = bad[3][[1, 0, 3, 2, 5, 4, 7, 6]]
     assert hex8_grid_tables(xyz, bad) is None
+
+
+def test_hex8_grid_tables_with_holes():
+    """An L-shaped structured hexa8 mesh (a box with one quarter removed): every element's
+    nodes are found in the tile halos at their natural offsets, the removed quarter's lattice
+    points are -1 in the halos, and every node is owned by exactly one tile."""
+    from scatter_gb300.batched import HEX8_NAT, HEX8_TILE, hex8_grid_tables
+    from scatter_gb300.system_matrix import model_arrays
+
+    m = meshgen.box_model(9, 3, 7, 0.5)
+    nodes, _, elem_idx, _ = model_arrays(m)
+    xyz = nodes[:, 1:].astype(float)
+    c = xyz[elem_idx].mean(axis=1)
+    keep = ~((c[:, 0] > 2.0) & (c[:, 2] < c[:, 2].min() + 1.5))  # drop a corner block of elements
+    el = elem_idx[keep]
+    used = np.unique(el)
+    remap = -np.ones(len(xyz), dtype=np.int64)
+    remap[used] = np.arange(len(used))
+    el = remap[el]
+    xyz = xyz[used]
+    N, E = len(xyz), len(el)
+    halo, elem8 = hex8_grid_tables(xyz, el)
+    tx, ty, tz = HEX8_TILE
+    hx, hy = tx + 2, ty + 2
+    inner = [(x + 1) + hx * ((y + 1) + hy * (z + 1)) for z in range(tz) for y in range(ty) for x in range(tx)]
+    owned = halo[:, inner].ravel()
+    owned = owned[owned >= 0]
+    assert len(owned) == N and len(np.unique(owned)) == N
+    assert (halo[:, inner] == -1).any()  # lattice points of the removed block
+    where = {}
+    for t in range(len(halo)):
+        for p in inner:
+            if halo[t, p] >= 0:
+                where[int(halo[t, p])] = (t, p)
+    for e in range(E):
+        for la in range(8):
+            a = el[e, la]
+            assert elem8[a, la] == e
+            t, p = where[int(a)]
+            for lb in range(8):
+                d = HEX8_NAT[lb] - HEX8_NAT[la]
+                assert halo[t, p + d[0] + hx * (d[1] + hy * d[2])] == el[e, lb]
+    # nodes at the re-entrant corner have fewer than 8 elements
+    assert ((elem8 >= 0).sum(axis=1) < 8).sum() > 0
