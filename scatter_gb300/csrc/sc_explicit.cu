@@ -1074,6 +1074,29 @@ extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_
   auto M = [&](void** p, size_t b) { return check(cudaMallocAsync(p, b, st), "adjoint malloc"); };
   // phase timers: forward [0, 1]; the last segment's recompute [1, 2]; the rest of the sweep [2, 3]
   cudaEvent_t tev[4] = {};
+  // threads per node row for the whole adjoint (forward, recompute and backward alike, so the
+  // recomputed states are bitwise the forward's): the handle's tuned value, lowered until the
+  // fused kernel, with its two sets of accumulators, fits in one wave of resident blocks
+  const int tpr0 = h->tpr;
+  const unsigned blocks0 = h->tpr_blocks;
+  {
+    int dev = 0, n_sm = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    int tpr = tpr0;
+    while (tpr > 1) {
+      int per_sm = 0;
+      cudaError_t e = tpr == 4   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adj_fused<3, 4>, kThreads, 0)
+                      : tpr == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adj_fused<3, 2>, kThreads, 0)
+                                 : cudaErrorInvalidValue;
+      const int64_t want = (((int64_t)g.n_nodes + 31) / 32 * 32 * tpr + kThreads - 1) / kThreads;
+      if (e == cudaSuccess && want <= (int64_t)per_sm * n_sm) break;
+      tpr /= 2;
+    }
+    cudaGetLastError();
+    const int64_t want = (((int64_t)g.n_nodes + 31) / 32 * 32 * tpr + kThreads - 1) / kThreads;
+    h->tpr = tpr;
+    h->tpr_blocks = (unsigned)(want < 152 * 16 ? (want < 1 ? 1 : want) : 152 * 16);
+  }
   do {
     if ((rc = M((void**)&ck_u, 8 * ns * nseg)) || (rc = M((void**)&ck_v, 8 * ns * nseg)) ||
         (rc = M((void**)&s.mu_u, 8 * ns)) || (rc = M((void**)&s.mu_v, 8 * ns)) || (rc = M((void**)&s.y[0], 8 * ns)) ||
@@ -1186,7 +1209,9 @@ extern "C" int sc_nb_adjoint(sc_nb_newmark* h, const sc_adj_desc* dp, double* J_
   for (void* q : frees)
     if (q) cudaFree(q);
   if (t_host) cudaFreeHost(t_host);
-  sc_nb_set_output(h, o_int, o_nrec, o_rec, o_u, o_v, o_a, o_nout);
+  sc_nb_set_output(h, o_int, o_nrec, o_rec, o_u, o_v, o_a, o_nout);  // drops the explicit graphs
+  h->tpr = tpr0;
+  h->tpr_blocks = blocks0;
   return rc;
 }
 
