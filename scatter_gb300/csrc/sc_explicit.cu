@@ -90,6 +90,14 @@ __global__ void __launch_bounds__(kThreads) k_explicit_pair(Args g, PairStep p, 
   const int sub = threadIdx.x % TPR;
   SELL_ROW_LOOP_T(TPR) {
     SELL_ROW_BEGIN(g.sf_ptr)
+    // the row's update inputs into L2 while its products run (one thread per row, the large
+    // meshes' shape; with more threads per row the extra registers cost more than it saves)
+    if (TPR == 1 && row < g.n_nodes) {
+      const int64_t i0 = row * D;
+      const void* pf[5] = {p.v_in + i0, p.u + i0, p.f + i0, p.aml + i0, p.iml + i0};
+#pragma unroll
+      for (int k = 0; k < 5; ++k) asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(pf[k])));
+    }
     float hi[D], lo[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) hi[c] = lo[c] = 0.f;
