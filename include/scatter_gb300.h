@@ -148,9 +148,10 @@ int sc_combine(int64_t n, double c0, const double* x, double c1, const double* y
  *     A x = f(t) - C vp - K up,   A = M + dt/2 C + dt^2/4 K,
  *     vp = v + dt/2 a,  up = u + dt v + dt^2/4 a,
  * then u = up + dt^2/4 x, v = vp + dt/2 x, a = x -- the same update as the reference's
- * K^ u = rhs form.  The solve is Jacobi-preconditioned CG on A, warm-started from the
- * previous acceleration, to ||r|| <= rtol ||rhs|| (FP64 dot products, deterministic
- * reductions).  One step is one CUDA graph launch with a device-side conditional loop.
+ * K^ u = rhs form.  The solve is Jacobi-preconditioned CG on A to ||r|| <= rtol ||rhs||
+ * (FP64 dot products, deterministic reductions), warm-started from the polynomial
+ * extrapolation of the previous accelerations, as sc_nb_set_predictor describes.  One step
+ * is one CUDA graph launch with a device-side conditional loop.
  *
  * The caller owns every buffer.  sc_newmark_workspace_doubles() gives the scratch size.
  * Force table (CSR over time): f_ptr [n_t+1], f_eq [f_ptr[n_t]], f_val [..]: the force at
@@ -173,6 +174,9 @@ int sc_newmark_set_output(sc_newmark* h, int out_interval, int n_rec, const int*
 int sc_newmark_initial_acceleration(sc_newmark* h);
 /* run steps t = t_begin .. t_end-1 -> states t+1; asynchronous (graph launches) */
 int sc_newmark_run(sc_newmark* h, int t_begin, int t_end);
+/* Order of the warm start, as sc_nb_set_predictor: 1..8 fixed, 0 adaptive (the default);
+ * 1..8 then 0 keeps the history entries that are current. */
+int sc_newmark_set_predictor(sc_newmark* h, int order);
 /* synchronous: CG status of the run so far (SC_OK / SC_NOT_CONVERGED / SC_BREAKDOWN),
  * total and maximum CG iterations per step */
 int sc_newmark_status(sc_newmark* h, int64_t* total_iters, int* max_iters_per_step);

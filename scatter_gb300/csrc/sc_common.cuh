@@ -61,4 +61,95 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return s;
 }
 
+// ------------------------------------------------ warm start of the per-step PCG (Newmark)
+// Both Newmark solvers start each step's PCG from the polynomial of degree p through the last
+// p+1 accelerations, evaluated one step ahead: x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k}
+// (p = 0: a_n; p = 2: 3a_n - 3a_{n-1} + a_{n-2}).  The order only changes the iteration
+// count, not the converged answer.
+constexpr int kHistMax = 8;  // acceleration history kept for the warm start
+// order control (fixed order 0 = adaptive): start at kPredStart, then compare the mean PCG
+// iterations of windows of kPredWin steps, keep climbing while a probed neighbour order is
+// better, step back when it is worse and hold there kPredHold windows
+constexpr int kPredStart = 4, kPredWin = 16, kPredHold = 8;
+
+// cf[k] = (-1)^k C(p+1, k+1) for k <= p, 0 beyond: exact integers, in a fixed order
+__device__ __forceinline__ void warm_start_coeffs(int p, double* cf) {
+  long long c = p + 1;
+  cf[0] = (double)c;
+#pragma unroll
+  for (int k = 1; k <= kHistMax; ++k) {
+    if (k <= p) c = c * (p + 1 - k) / (k + 1);
+    cf[k] = k <= p ? ((k & 1) ? -(double)c : (double)c) : 0.0;
+  }
+}
+
+// The controller's state lives in each solver's scalar block S, which has the int fields
+// hist, pord, pdir, win_n, win_it, probing, hold, it and the double ref_avg.
+template <class S>
+__device__ __forceinline__ int warm_start_order(const S* s, int fixed) {
+  const int ord = fixed > 0 ? fixed : s->pord;
+  return s->hist < ord ? s->hist : ord;
+}
+
+// history entries kept after a step: the fixed order's, or one beyond the adaptive order
+// (it moves by at most one per window)
+template <class S>
+__device__ __forceinline__ int warm_start_depth(const S* s, int fixed) {
+  return fixed > 0 ? fixed : min(kHistMax, s->pord + 1);
+}
+
+template <class S>
+__device__ inline void warm_start_init(S* s) {
+  s->hist = 0;
+  s->pord = kPredStart;
+  s->pdir = 1;
+  s->win_n = s->win_it = s->probing = s->hold = 0;
+  s->ref_avg = 0.0;
+}
+
+// After a step (one thread): one more history entry, and the step's iterations (s->it) into
+// the adaptive order's window.
+template <class S>
+__device__ inline void warm_start_advance(S* s, int fixed) {
+  if (s->hist < kHistMax) s->hist += 1;
+  if (fixed > 0) return;
+  if (++s->win_n < kPredWin) {
+    s->win_it += s->it;
+    return;
+  }
+  // the window just ended: its mean iterations per step
+  const double avg = (double)(s->win_it + s->it) / kPredWin;
+  s->win_n = 0;
+  s->win_it = 0;
+  if (s->probing) {
+    if (avg <= s->ref_avg) {  // the probed order is no worse: keep it, probe further
+      s->ref_avg = avg;
+      const int np = s->pord + s->pdir;
+      if (np >= 1 && np <= kHistMax) {
+        s->pord = np;
+      } else {
+        s->probing = 0;
+        s->pdir = -s->pdir;
+        s->hold = kPredHold;
+      }
+    } else {  // worse: back to the better order, hold, probe the other side next
+      s->pord -= s->pdir;
+      s->pdir = -s->pdir;
+      s->probing = 0;
+      s->hold = kPredHold;
+    }
+  } else if (s->hold > 0) {
+    s->hold -= 1;
+  } else {  // this window is the reference: probe the neighbour in the current direction
+    s->ref_avg = avg;
+    const int np = s->pord + s->pdir;
+    if (np >= 1 && np <= kHistMax) {
+      s->pord = np;
+      s->probing = 1;
+    } else {
+      s->pdir = -s->pdir;
+    }
+  }
+}
+
 }  // namespace sc

@@ -14,11 +14,6 @@ namespace nb {
 
 constexpr int kThreads = 256;
 constexpr int kMaxFsai = 64;  // FSAI row pattern capacity (slots); larger rows fall back to Jacobi
-constexpr int kHistMax = 8;   // acceleration history kept for the warm start
-// warm-start order control (pred_order 0 = adaptive): start at kPredStart, then compare the
-// mean PCG iterations of windows of kPredWin steps, keep climbing while a probed neighbour
-// order is better, step back when it is worse and hold there kPredHold windows
-constexpr int kPredStart = 4, kPredWin = 16, kPredHold = 8;
 
 struct Scal {
   double rz, pw, rr, bb, alpha, beta, tol2, pad0;

@@ -54,21 +54,10 @@ __global__ void k_force(Args g) {
 // stored: q1 = up + beta vp, q2 = alpha vp, y1 = vp, x0.
 __global__ void k_predict(Args g) {
   const double dt = g.dt, h = 0.5 * dt, qq = 0.25 * dt * dt;
-  const int hist = g.s->hist;
-  // warm-start order p = min(history, order) and its coefficients (-1)^k C(p+1, k+1), exact
-  // integers, computed once per thread
-  const int ord = g.pred_order > 0 ? g.pred_order : g.s->pord;
-  const int p = hist < ord ? hist : ord;
+  // warm-start order p = min(history, order) and its coefficients, once per thread
+  const int p = warm_start_order(g.s, g.pred_order);
   double cf[kHistMax + 1];
-  {
-    long long c = p + 1;
-    cf[0] = (double)c;
-#pragma unroll
-    for (int k = 1; k <= kHistMax; ++k) {
-      if (k <= p) c = c * (p + 1 - k) / (k + 1);
-      cf[k] = k <= p ? ((k & 1) ? -(double)c : (double)c) : 0.0;
-    }
-  }
+  warm_start_coeffs(p, cf);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
     const double ai = g.a[i], vi = g.v[i];
     const double vp = vi + h * ai;
@@ -507,9 +496,7 @@ __global__ void k_direction(Args g) {
 // u = up + dt^2/4 x ; v = vp + dt/2 x ; shift the acceleration history ; record ; t += 1
 __global__ void k_finalize(Args g) {
   const double dt = g.dt, h = 0.5 * dt, qq = 0.25 * dt * dt;
-  // history kept: the fixed order's entries, or one beyond the adaptive order (it moves by
-  // at most one per window)
-  const int depth = g.pred_order > 0 ? g.pred_order : min(kHistMax, g.s->pord + 1);
+  const int depth = warm_start_depth(g.s, g.pred_order);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
     const double x = g.x[i], ai = g.a[i], vi = g.v[i];
     const double up = g.u[i] + dt * vi + qq * ai;
@@ -547,44 +534,7 @@ __global__ void k_advance(Args g) {
     s->total_iters += s->it;
     if (s->it > s->max_seen) s->max_seen = s->it;
     s->t += 1;
-    if (s->hist < kHistMax) s->hist += 1;
-    if (g.pred_order == 0 && ++s->win_n == kPredWin) {
-      // adaptive warm-start order, from the mean iterations of the window just ended
-      const double avg = (double)(s->win_it + s->it) / kPredWin;
-      s->win_n = 0;
-      s->win_it = 0;
-      if (s->probing) {
-        if (avg <= s->ref_avg) {  // the probed order is no worse: keep it, probe further
-          s->ref_avg = avg;
-          const int np = s->pord + s->pdir;
-          if (np >= 1 && np <= kHistMax) {
-            s->pord = np;
-          } else {
-            s->probing = 0;
-            s->pdir = -s->pdir;
-            s->hold = kPredHold;
-          }
-        } else {  // worse: back to the better order, hold, probe the other side next
-          s->pord -= s->pdir;
-          s->pdir = -s->pdir;
-          s->probing = 0;
-          s->hold = kPredHold;
-        }
-      } else if (s->hold > 0) {
-        s->hold -= 1;
-      } else {  // this window is the reference: probe the neighbour in the current direction
-        s->ref_avg = avg;
-        const int np = s->pord + s->pdir;
-        if (np >= 1 && np <= kHistMax) {
-          s->pord = np;
-          s->probing = 1;
-        } else {
-          s->pdir = -s->pdir;
-        }
-      }
-    } else if (g.pred_order == 0) {
-      s->win_it += s->it;
-    }
+    warm_start_advance(s, g.pred_order);
   }
 }
 
@@ -872,11 +822,7 @@ __global__ void k_init_scal(Scal* s, double tol2, int max_it) {
   s->t = 0;
   s->fsai_fallback = 0;
   s->ticket = 0;
-  s->hist = 0;
-  s->pord = kPredStart;
-  s->pdir = 1;
-  s->win_n = s->win_it = s->probing = s->hold = 0;
-  s->ref_avg = 0.0;
+  warm_start_init(s);
 }
 
 }  // namespace nb

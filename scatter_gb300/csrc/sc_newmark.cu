@@ -5,10 +5,13 @@
 //   vp = v + dt/2 a,  up = u + dt v + dt^2/4 a
 //   A x = f(t+1) - C vp - K up,          A = M + dt/2 C + dt^2/4 K
 //   u = up + dt^2/4 x,  v = vp + dt/2 x,  a = x
-// x is found by Jacobi-PCG warm-started from a, stopped at ||r|| <= rtol ||rhs||.
+// x is found by Jacobi-PCG stopped at ||r|| <= rtol ||rhs||, warm-started from the polynomial
+// extrapolation of the previous accelerations (x0 = sum_k (-1)^k C(p+1, k+1) a_{n-k}, order p
+// fixed by the caller or adapted on the device to the iteration counts: warm_start_* in
+// sc_common.cuh, shared with the node-block solver).
 //
 // Execution: one CUDA graph per step: [force, predict, residual] -> WHILE{spmv, update,
-// direction} -> [finalize].  The WHILE node is a graph conditional whose value the residual
+// direction} -> [finalize, record, advance].  The WHILE node is a graph conditional whose value the residual
 // and update kernels set on the device (converged / iteration cap / breakdown), so a step
 // costs exactly the iterations it needs with no host round trip.  Reductions are per-block
 // partials summed by the last block to finish (ticket counter, no spin-waits), in a fixed
@@ -23,11 +26,14 @@ namespace sc {
 constexpr int kRowThreads = 256;  // 8 warps, one row per warp
 
 struct NmScalars {
-  double rz, pw, rr, bb, alpha, beta, tol2, pad0;
+  double rz, pw, rr, bb, alpha, beta, tol2;
+  double ref_avg;  // warm start: mean iterations per step of the reference window
   long long total_iters;
-  int it, max_it, max_seen, status, t, pad1;
+  int it, max_it, max_seen, status, t;
+  int hist;  // valid previous accelerations (0..kHistMax) for the warm start
   unsigned int ticket;
-  unsigned int pad2[3];
+  // adaptive warm-start order: current order, probing direction, window and hold counters
+  int pord, pdir, win_n, win_it, probing, hold;
 };
 
 struct NmArgs {
@@ -37,7 +43,9 @@ struct NmArgs {
   const double *M, *C, *K, *A;
   double *u, *v, *a;
   double *vp, *up, *x, *r, *z, *p, *w, *dinv, *f;
-  double* part;  // [nblocks][4]
+  double* ah[kHistMax];  // previous accelerations a_{n-1} .. a_{n-kHistMax} (ah[0] most recent)
+  int pred_order;        // warm-start order (1..kHistMax), 0: adaptive (NmScalars::pord)
+  double* part;          // [nblocks][4]
   NmScalars* s;
   double dt;
   // force table
@@ -81,17 +89,26 @@ __global__ void k_force(NmArgs g) {
     for (int64_t k = g.f_ptr[t1] + threadIdx.x; k < g.f_ptr[t1 + 1]; k += blockDim.x) g.f[g.f_eq[k]] += g.f_val[k];
 }
 
+// vp, up ; the warm start x0 into w (w is scratch until the first k_spmv of the step)
 __global__ void k_predict(NmArgs g) {
   const double dt = g.dt, h = 0.5 * dt, q = 0.25 * dt * dt;
+  const int p = warm_start_order(g.s, g.pred_order);
+  double cf[kHistMax + 1];
+  warm_start_coeffs(p, cf);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
     const double ai = g.a[i], vi = g.v[i];
     g.vp[i] = vi + h * ai;
     g.up[i] = g.u[i] + dt * vi + q * ai;
+    double x0 = cf[0] * ai;  // terms summed in a fixed order
+#pragma unroll
+    for (int k = 1; k <= kHistMax; ++k)
+      if (k <= p) x0 += cf[k] * g.ah[k - 1][i];
+    g.w[i] = x0;
   }
 }
 
-// rhs = f - C vp - K up ; r = rhs - Op x0 ; z = dinv r ; p = z.  mode 0: x0 = a (step),
-// mode 1: x0 = 0 (initial acceleration, Op = M, vp/up point at v/u).
+// rhs = f - C vp - K up ; r = rhs - Op x0 ; z = dinv r ; p = z.  mode 0: x0 = w (the warm
+// start, step), mode 1: x0 = 0 (initial acceleration, Op = M, vp/up point at v/u).
 __global__ void __launch_bounds__(kRowThreads) k_residual(NmArgs g, const double* __restrict__ Op, int mode,
                                                           cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
@@ -108,7 +125,7 @@ __global__ void __launch_bounds__(kRowThreads) k_residual(NmArgs g, const double
       const int c = g.cols[k];
       sr = fma(g.C[k], vp[c], sr);
       sr = fma(g.K[k], up[c], sr);
-      if (mode == 0) sa = fma(Op[k], g.a[c], sa);
+      if (mode == 0) sa = fma(Op[k], g.w[c], sa);
     }
     sr = warp_sum(sr);
     sa = warp_sum(sa);
@@ -116,7 +133,7 @@ __global__ void __launch_bounds__(kRowThreads) k_residual(NmArgs g, const double
       const double rhs = g.f[row] - sr;
       const double r = rhs - sa;
       const double z = g.dinv[row] * r;
-      g.x[row] = mode == 0 ? g.a[row] : 0.0;
+      g.x[row] = mode == 0 ? g.w[row] : 0.0;
       g.r[row] = r;
       g.z[row] = z;
       g.p[row] = z;
@@ -247,13 +264,16 @@ __device__ inline void record(const NmArgs& g, int step) {
   }
 }
 
-// u = up + dt^2/4 x ; v = vp + dt/2 x ; a = x ; t += 1
+// u = up + dt^2/4 x ; v = vp + dt/2 x ; shift the acceleration history ; a = x
 __global__ void k_finalize(NmArgs g) {
   const double h = 0.5 * g.dt, q = 0.25 * g.dt * g.dt;
+  const int depth = warm_start_depth(g.s, g.pred_order);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
     const double x = g.x[i];
     g.u[i] = fma(q, x, g.up[i]);
     g.v[i] = fma(h, x, g.vp[i]);
+    for (int k = depth - 1; k > 0; --k) g.ah[k][i] = g.ah[k - 1][i];
+    g.ah[0][i] = g.a[i];
     g.a[i] = x;
   }
 }
@@ -270,8 +290,17 @@ __global__ void k_record(NmArgs g, int bump) {
   }
 }
 
-__global__ void k_advance(NmScalars* s) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) s->t += 1;
+// t += 1 ; the step's iterations into the warm start's order control
+__global__ void k_advance(NmArgs g) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    NmScalars* s = g.s;
+    s->t += 1;
+    warm_start_advance(s, g.pred_order);
+  }
+}
+
+__global__ void k_cap_hist(NmScalars* s, int n) {
+  if (s->hist > n) s->hist = n;
 }
 
 // initial acceleration: a = x after CG on M
@@ -304,6 +333,7 @@ __global__ void k_init_scalars(NmScalars* s, double tol2, int max_it) {
   s->status = SC_OK;
   s->t = 0;
   s->ticket = 0;
+  warm_start_init(s);
 }
 
 __global__ void k_set_t(NmScalars* s, int t) { s->t = t; }
@@ -374,7 +404,7 @@ int build_pcg_graph(sc_newmark* h, const double* Op, int mode, cudaGraph_t* grap
     if (mode == 0) {
       k_finalize<<<h->vec_blocks, 256, 0, cs>>>(g);
       k_record<<<h->vec_blocks, 256, 0, cs>>>(g, 1);
-      k_advance<<<1, 32, 0, cs>>>(g.s);
+      k_advance<<<1, 32, 0, cs>>>(g);
     } else {
       k_copy_x_to_a<<<h->vec_blocks, 256, 0, cs>>>(g);
       k_record<<<h->vec_blocks, 256, 0, cs>>>(g, 0);
@@ -401,6 +431,14 @@ int build_pcg_graph(sc_newmark* h, const double* Op, int mode, cudaGraph_t* grap
   return SC_OK;
 }
 
+// graphs bake in the kernel arguments: rebuilt lazily after a change
+void drop_graphs(sc_newmark* h) {
+  if (h->step_exec) cudaGraphExecDestroy(h->step_exec), h->step_exec = nullptr;
+  if (h->step_graph) cudaGraphDestroy(h->step_graph), h->step_graph = nullptr;
+  if (h->init_exec) cudaGraphExecDestroy(h->init_exec), h->init_exec = nullptr;
+  if (h->init_graph) cudaGraphDestroy(h->init_graph), h->init_graph = nullptr;
+}
+
 unsigned row_blocks_for(int64_t n) {
   // one row per warp, 8 warps per block, grid-stride; 16 blocks of 256 per SM
   int64_t b = (n + 7) / 8;
@@ -413,8 +451,8 @@ unsigned row_blocks_for(int64_t n) {
 }  // namespace
 
 extern "C" int64_t sc_newmark_workspace_doubles(int64_t n_eq, int64_t) {
-  // vp up x r z p w dinv f  +  part[blocks][4]  +  scalars
-  return 9 * n_eq + 4 * (int64_t)row_blocks_for(n_eq) + 4 * 152 * 16 + 64;
+  // vp up x r z p w dinv f  +  history ah[kHistMax]  +  part[blocks][4]  +  scalars
+  return (9 + kHistMax) * n_eq + 4 * (int64_t)row_blocks_for(n_eq) + 4 * 152 * 16 + 64;
 }
 
 extern "C" int sc_newmark_create(sc_newmark** out, int64_t n_eq, const int64_t* rowptr, const int* cols,
@@ -450,6 +488,11 @@ extern "C" int sc_newmark_create(sc_newmark** out, int64_t n_eq, const int64_t* 
   g.w = p; p += n_eq;
   g.dinv = p; p += n_eq;
   g.f = p; p += n_eq;
+  for (int k = 0; k < kHistMax; ++k) {
+    g.ah[k] = p;
+    p += n_eq;
+  }
+  g.pred_order = 0;  // adaptive
   h->row_blocks = row_blocks_for(n_eq);
   h->vec_blocks = grid_for(n_eq, 256, 152 * 16);
   g.part = p; p += 4 * (int64_t)(h->row_blocks > h->vec_blocks ? h->row_blocks : h->vec_blocks);
@@ -471,6 +514,7 @@ extern "C" int sc_newmark_create(sc_newmark** out, int64_t n_eq, const int64_t* 
     if ((rc = check(cudaStreamSynchronize(st), "sync"))) break;
     if ((rc = sc_combine(nnz, 1.0, M, 0.5 * dt, C, 0.25 * dt * dt, K, A, st))) break;
     if ((rc = check(cudaMemsetAsync(g.f, 0, sizeof(double) * n_eq, st), "memset f"))) break;
+    if ((rc = check(cudaMemsetAsync(g.ah[0], 0, sizeof(double) * n_eq * kHistMax, st), "memset history"))) break;
     if ((rc = check(cudaMallocAsync((void**)&bad, sizeof(int), st), "malloc"))) break;
     if ((rc = check(cudaMemsetAsync(bad, 0, sizeof(int), st), "memset"))) break;
     k_dinv<<<h->vec_blocks, 256, 0, st>>>(n_eq, rowptr, cols, A, g.dinv, bad);
@@ -503,11 +547,7 @@ extern "C" int sc_newmark_set_force(sc_newmark* h, int n_t, const int64_t* f_ptr
   h->g.f_ptr = n_t > 0 ? f_ptr : nullptr;
   h->g.f_eq = f_eq;
   h->g.f_val = f_val;
-  // graphs bake in the arguments: rebuild lazily
-  if (h->step_exec) cudaGraphExecDestroy(h->step_exec), h->step_exec = nullptr;
-  if (h->step_graph) cudaGraphDestroy(h->step_graph), h->step_graph = nullptr;
-  if (h->init_exec) cudaGraphExecDestroy(h->init_exec), h->init_exec = nullptr;
-  if (h->init_graph) cudaGraphDestroy(h->init_graph), h->init_graph = nullptr;
+  drop_graphs(h);
   return SC_OK;
 }
 
@@ -521,11 +561,20 @@ extern "C" int sc_newmark_set_output(sc_newmark* h, int out_interval, int n_rec,
   h->g.out_v = out_v;
   h->g.out_a = out_a;
   h->g.n_out = n_out;
-  if (h->step_exec) cudaGraphExecDestroy(h->step_exec), h->step_exec = nullptr;
-  if (h->step_graph) cudaGraphDestroy(h->step_graph), h->step_graph = nullptr;
-  if (h->init_exec) cudaGraphExecDestroy(h->init_exec), h->init_exec = nullptr;
-  if (h->init_graph) cudaGraphDestroy(h->init_graph), h->init_graph = nullptr;
+  drop_graphs(h);
   return SC_OK;
+}
+
+// Polynomial order (1..kHistMax; 0: adaptive, the default) of the extrapolated accelerations
+// that start each step's PCG: it changes the iteration count, not the converged answer.
+extern "C" int sc_newmark_set_predictor(sc_newmark* h, int order) {
+  if (!h || order < 0 || order > kHistMax) return SC_BAD_ARG;
+  // only the previous fixed order's entries of the history are current (adaptive keeps all)
+  if (h->g.pred_order > 0 && (order == 0 || order > h->g.pred_order))
+    k_cap_hist<<<1, 1, 0, h->user>>>(h->g.s, h->g.pred_order);
+  h->g.pred_order = order;
+  drop_graphs(h);
+  return check_launch("predictor order");
 }
 
 extern "C" int sc_newmark_initial_acceleration(sc_newmark* h) {

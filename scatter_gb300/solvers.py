@@ -126,6 +126,11 @@ class NewmarkGPU:
     def run(self, t_begin, t_end):
         nat.call("sc_newmark_run", self.h, int(t_begin), int(t_end))
 
+    def set_predictor(self, order):
+        """Order (1..8) of the extrapolated accelerations each step's PCG starts from; 0 (the
+        default) adapts the order to the iteration counts."""
+        nat.call("sc_newmark_set_predictor", self.h, int(order))
+
     def status(self):
         tot = ctypes.c_int64()
         mx = ctypes.c_int()

@@ -101,13 +101,11 @@ def test_eager_mode_matches_graph_mode(cuda):
     assert outs[0][1] == outs[1][1]
 
 
-def test_warm_start_order_changes_iterations_not_the_answer(cuda):
-    """Fixed warm-start orders 1..8 and the adaptive default reach the same displacements
-    (the PCG tolerance), and the adaptive order needs fewer PCG iterations than order 2 on a
-    smooth load history."""
+def _ricker_box():
+    """Box with Lysmer dashpots, Rayleigh damping and a Ricker point load on the top: a smooth
+    load history over 400 steps."""
     from scatter_gb300 import meshgen
     from scatter_gb300.force_external import ricker_table
-    from scatter_gb300.solvers import NodeBlockNewmark
     from scatter_gb300.system_matrix import GenerateMatrix
 
     mats = {"lower": {"density": 2000.0, "Young": 150e6, "poisson": 0.25},
@@ -123,9 +121,13 @@ def test_warm_start_order_changes_iterations_not_the_answer(cuda):
     top = m.top_nodes()
     table = ricker_table(m, int(top[len(top) // 2]), -1e4, 40.0, 0.004, time)
     rec = np.asarray([int(m.eq_nb_dof[m.node_index()[n], 1]) for n in top[::3]], dtype=np.int64)
+    return g, table, rec, dt, n_t
+
+
+def _warm_start_runs(make, orders, table, rec, n_t):
     runs = {}
-    for order in (0, 1, 2, 4, 6, 8):
-        s = NodeBlockNewmark(g, dt)
+    for order in orders:
+        s = make()
         if order:
             s.set_predictor(order)
         s.set_force(table)
@@ -136,8 +138,35 @@ def test_warm_start_order_changes_iterations_not_the_answer(cuda):
         assert rc == 0
         runs[order] = (s.outputs()["u"].copy(), iters)
         s.close()
+    return runs
+
+
+def test_warm_start_order_changes_iterations_not_the_answer(cuda):
+    """Fixed warm-start orders 1..8 and the adaptive default reach the same displacements
+    (the PCG tolerance), and the adaptive order needs fewer PCG iterations than order 2 on a
+    smooth load history."""
+    from scatter_gb300.solvers import NodeBlockNewmark
+
+    g, table, rec, dt, n_t = _ricker_box()
+    runs = _warm_start_runs(lambda: NodeBlockNewmark(g, dt), (0, 1, 2, 4, 6, 8), table, rec, n_t)
     ref = runs[2][0]
     assert np.abs(ref).max() > 0
     for order, (u, _) in runs.items():
         assert rel_l2(u, ref) <= 1e-10, order
     assert runs[0][1] < runs[2][1]
+
+
+def test_csr_warm_start_order_changes_iterations_not_the_answer(cuda):
+    """The CSR loop (scipy matrices, Jacobi-PCG) with the same warm start: every order reaches
+    the node-block loop's displacements to the PCG tolerance, and the adaptive order needs
+    fewer iterations than the linear extrapolation (order 1)."""
+    from scatter_gb300.solvers import NewmarkGPU, NodeBlockNewmark, _device_matrices
+
+    g, table, rec, dt, n_t = _ricker_box()
+    pat, Md, Cd, Kd = _device_matrices(g.M, g.C, g.K)
+    runs = _warm_start_runs(lambda: NewmarkGPU(pat, Md, Cd, Kd, dt), (0, 1, 2, 4, 8), table, rec, n_t)
+    ref = _warm_start_runs(lambda: NodeBlockNewmark(g, dt), (0,), table, rec, n_t)[0][0]
+    assert np.abs(ref).max() > 0
+    for order, (u, _) in runs.items():
+        assert rel_l2(u, ref) <= 1e-10, order
+    assert runs[0][1] < runs[1][1]
