@@ -10,6 +10,7 @@ is one Newmark time step (graph launch: force, predictor, residual, device-side 
 update).  Synthetic seeded inputs; no dataset.
 
     python bench.py [--steps K] [--warmup W] [--gpus N] [--impl gb300|reference]
+    python bench.py --section batched|ragged|adjoint|csr [--dims nx,ny,nz]   # one added workload
 
 Prints one JSON line.  --impl reference times the CPU restatement of the reference path
 (oracle/: numpy assembly + C Newmark/PCG loop on all host threads) on the same workload.
@@ -466,6 +467,51 @@ def ragged_run(k, w, n_meshes=64, seed=4, hexa_edges=(10, 80), tetra_edges=(5, 4
             "arithmetic": "matrix-free: FP32 element products, u and v in FP32 (hi, lo) pairs"}
 
 
+def csr_run(k, w, dims=(60, 30, 40, 0.5)):
+    """The Newmark loop on scipy matrices (the CSR layout, Jacobi-PCG with the adaptive warm
+    start): a box of the benchmark's physics (default 30 x 15 x 20 m, hexa8 at 0.5 m).  The
+    standalone SpMV timing runs first, before any graph launch, so a profiler can capture it."""
+    import ctypes
+
+    import torch
+
+    from scatter_gb300 import _native as nat
+    from scatter_gb300.solvers import NewmarkGPU, _device_matrices
+    from scatter_gb300.system_matrix import GenerateMatrix
+
+    model, load, tg, rec_eq = workload(dims)
+    table = force_table(model, load, tg)
+    g = GenerateMatrix(model.number_eq, 2)
+    g.generate_stiffness_and_mass(model, MATERIALS)
+    g.absorbing_boundaries(model, MATERIALS, SETTINGS["absorbing_BC"], SETTINGS["absorbing_BC_stiff"])
+    g.damping_Rayleigh(SETTINGS["damping"])
+    pat, Md, Cd, Kd = _device_matrices(g.M, g.C, g.K)
+    s = NewmarkGPU(pat, Md, Cd, Kd, DT)
+    ms, nb = ctypes.c_float(), ctypes.c_int64()
+    nat.call("sc_newmark_time_spmv", s.h, 20, ctypes.byref(ms), ctypes.byref(nb))
+    k = max(1, min(k, len(tg) - 1 - w))
+    s.set_force(table)
+    s.set_output(1, rec_eq, len(tg), what=("v",))
+    s.initial_acceleration()
+    s.run(0, w)
+    _, it0, _ = s.status()
+    e0, e1 = _events()
+    e0.record()
+    s.run(w, w + k)
+    e1.record()
+    torch.cuda.synchronize()
+    rc, it1, it_max = s.status()
+    step_ms = e0.elapsed_time(e1) / k
+    s.close()
+    n = model.number_eq
+    return {"value": n * k / (step_ms / 1e3), "unit": "DOF-steps/s", "n_eq": n, "nnz": int(pat.nnz), "steps": k,
+            "ms_per_step": step_ms, "pcg_iterations_per_step": (it1 - it0) / k, "max_iterations": it_max,
+            "status": rc, "spmv_us": ms.value * 1e3, "spmv_bytes": nb.value,
+            "spmv_gbs": nb.value / ms.value / 1e6,
+            "workload": f"box {dims[0]}x{dims[1]}x{dims[2]} hexa8 {dims[3]} m, benchmark physics, scipy CSR "
+                        "matrices, Jacobi-PCG"}
+
+
 def adjoint_run(n_steps=4000, checkpoint=200, n_fd=20):
     """Differentiation workload: misfit of vertical surface velocities at 25 receivers w.r.t.
     per-element E and rho, box 20 x 10 x 20 m (x / y vertical / z) hexa8 at 0.5 m (32,000
@@ -681,7 +727,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-realisation batched measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost and FD measurement")
     ap.add_argument("--no-ragged", action="store_true", help="skip the 64-mesh ragged batching measurement")
-    ap.add_argument("--section", default="all", choices=["all", "batched", "adjoint", "ragged"],
+    ap.add_argument("--section", default="all", choices=["all", "batched", "adjoint", "ragged", "csr"],
                     help="run one added workload alone and print its JSON (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -699,6 +745,9 @@ def main():
             out = batched_run(min(args.steps, 2990), args.warmup)
         elif args.section == "ragged":
             out = ragged_run(min(args.steps, 1990), args.warmup)
+        elif args.section == "csr":
+            dims = tuple(int(x) for x in args.dims.split(",")) + (0.5,) if args.dims else (60, 30, 40, 0.5)
+            out = csr_run(args.steps, args.warmup, dims)
         else:
             out = adjoint_run(n_steps=args.steps, checkpoint=min(200, args.steps), n_fd=0 if args.no_cpu else 20)
         print(json.dumps({"section": args.section, **out}))
