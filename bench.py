@@ -504,7 +504,7 @@ def csr_run(k, w, dims=(60, 30, 40, 0.5)):
     step_ms = e0.elapsed_time(e1) / k
     s.close()
     n = model.number_eq
-    return {"value": n * k / (step_ms / 1e3), "unit": "DOF-steps/s", "n_eq": n, "nnz": int(pat.nnz), "steps": k,
+    return {"value": n / (step_ms / 1e3), "unit": "DOF-steps/s", "n_eq": n, "nnz": int(pat.nnz), "steps": k,
             "ms_per_step": step_ms, "pcg_iterations_per_step": (it1 - it0) / k, "max_iterations": it_max,
             "status": rc, "spmv_us": ms.value * 1e3, "spmv_bytes": nb.value,
             "spmv_gbs": nb.value / ms.value / 1e6,

@@ -23,7 +23,20 @@
 
 namespace sc {
 
-constexpr int kRowThreads = 256;  // 8 warps, one row per warp
+constexpr int kRowThreads = 256;  // 8 warps
+// A row takes kRowLanes lanes (a warp takes kRowsPerWarp rows at once): on GB300 an FP64 warp
+// instruction costs ~16 SM cycles, and with a whole warp per row the 5-step FP64 warp
+// reduction and the partly idle last FMA pass cost more than the row's own FMAs (an 81-entry
+// hexa8 row: 9 FP64 warp instructions; with 4 lanes about 3).  The 4 lanes of a row read 32
+// contiguous bytes of values per pass.
+constexpr int kRowLanes = 4, kRowsPerWarp = 32 / kRowLanes;
+
+// sum over the kRowLanes lanes of a row (all 32 lanes call it); every lane of the row gets it
+__device__ __forceinline__ double row_sum(double v) {
+#pragma unroll
+  for (int o = 1; o < kRowLanes; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
 
 struct NmScalars {
   double rz, pw, rr, bb, alpha, beta, tol2;
@@ -112,24 +125,29 @@ __global__ void k_predict(NmArgs g) {
 __global__ void __launch_bounds__(kRowThreads) k_residual(NmArgs g, const double* __restrict__ Op, int mode,
                                                           cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, sub = lane % kRowLanes;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const double* __restrict__ vp = mode == 0 ? g.vp : g.v;
   const double* __restrict__ up = mode == 0 ? g.up : g.u;
   double prz = 0, prr = 0, pbb = 0;
-  for (int64_t row = gw; row < g.n; row += nw) {
-    const int64_t k0 = g.rowptr[row], k1 = g.rowptr[row + 1];
+  // the loop bound depends on the warp only, so all 32 lanes reach the shuffles
+  for (int64_t rb = gw * kRowsPerWarp; rb < g.n; rb += nw * kRowsPerWarp) {
+    const int64_t row = rb + lane / kRowLanes;
+    const bool live = row < g.n;
     double sr = 0.0, sa = 0.0;
-    for (int64_t k = k0 + lane; k < k1; k += 32) {
-      const int c = g.cols[k];
-      sr = fma(g.C[k], vp[c], sr);
-      sr = fma(g.K[k], up[c], sr);
-      if (mode == 0) sa = fma(Op[k], g.w[c], sa);
+    if (live) {
+      const int64_t k0 = g.rowptr[row], k1 = g.rowptr[row + 1];
+      for (int64_t k = k0 + sub; k < k1; k += kRowLanes) {
+        const int c = g.cols[k];
+        sr = fma(g.C[k], vp[c], sr);
+        sr = fma(g.K[k], up[c], sr);
+        if (mode == 0) sa = fma(Op[k], g.w[c], sa);
+      }
     }
-    sr = warp_sum(sr);
-    sa = warp_sum(sa);
-    if (lane == 0) {
+    sr = row_sum(sr);
+    sa = row_sum(sa);
+    if (live && sub == 0) {
       const double rhs = g.f[row] - sr;
       const double r = rhs - sa;
       const double z = g.dinv[row] * r;
@@ -171,16 +189,20 @@ template <bool kInGraph>
 __global__ void __launch_bounds__(kRowThreads) k_spmv(NmArgs g, const double* __restrict__ Op,
                                                       cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, sub = lane % kRowLanes;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   double ppw = 0.0;
-  for (int64_t row = gw; row < g.n; row += nw) {
-    const int64_t k0 = g.rowptr[row], k1 = g.rowptr[row + 1];
+  for (int64_t rb = gw * kRowsPerWarp; rb < g.n; rb += nw * kRowsPerWarp) {
+    const int64_t row = rb + lane / kRowLanes;
+    const bool live = row < g.n;
     double s = 0.0;
-    for (int64_t k = k0 + lane; k < k1; k += 32) s = fma(__ldcs(Op + k), g.p[__ldcs(g.cols + k)], s);
-    s = warp_sum(s);
-    if (lane == 0) {
+    if (live) {
+      const int64_t k0 = g.rowptr[row], k1 = g.rowptr[row + 1];
+      for (int64_t k = k0 + sub; k < k1; k += kRowLanes) s = fma(__ldcs(Op + k), g.p[__ldcs(g.cols + k)], s);
+    }
+    s = row_sum(s);
+    if (live && sub == 0) {
       g.w[row] = s;
       ppw += g.p[row] * s;
     }
@@ -440,8 +462,9 @@ void drop_graphs(sc_newmark* h) {
 }
 
 unsigned row_blocks_for(int64_t n) {
-  // one row per warp, 8 warps per block, grid-stride; 16 blocks of 256 per SM
-  int64_t b = (n + 7) / 8;
+  // kRowsPerWarp rows per warp, 8 warps per block, grid-stride; at most 16 blocks of 256 per SM
+  const int64_t rows_per_block = (int64_t)kRowsPerWarp * (kRowThreads / 32);
+  int64_t b = (n + rows_per_block - 1) / rows_per_block;
   const int64_t cap = 152 * 16;
   if (b > cap) b = cap;
   if (b < 1) b = 1;
