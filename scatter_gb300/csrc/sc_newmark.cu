@@ -530,8 +530,6 @@ extern "C" int sc_newmark_create(sc_newmark** out, int64_t n_eq, const int64_t* 
     if ((rc = check(cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking), "stream"))) break;
     if ((rc = check(cudaStreamCreateWithFlags(&h->cap2, cudaStreamNonBlocking), "stream"))) break;
     // A = M + dt/2 C + dt^2/4 K on the shared pattern
-    const int64_t nnz_dummy = 0;
-    (void)nnz_dummy;
     int64_t nnz = 0;
     if ((rc = check(cudaMemcpyAsync(&nnz, rowptr + n_eq, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "nnz"))) break;
     if ((rc = check(cudaStreamSynchronize(st), "sync"))) break;
