@@ -2,8 +2,7 @@
 import numpy as np
 import pytest
 
-from helpers import (case, element_coords, element_props, full_field, golden_csr, model_ns, npz, oracle_system,
-                     pattern_hash, rel_l2)
+from helpers import full_field, golden_csr, model_ns, npz, oracle_system, pattern_hash, rel_l2
 
 pytestmark = pytest.mark.gpu
 

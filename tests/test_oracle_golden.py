@@ -8,8 +8,7 @@ histories.
 import numpy as np
 import pytest
 
-from helpers import (GOLDEN, case, element_coords, element_props, full_field, golden_csr, golden_load_table, npz,
-                     oracle_system, pattern_hash, rel_l2)
+from helpers import case, full_field, golden_csr, golden_load_table, npz, oracle_system, pattern_hash, rel_l2
 from oracle import elements as el
 from oracle import loads, newmark
 from oracle.assembly import rayleigh_coefficients
