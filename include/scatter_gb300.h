@@ -174,8 +174,8 @@ int sc_newmark_set_output(sc_newmark* h, int out_interval, int n_rec, const int*
 int sc_newmark_initial_acceleration(sc_newmark* h);
 /* run steps t = t_begin .. t_end-1 -> states t+1; asynchronous (graph launches) */
 int sc_newmark_run(sc_newmark* h, int t_begin, int t_end);
-/* Order of the warm start, as sc_nb_set_predictor: 1..8 fixed, 0 adaptive (the default);
- * 1..8 then 0 keeps the history entries that are current. */
+/* Warm start of each step (no reference counterpart), as sc_nb_set_predictor: order 1..8
+ * fixed, 0 adaptive (the default); 1..8 then 0 keeps the history entries that are current. */
 int sc_newmark_set_predictor(sc_newmark* h, int order);
 /* synchronous: CG status of the run so far (SC_OK / SC_NOT_CONVERGED / SC_BREAKDOWN),
  * total and maximum CG iterations per step */
