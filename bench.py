@@ -150,11 +150,12 @@ def cpu_baseline_run(n, rowptr, cols, M, C, K, table, rec_eq, target_s=20.0, max
     if max_steps:
         steps = min(steps, max_steps)
     t0 = time.perf_counter()
-    s.run(1, steps, table.f_ptr, table.f_eq, table.f_val, rec_eq)
+    _, its = s.run(1, steps, table.f_ptr, table.f_eq, table.f_val, rec_eq)
     el = time.perf_counter() - t0
     return {"value": n * steps / el, "unit": "DOF-steps/s", "cores": cpu.threads(), "kind": "port",
             "sample": f"{steps} Newmark steps (steps 1..{steps}) of the same workload from rest, Jacobi-PCG "
-                      f"per step to rtol 1e-12, {cpu.threads()} OpenMP threads, {el:.1f} s"}
+                      f"per step to rtol 1e-12 started from the previous acceleration ({its / steps:.1f} "
+                      f"iterations per step), {cpu.threads()} OpenMP threads, {el:.1f} s"}
 
 
 def dist_env():
@@ -697,13 +698,14 @@ def run_reference(args):
         s.run(1, w_steps - 1, table.f_ptr, table.f_eq, table.f_val, rec_eq)  # (first step, step count)
     steps = int(max(2, min(args.steps, budget / max(one, 1e-6))))
     t1 = time.perf_counter()
-    s.run(w_steps, steps, table.f_ptr, table.f_eq, table.f_val, rec_eq)
+    _, its = s.run(w_steps, steps, table.f_ptr, table.f_eq, table.f_val, rec_eq)
     el_s = time.perf_counter() - t1
     value = n * steps / el_s
     cb = {"value": value, "unit": "DOF-steps/s", "cores": cpu.threads(), "kind": "port",
           "sample": f"{steps} Newmark steps ({w_steps}..{w_steps + steps - 1}) of the same workload after {w_steps} "
                     f"untimed steps from rest; oracle numpy assembly "
-                    f"({setup:.0f} s, untimed) + C Jacobi-PCG loop on {cpu.threads()} threads, {el_s:.1f} s"}
+                    f"({setup:.0f} s, untimed) + C Jacobi-PCG loop started from the previous acceleration "
+                    f"({its / steps:.1f} iterations per step) on {cpu.threads()} threads, {el_s:.1f} s"}
     print(json.dumps({"metric": METRIC, "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": steps,
                       "warmup": w_steps, "ms_per_step": el_s / steps * 1e3, "higher_is_better": True, "scaling": "weak",
                       "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded structured mesh)",
