@@ -10,7 +10,6 @@ not needed).
 """
 import os
 import pickle
-import struct
 from collections import defaultdict
 
 import numpy as np
@@ -105,6 +104,7 @@ class Write:
 
 
 def _write_vtk(path, title, binary, X, cells, cell_type, point_vectors, cell_scalars):
+    """Legacy VTK unstructured grid; binary blocks are big-endian, as the format requires."""
     n, nc = len(X), len(cells)
     npe = cells.shape[1]
     with open(path, "wb") as f:
@@ -157,4 +157,3 @@ def _write_vtk(path, title, binary, X, cells, cell_type, point_vectors, cell_sca
             else:
                 for v in a:
                     line(repr(float(v)))
-    _ = struct  # binary layout is big-endian as legacy VTK requires
