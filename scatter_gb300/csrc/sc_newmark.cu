@@ -11,9 +11,9 @@
 // sc_common.cuh, shared with the node-block solver).
 //
 // Execution: one CUDA graph per step: [force, predict, residual] -> WHILE{spmv, update,
-// direction} -> [finalize, record, advance].  The WHILE node is a graph conditional whose value the residual
-// and update kernels set on the device (converged / iteration cap / breakdown), so a step
-// costs exactly the iterations it needs with no host round trip.  Reductions are per-block
+// direction} -> [finalize, record, advance].  The WHILE node is a graph conditional whose
+// value the residual and update kernels set on the device (converged / iteration cap /
+// breakdown), so a step costs exactly the iterations it needs with no host round trip.  Reductions are per-block
 // partials summed by the last block to finish (ticket counter, no spin-waits), in a fixed
 // order, so every run is bitwise reproducible.  Matrices are CSR over the reference's
 // equation numbering with a shared element-graph pattern.
