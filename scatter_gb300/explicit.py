@@ -58,6 +58,9 @@ class ExplicitLumped:
         if not isinstance(M, GenerateMatrix):
             raise TypeError("the explicit GPU scheme takes the GenerateMatrix that assembled M, C, K")
         g = M
+        if np.any(self.u[0]) or np.any(self.v[0]):
+            # the central-difference state is (u_n, v_{n-1/2}): it starts from rest only
+            raise NotImplementedError("the explicit GPU scheme starts from rest (u[0] = v[0] = 0)")
         dt = self.time[1] - self.time[0]
         if self.check_cfl:
             dtc = critical_time_step(g)

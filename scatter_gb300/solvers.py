@@ -6,6 +6,7 @@ the reference uses it:
     numerical = NewmarkExplicit()
     numerical.output_interval = k                       # scatter.py:137
     numerical.initialise(n_eq, time)                    # scatter.py:138
+    numerical.u[0, :], numerical.v[0, :] = u0, v0       # optional initial state (rose_utils.py:53-58)
     numerical.update_rhs_at_time_step_func = F.update_load_at_t   # scatter.py:151
     numerical.update(0)                                 # scatter.py:158
     numerical.calculate(M, C, K, F0, 0, len(time) - 1)  # scatter.py:159
@@ -120,6 +121,12 @@ class NewmarkGPU:
                  *(dv.ptr(self.out[k]) for k in ("u", "v", "a")), int(n_out))
         self.n_out, self.n_rec = int(n_out), nr
 
+    def set_state(self, u0, v0):
+        """Initial displacement and velocity (equation order) in place of rest; before
+        initial_acceleration(), which then solves M a0 = f(0) - C v0 - K u0."""
+        self.u.copy_(dv.to_dev(np.asarray(u0, dtype=float), torch.float64))
+        self.v.copy_(dv.to_dev(np.asarray(v0, dtype=float), torch.float64))
+
     def initial_acceleration(self):
         nat.call("sc_newmark_initial_acceleration", self.h)
 
@@ -195,6 +202,7 @@ class NodeBlockNewmark:
         self.u = dv.zeros(self.n_s, torch.float64)
         self.v = dv.zeros(self.n_s, torch.float64)
         self.a = dv.zeros(self.n_s, torch.float64)
+        self.u0_eq = self.v0_eq = None  # initial conditions other than rest (set_state)
         nnzb = int(g.adj.numel())
         wsb = nat.value("sc_nb_workspace_bytes", N, D, nnzb)
         self.ws = dv.empty(wsb, torch.uint8)
@@ -237,14 +245,25 @@ class NodeBlockNewmark:
                  *(dv.ptr(self.out[k]) for k in ("u", "v", "a")), int(n_out))
         self.n_out, self.n_rec = int(n_out), nr
 
+    def set_state(self, u0, v0):
+        """Initial displacement and velocity in equation order (the reference solver's
+        u[0, :] and v[0, :]) in place of rest; before initial_acceleration()."""
+        self.u0_eq, self.v0_eq = np.asarray(u0, dtype=float), np.asarray(v0, dtype=float)
+        free = self.eq2slot >= 0
+        self.u[self.eq2slot[free]] = dv.to_dev(self.u0_eq, torch.float64)[free]
+        self.v[self.eq2slot[free]] = dv.to_dev(self.v0_eq, torch.float64)[free]
+
     def initial_acceleration(self):
         """a0 = M^-1 (f(0) - C v0 - K u0); zero for a start from rest without load at t = 0
         (pulse, heaviside, moving loads all start at 0), else solved with the CSR path."""
         t = self.table
-        if t.f_ptr[1] > t.f_ptr[0] and np.any(t.f_val[t.f_ptr[0]:t.f_ptr[1]] != 0):
+        loaded = t.f_ptr[1] > t.f_ptr[0] and np.any(t.f_val[t.f_ptr[0]:t.f_ptr[1]] != 0)
+        if loaded or self.u0_eq is not None:
             g = self.g
             csr = NewmarkGPU(g.pattern, g.M_d, g.C_d, g.K_d, self.dt)
             csr.set_force(t)
+            if self.u0_eq is not None:
+                csr.set_state(self.u0_eq, self.v0_eq)
             csr.initial_acceleration()
             a_eq = csr.a
             free = self.eq2slot >= 0
@@ -362,6 +381,10 @@ class NewmarkExplicit:
                 table = ForceTable.from_callback(lambda t: F0, n_t, n)
         rec = np.arange(n) if self.receivers is None else np.asarray(self.receivers)
         n_out = len(range(0, n_t, self.output_interval))
+        # the reference solver's u[0, :] and v[0, :] are writable initial conditions
+        ic = None
+        if getattr(self, "u", None) is not None and (np.any(self.u[0]) or np.any(self.v[0])):
+            ic = (np.array(self.u[0], dtype=float), np.array(self.v[0], dtype=float))
         attempts = ["fsai", "csr"] if (isinstance(M, GenerateMatrix) and self.layout == "node-block"
                                        and M.adj_ptr is not None) else ["csr"]
         for kind in attempts:
@@ -371,6 +394,8 @@ class NewmarkExplicit:
                 solver = NodeBlockNewmark(M, dt, self.rtol, self.max_iter, precond=kind, spmv=self.spmv)
             solver.set_force(table)
             solver.set_output(self.output_interval, rec, n_out)
+            if ic is not None:
+                solver.set_state(*ic)
             solver.initial_acceleration()
             solver.run(t_start_idx, t_end_idx)
             rc, tot, mx = solver.status()
