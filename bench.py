@@ -57,6 +57,15 @@ def workload(dims=DIMS):
     return model, load, time_grid, rec_eq
 
 
+def workload_config(model, dims=DIMS):
+    """The workload's description, identical in both arms' lines."""
+    return {"workload": "plain Newmark FP64, box 60x40x30 m hexa8 0.5 m (120x80x60 el), 2 layers, "
+                        "Lysmer sides+base, moving 100 kN at 40 km/h, dt 5e-5" if dims == DIMS
+            else f"profiling case: box {dims[0]}x{dims[1]}x{dims[2]} hexa8 0.5 m, same physics",
+            "n_eq": int(model.number_eq), "elements": int(len(model.elem)), "receivers": N_REC,
+            "parallelism": "replicas", "l2": "inputs larger than L2 (matrices 5.1 GB), no flush"}
+
+
 def force_table(model, load, time_grid):
     from scatter_gb300.force_external import Force
 
@@ -138,24 +147,38 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline_run(n, rowptr, cols, M, C, K, table, rec_eq, target_s=20.0, max_steps=None):
-    """Oracle C Newmark/PCG on the host cores, bounded to ~target_s of work."""
+def cpu_baseline_run(n, rowptr, cols, M, C, K, table, rec_eq, target_s=20.0, max_steps=None, dt=DT):
+    """Oracle C Newmark/PCG on the host cores, bounded to ~target_s of work.  Returns the
+    baseline record and the receiver velocities after steps 1 .. steps + 1 (from rest)."""
     from oracle import cpu
 
-    s = cpu.NewmarkCPU.from_csr(n, rowptr, cols, M, C, K, DT)
+    s = cpu.NewmarkCPU.from_csr(n, rowptr, cols, M, C, K, dt)
     t0 = time.perf_counter()
-    s.run(0, 1, table.f_ptr, table.f_eq, table.f_val, rec_eq)
+    v1, _ = s.run(0, 1, table.f_ptr, table.f_eq, table.f_val, rec_eq)
     t1 = time.perf_counter() - t0
     steps = int(max(2, min(200, target_s / max(t1, 1e-6))))
     if max_steps:
         steps = min(steps, max_steps)
     t0 = time.perf_counter()
-    _, its = s.run(1, steps, table.f_ptr, table.f_eq, table.f_val, rec_eq)
+    vs, its = s.run(1, steps, table.f_ptr, table.f_eq, table.f_val, rec_eq)
     el = time.perf_counter() - t0
-    return {"value": n * steps / el, "unit": "DOF-steps/s", "cores": cpu.threads(), "kind": "port",
-            "sample": f"{steps} Newmark steps (steps 1..{steps}) of the same workload from rest, Jacobi-PCG "
-                      f"per step to rtol 1e-12 started from the previous acceleration ({its / steps:.1f} "
-                      f"iterations per step), {cpu.threads()} OpenMP threads, {el:.1f} s"}
+    rec = {"value": n * steps / el, "unit": "DOF-steps/s", "cores": cpu.threads(), "kind": "port",
+           "sample": f"{steps} Newmark steps (steps 1..{steps}) of the same workload from rest, Jacobi-PCG "
+                     f"per step to rtol 1e-12 started from the previous acceleration ({its / steps:.1f} "
+                     f"iterations per step), {cpu.threads()} OpenMP threads, {el:.1f} s"}
+    return rec, np.vstack([v1, vs])
+
+
+PARITY_RTOL = 1e-8  # receiver velocities, GPU loop vs the CPU port from rest (both PCG to rtol 1e-12)
+
+
+def parity_record(v_gpu, v_cpu):
+    """Relative L2 of the receiver velocities over the steps both legs ran (rows = steps 1..)."""
+    k = min(len(v_gpu), len(v_cpu))
+    a, b = v_gpu[:k], v_cpu[:k]
+    rel = float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    return {"rel_l2": rel, "steps": k, "receivers": int(a.shape[1]), "rtol": PARITY_RTOL, "ok": rel <= PARITY_RTOL,
+            "against": "the CPU port (oracle C Newmark/Jacobi-PCG, FP64) on the same workload from rest"}
 
 
 def dist_env():
@@ -230,18 +253,20 @@ def run_gb300(args):
     peak, peak_kind = peaks()
     achieved = bytes_spmv / (ms_spmv * 1e-3) / 1e9
     traffic = profile_traffic()
+    v_gpu = solver.outputs()["v"][1:W + K_steps + 1]  # receiver velocities after steps 1 .. W + K
+    solver.close()
 
-    # end to end through the solver API: each step copies its force entries host->device from
-    # pinned memory and reads the step's receiver velocities back to pinned host memory
-    e2e = None if args.no_e2e else e2e_run(solver, table, rec_eq, W + K_steps,
-                                          min(K_steps, len(time_grid) - 1 - (W + K_steps)), n)
+    # end to end through the drop-in call: the same steps as the timed region, from a fresh
+    # solver given the same warm-up
+    e2e = None if args.no_e2e else e2e_run(g, table, time_grid, rec_eq, W, K_steps, n)
+    if e2e is not None:
+        e2e["cg_iters_per_step_device_leg"] = iters / K_steps
     # the added explicit scheme (lumped mass, one fused kernel per step) on the same model
     explicit = explicit_run(g, table, rec_eq, K_steps, W, n)
     host_csr = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         host_csr = (g.pattern.rowptr.cpu().numpy(), g.pattern.cols.cpu().numpy(),
                     *(x.cpu().numpy() for x in (g.M_d, g.C_d, g.K_d)))
-    solver.close()
     nnz = int(g.pattern.nnz)
     del g
     batched = None if args.no_batched else batched_run(min(K_steps, 2990), W)
@@ -251,16 +276,11 @@ def run_gb300(args):
     out = {"metric": METRIC, "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": K_steps, "warmup": W,
            "ms_per_step": ms / K_steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f64", "data": "synthetic (seeded structured mesh, moving point load)",
-           "config": {"workload": "plain Newmark FP64, box 60x40x30 m hexa8 0.5 m (120x80x60 el), 2 layers, "
-                                  "Lysmer sides+base, moving 100 kN at 40 km/h, dt 5e-5" if not args.dims
-                      else f"profiling case: box {args.dims} hexa8 0.5 m, same physics",
-                      "n_eq": n, "nnz": nnz, "elements": int(len(model.elem)), "receivers": len(rec_eq),
-                      "parallelism": f"replicas x{ws}",
-                      "l2": "inputs larger than L2 (CSR values+cols 5.1 GB), no flush",
-                      "solver": "Newmark beta=1/4 gamma=1/2; per step PCG (FSAI preconditioner, FP16 factor), "
-                                "warm start extrapolating the accelerations, order adapted on the device, rtol 1e-12; node-block operator, SpMV products in FP32 "
-                                "pairs, residual, dot products and state FP64"},
-           "cg_iters_per_step": iters / K_steps, "cg_iters_max": it_max,
+           "config": workload_config(model, dims),
+           "solver": "Newmark beta=1/4 gamma=1/2; per step PCG (FSAI preconditioner, FP16 factor), warm start "
+                     "extrapolating the accelerations, order adapted on the device, rtol 1e-12; node-block operator, "
+                     "SpMV products in FP32 pairs, residual, dot products and state FP64",
+           "nnz": nnz, "cg_iters_per_step": iters / K_steps, "cg_iters_max": it_max,
            "setup_s": {"host_mesh_and_loads": round(t_host, 2), "gpu_assembly_lysmer_rayleigh": round(t_assembly, 3),
                        "gpu_solver_setup_fsai": round(t_solver_setup, 3)},
            "fsai_fallback_rows": solver.fsai_fallback_rows,
@@ -271,13 +291,17 @@ def run_gb300(args):
                         "traffic": traffic, "bytes_per_launch": bytes_spmv, "ms_per_launch": ms_spmv},
            "clocks": clk.summary(), "e2e": e2e, "explicit_lumped": explicit, "batched": batched,
            "ragged": ragged, "adjoint": adjoint}
-    # CPU baseline (rank 0 only, N = 1): the oracle's C loop on the host cores
+    # CPU baseline (rank 0 only, N = 1): the oracle's C loop on the host cores, from rest, and
+    # the GPU loop's receiver velocities over the same steps checked against it
     if rank == 0 and ws == 1 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline_run(n, *host_csr, table, rec_eq, target_s=args.cpu_seconds)
+        out["cpu_baseline"], v_cpu = cpu_baseline_run(n, *host_csr, table, rec_eq, target_s=args.cpu_seconds)
+        out["parity"] = parity_record(v_gpu, v_cpu)
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:
         torch.distributed.destroy_process_group()
+    if "parity" in out and not out["parity"]["ok"]:
+        raise SystemExit(f"parity failed: receiver velocities differ from the CPU port by {out['parity']['rel_l2']:.3e}")
 
 
 def explicit_run(g, table, rec_eq, k, w, n):
@@ -371,41 +395,56 @@ def batched_run(k, w, R=256):
     e1.record()
     torch.cuda.synchronize()
     ms_b = e0.elapsed_time(e1)
-    vb = b.velocities()[: w + k + 1, :, 0]
-    y0 = dv.host(young[:, 0]).astype(float)
+    vb_all = b.velocities()[: w + k + 1]  # [step, receiver, realisation]
+    young_h = dv.host(young).astype(float)
     b.close()
     del b
     n_el = len(m.elem)
-    g = GenerateMatrix(n, SETTINGS["int_order"])
-    g.generate_stiffness_and_mass(m, None, element_props=(y0, np.full(n_el, nu), np.full(n_el, rho)))
-    g.absorbing_boundaries(m, None, SETTINGS["absorbing_BC"], SETTINGS["absorbing_BC_stiff"])
-    g.damping_Rayleigh(SETTINGS["damping"])
-    s = NodeBlockNewmark(g, DT, precond="jacobi")
-    s.set_force(table)
-    s.set_output(1, rec_eq, n_t, what=("v",))
-    single_tpr, _ = s.tune_explicit()  # the single solve at its own best shape
-    s.run_explicit(0, w)
-    torch.cuda.synchronize()
-    e0, e1 = _events()
-    e0.record()
-    s.run_explicit(w, w + k)
-    e1.record()
-    torch.cuda.synchronize()
-    ms_s = e0.elapsed_time(e1)
-    vs = dv.host(s.out["v"]).reshape(n_t, len(rec_eq))[: w + k + 1]
-    s.close()
-    rel = float(np.linalg.norm(vb - vs) / max(np.linalg.norm(vs), 1e-300))
+
+    def single_run(r, timed):
+        """Realisation r through the plain FP64-class explicit GPU path (its own assembly)."""
+        g = GenerateMatrix(n, SETTINGS["int_order"])
+        g.generate_stiffness_and_mass(m, None, element_props=(young_h[:, r], np.full(n_el, nu), np.full(n_el, rho)))
+        g.absorbing_boundaries(m, None, SETTINGS["absorbing_BC"], SETTINGS["absorbing_BC_stiff"])
+        g.damping_Rayleigh(SETTINGS["damping"])
+        s = NodeBlockNewmark(g, DT, precond="jacobi")
+        s.set_force(table)
+        s.set_output(1, rec_eq, n_t, what=("v",))
+        tpr = s.tune_explicit()[0] if timed else None  # the single solve at its own best shape
+        s.run_explicit(0, w)
+        torch.cuda.synchronize()
+        e0, e1 = _events()
+        e0.record()
+        s.run_explicit(w, w + k)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        vs = dv.host(s.out["v"]).reshape(n_t, len(rec_eq))[: w + k + 1]
+        s.close()
+        return vs, ms, tpr
+
+    # the checked realisations: eight spread over the batch, the first one timed
+    picks = np.unique(np.linspace(0, R - 1, min(8, R)).round().astype(int))
+    rels = {}
+    for r in picks:
+        vs, ms, tpr = single_run(int(r), r == picks[0])
+        if r == picks[0]:
+            ms_s, single_tpr = ms, tpr
+        vb = vb_all[:, :, r]
+        rels[int(r)] = float(np.linalg.norm(vb - vs) / max(np.linalg.norm(vs), 1e-300))
     vb_rate = n * R * k / (ms_b / 1e3)
     single = n * k / (ms_s / 1e3)
     return {"value": vb_rate, "unit": "DOF-steps/s", "single_solve": single, "speedup_vs_single": vb_rate / single,
             "realisations": R, "n_eq": n, "elements": n_el, "steps": k, "warmup": w, "ms_per_step": ms_b / k,
-            "single_ms_per_step": ms_s / k, "rel_l2_vs_fp64_realisation0": rel,
+            "single_ms_per_step": ms_s / k, "rel_l2_vs_fp64_max": max(rels.values()),
+            "rel_l2_vs_fp64": rels, "rel_l2_rtol": 1e-5,
             "tuned_shape": {"kernel": "uniform hexa8 grid (k_batch_step_hex8g)" if grid_kernel else
                             "incidence lists (k_batch_step)", "realisations_per_thread": rpt,
                             "threads_per_block": tpb, "tuned_ms": tuned_ms},
             "workload": "256 log-normal E realisations, box 40x20x10 m hexa8 0.5 m, Lysmer, Ricker 20 Hz, dt 5e-5",
             "single": "plain FP64-class explicit GPU path (node-block graph, threads per row tuned: "
-                      f"{single_tpr}), realisation 0, same steps"}
+                      f"{single_tpr}), realisation 0 timed, same steps; receiver velocities of realisations "
+                      f"{[int(r) for r in picks]} checked against their own single solves"}
 
 
 def ragged_run(k, w, n_meshes=64, seed=4, hexa_edges=(10, 80), tetra_edges=(5, 40)):
@@ -597,39 +636,56 @@ def adjoint_run(n_steps=4000, checkpoint=200, n_fd=20):
                       "sc_nb_adjoint call (forward with checkpoints, recompute, backward, graph set-up, copies)"}
 
 
-def e2e_run(solver, table, rec_eq, t0, k, n):
+def e2e_run(g, table, time_grid, rec_eq, w, k, n):
+    """The metric end to end through the drop-in call, over the same steps as the timed region.
+
+    A fresh solver is driven as the reference drives PuggleSolvers' NewmarkExplicit
+    (scatter/scatter.py:121-159): ``calculate(M, C, K, F, t0, t1)``, with the GenerateMatrix
+    passed for M, C and K (the form this package's scatter() uses; the scipy matrices it
+    hands out reach the same solver, but downloading three 141.7 M-entry matrices to the host
+    is set-up cost outside this metric).  The untimed first call (steps 0 .. w)
+    builds the solver and runs the same warm-up as the device-timed leg; the timed region is
+    then k calls of one step each, w .. w + k, each copying that step's force values host ->
+    device from pinned memory and its receiver outputs (u, v, a) device -> host into the
+    solver's host arrays before it returns."""
     import torch
+
+    from scatter_gb300.solvers import NewmarkExplicit
 
     if k <= 0:
         return None
-    p, e, v = solver._keep_force
-    host_eq = e.cpu().pin_memory()  # slot indices of the force entries, as the solver reads them
-    host_val = torch.from_numpy(table.f_val).pin_memory()
-    out_v = solver.out["v"].view(solver.n_out, solver.n_rec)
-    host_out = torch.empty((k, solver.n_rec), dtype=torch.float64).pin_memory()
-    ptr = table.f_ptr
-    h2d = 0
+    M = C = K = g
+    s = NewmarkExplicit()
+    s.output_interval = 1
+    s.initialise(n, time_grid)
+    s.force_table = table
+    s.receivers = rec_eq
+    s.stream_force = True
+    s.update(0)
+    s.calculate(M, C, K, None, 0, w)
+    dev = s.device_solver
+    rc, it_w, _ = dev.status()
+    h2d0 = dev.force.h2d_bytes
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     wall0 = time.perf_counter()
     ev0.record()
-    for s in range(k):
-        t = t0 + s
-        a, b = int(ptr[t + 1]), int(ptr[t + 2]) if t + 2 < len(ptr) else int(ptr[t + 1])
-        if b > a:
-            e[a:b].copy_(host_eq[a:b], non_blocking=True)
-            v[a:b].copy_(host_val[a:b], non_blocking=True)
-            h2d += (b - a) * 12
-        solver.run(t, t + 1)
-        host_out[s].copy_(out_v[t + 1], non_blocking=True)
+    for t in range(w, w + k):
+        s.calculate(M, C, K, None, t, t + 1)
     ev1.record()
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     ms = ev0.elapsed_time(ev1)
+    rc, it_all, _ = dev.status()
+    h2d = dev.force.h2d_bytes - h2d0
+    s.close()
     return {"value": n * k / (ms / 1e3), "unit": "DOF-steps/s", "h2d_bytes_per_step": h2d / k,
-            "d2h_bytes_per_step": solver.n_rec * 8, "steps": k, "host_wall_s": wall,
-            "api": "NewmarkGPU.run per step + pinned H2D force entries + pinned D2H receiver velocities"}
+            "d2h_bytes_per_step": 3 * len(rec_eq) * 8, "steps": k, "first_step": w, "ms_per_step": ms / k,
+            "host_wall_s": wall, "cg_iters_per_step": (it_all - it_w) / k, "preconditioner": s.preconditioner,
+            "api": "NewmarkExplicit.calculate(matrix, matrix, matrix, F, t, t + 1) once per step (GenerateMatrix "
+                   "for M, C, K; force values streamed from pinned host memory; receiver u, v, a copied back to the "
+                   "host each call)"}
 
 
 def run_reference(args):
@@ -709,9 +765,7 @@ def run_reference(args):
     print(json.dumps({"metric": METRIC, "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": steps,
                       "warmup": w_steps, "ms_per_step": el_s / steps * 1e3, "higher_is_better": True, "scaling": "weak",
                       "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded structured mesh)",
-                      "config": {"workload": "plain Newmark FP64, box 60x40x30 m hexa8 0.5 m (120x80x60 el), "
-                                             "2 layers, Lysmer sides+base, moving 100 kN at 40 km/h, dt 5e-5",
-                                 "n_eq": n}, "impl": "reference", "cpu_baseline": cb,
+                      "config": workload_config(model), "impl": "reference", "cpu_baseline": cb,
                       "e2e": {"value": value, "unit": "DOF-steps/s", "h2d_bytes_per_step": 0,
                               "d2h_bytes_per_step": 0}}))
 

@@ -16,7 +16,7 @@ import torch
 from . import _native as nat
 from . import device as dv
 from .solvers import ForceTable, NodeBlockNewmark
-from .system_matrix import GenerateMatrix
+from .system_matrix import GenerateMatrix, generator_of
 
 
 def critical_time_step(g: GenerateMatrix):
@@ -55,9 +55,10 @@ class ExplicitLumped:
         self.t_idx = t_idx
 
     def calculate(self, M, C, K, F, t_start_idx, t_end_idx):
-        if not isinstance(M, GenerateMatrix):
-            raise TypeError("the explicit GPU scheme takes the GenerateMatrix that assembled M, C, K")
-        g = M
+        g = M if isinstance(M, GenerateMatrix) else generator_of(M, C, K)
+        if g is None:
+            raise TypeError("the explicit GPU scheme takes the GenerateMatrix that assembled M, C, K, or the "
+                            "scipy matrices it handed out")
         if np.any(self.u[0]) or np.any(self.v[0]):
             # the central-difference state is (u_n, v_{n-1/2}): it starts from rest only
             raise NotImplementedError("the explicit GPU scheme starts from rest (u[0] = v[0] = 0)")

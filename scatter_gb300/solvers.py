@@ -24,7 +24,7 @@ import torch
 
 from . import _native as nat
 from . import device as dv
-from .system_matrix import DeviceCSR, GenerateMatrix
+from .system_matrix import DeviceCSR, GenerateMatrix, generator_of
 
 
 class ForceTable:
@@ -62,6 +62,50 @@ class ForceTable:
         s = slice(self.f_ptr[t], self.f_ptr[t + 1])
         f[self.f_eq[s]] = self.f_val[s]
         return f
+
+
+class _DeviceForce:
+    """A force table on the device, as the step kernels read it: step pointers, target
+    indices (equations or slots) and values.
+
+    Resident (default): the whole history is copied once.  Streamed: the pointers and the
+    indices go up once, and each run copies the values of the steps it reads -- steps
+    t_begin .. t_end, since step t -> t + 1 clears the entries of step t and adds those of
+    step t + 1 -- from pinned host memory on the solver's stream, as a caller feeding
+    loads step by step would."""
+
+    def __init__(self, table, index, stream=False):
+        n = max(len(table.f_val), 1)
+        self.ptr_h = np.asarray(table.f_ptr, dtype=np.int64)
+        self.ptr = dv.to_dev(self.ptr_h, torch.int64)
+        self.idx = dv.zeros(n, torch.int32)
+        if len(table.f_val):
+            self.idx[:len(table.f_val)] = index
+        self.stream = bool(stream)
+        if self.stream:
+            self.val = dv.zeros(n, torch.float64)
+            self.val_h = torch.from_numpy(np.ascontiguousarray(table.f_val, dtype=np.float64)).pin_memory()
+            self.pushed = -1  # last step whose values are on the device
+        else:
+            self.val = dv.zeros(n, torch.float64)
+            if len(table.f_val):
+                self.val[:len(table.f_val)] = dv.to_dev(table.f_val, torch.float64)
+        self.h2d_bytes = 0
+
+    def push(self, t_begin, t_end):
+        """Before a run over steps t_begin .. t_end: copy the values it reads (streamed)."""
+        if not self.stream:
+            return
+        n_t = len(self.ptr_h) - 1
+        first = max(t_begin, self.pushed + 1)
+        last = min(t_end, n_t - 1)
+        if last < first:
+            return
+        a, b = int(self.ptr_h[first]), int(self.ptr_h[last + 1])
+        if b > a:
+            self.val[a:b].copy_(self.val_h[a:b], non_blocking=True)
+            self.h2d_bytes += (b - a) * 8
+        self.pushed = last
 
 
 def _device_matrices(M, C, K):
@@ -107,11 +151,15 @@ class NewmarkGPU:
         self.h = h
         self._keep = []
 
-    def set_force(self, table: ForceTable):
-        self._keep_force = [dv.to_dev(table.f_ptr, torch.int64), dv.to_dev(table.f_eq, torch.int32),
-                            dv.to_dev(table.f_val, torch.float64)]
-        p, e, v = self._keep_force
-        nat.call("sc_newmark_set_force", self.h, table.n_t, p.data_ptr(), e.data_ptr(), v.data_ptr())
+    def set_force(self, table: ForceTable, stream=False):
+        """Force history (equation indices).  stream=True: values copied per run (push_force)."""
+        eq = dv.to_dev(table.f_eq, torch.int32) if len(table.f_eq) else None
+        self.force = _DeviceForce(table, eq, stream)
+        f = self.force
+        nat.call("sc_newmark_set_force", self.h, table.n_t, f.ptr.data_ptr(), f.idx.data_ptr(), f.val.data_ptr())
+
+    def push_force(self, t_begin, t_end):
+        self.force.push(t_begin, t_end)
 
     def set_output(self, interval, rec_eq, n_out, what=("u", "v", "a")):
         self.rec = dv.to_dev(np.asarray(rec_eq, dtype=np.int32), torch.int32)
@@ -146,6 +194,12 @@ class NewmarkGPU:
 
     def outputs(self):
         return {k: (None if t is None else dv.host(t).reshape(self.n_out, self.n_rec)) for k, t in self.out.items()}
+
+    def output_rows(self, r0, r1):
+        """Output rows r0 .. r1 (host arrays [r1 - r0 + 1, n_rec]); None for what is not kept."""
+        nr = self.n_rec
+        return {k: (None if t is None else dv.host(t[r0 * nr:(r1 + 1) * nr]).reshape(-1, nr))
+                for k, t in self.out.items()}
 
     def close(self):
         if getattr(self, "h", None):
@@ -222,19 +276,20 @@ class NodeBlockNewmark:
         default) adapts the order to the iteration counts."""
         nat.call("sc_nb_set_predictor", self.h, int(order))
 
-    def set_force(self, table: ForceTable):
+    def set_force(self, table: ForceTable, stream=False):
+        """Force history (equation indices, mapped to slots here).  stream=True: the values
+        are copied from pinned host memory by push_force before each run."""
         eq = dv.to_dev(table.f_eq, torch.int64)
-        slot = self.eq2slot[eq].to(torch.int32) if eq.numel() else eq.to(torch.int32)
-        if eq.numel() and bool((slot < 0).any()):
+        slot = self.eq2slot[eq].to(torch.int32) if eq.numel() else None
+        if slot is not None and bool((slot < 0).any()):
             raise ValueError("force on a fixed DOF")
-        self._keep_force = [dv.to_dev(table.f_ptr, torch.int64), slot.contiguous(), dv.to_dev(table.f_val,
-                                                                                              torch.float64)]
-        if self._keep_force[1].numel() == 0:
-            self._keep_force[1] = torch.zeros(1, dtype=torch.int32, device=slot.device)
-            self._keep_force[2] = torch.zeros(1, dtype=torch.float64, device=slot.device)
-        p, e, v = self._keep_force
+        self.force = _DeviceForce(table, slot, stream)
         self.table = table
-        nat.call("sc_nb_set_force", self.h, table.n_t, p.data_ptr(), e.data_ptr(), v.data_ptr())
+        f = self.force
+        nat.call("sc_nb_set_force", self.h, table.n_t, f.ptr.data_ptr(), f.idx.data_ptr(), f.val.data_ptr())
+
+    def push_force(self, t_begin, t_end):
+        self.force.push(t_begin, t_end)
 
     def set_output(self, interval, rec_eq, n_out, what=("u", "v", "a")):
         rec = self.eq2slot[dv.to_dev(np.asarray(rec_eq, dtype=np.int64), torch.int64)].to(torch.int32).contiguous()
@@ -318,6 +373,12 @@ class NodeBlockNewmark:
     def outputs(self):
         return {k: (None if t is None else dv.host(t).reshape(self.n_out, self.n_rec)) for k, t in self.out.items()}
 
+    def output_rows(self, r0, r1):
+        """Output rows r0 .. r1 (host arrays [r1 - r0 + 1, n_rec]); None for what is not kept."""
+        nr = self.n_rec
+        return {k: (None if t is None else dv.host(t[r0 * nr:(r1 + 1) * nr]).reshape(-1, nr))
+                for k, t in self.out.items()}
+
     def state_eq(self):
         """u, v, a in the reference's equation numbering (host arrays)."""
         free = self.eq2slot
@@ -336,7 +397,20 @@ class NodeBlockNewmark:
 
 
 class NewmarkExplicit:
-    """GPU drop-in for PuggleSolvers' NewmarkExplicit as called by scatter/scatter.py:120-159."""
+    """GPU drop-in for PuggleSolvers' NewmarkExplicit as called by scatter/scatter.py:120-159.
+
+    ``calculate(M, C, K, F, t_start, t_end)`` takes the matrices as scipy CSR or as the
+    GenerateMatrix that assembled them.  Scipy matrices that this package's GenerateMatrix
+    handed out (``m.M, m.C, m.K``, the reference's call form) are recognised and run from
+    the generator's device arrays on the node-block solver; any other scipy matrices are
+    uploaded and run on the CSR loop.
+
+    The device solver outlives the call: a later call with the same matrices, time grid and
+    force that starts where the previous one ended (t_start == previous t_end) continues
+    the run on the device, and fills rows t_start .. t_end of the outputs.  With
+    ``stream_force = True`` each call copies the force values of its own steps host ->
+    device (pinned memory) instead of the whole history at set-up.  ``close()`` frees the
+    device solver."""
 
     def __init__(self, rtol=1e-12, max_iter=1000, layout="node-block", spmv="pair"):
         self.output_interval = 1
@@ -347,9 +421,13 @@ class NewmarkExplicit:
         self.max_iter = max_iter
         self.receivers = None  # optional equation subset for the outputs (default: all)
         self.force_table = None  # optional ForceTable (skips sampling the callback)
+        self.stream_force = False
         self.iterations = None
+        self.preconditioner = None
+        self._live = None  # (key, device solver, last step reached)
 
     def initialise(self, number_equations, time):
+        self.close()
         self.number_equations = int(number_equations)
         self.time = np.asarray(time, dtype=float)
         n_out = len(range(0, len(self.time), self.output_interval))
@@ -361,17 +439,7 @@ class NewmarkExplicit:
     def update(self, t_idx):
         self.t_idx = t_idx
 
-    def calculate(self, M, C, K, F, t_start_idx, t_end_idx):
-        """Run steps t_start_idx .. t_end_idx on the GPU.  M, C, K: scipy matrices, or the
-        GenerateMatrix that produced them (its device arrays are used without a copy)."""
-        if isinstance(M, GenerateMatrix):
-            g = M
-            pat, Md, Cd, Kd = g.pattern, g.M_d, g.C_d, g.K_d
-        else:
-            pat, Md, Cd, Kd = _device_matrices(M, C, K)
-        n = pat.n
-        dt = self.time[1] - self.time[0]
-        n_t = len(self.time)
+    def _force(self, n, n_t, F):
         table = self.force_table
         if table is None:
             if self.update_rhs_at_time_step_func is not None:
@@ -379,24 +447,36 @@ class NewmarkExplicit:
             else:
                 F0 = np.asarray(F, dtype=float)
                 table = ForceTable.from_callback(lambda t: F0, n_t, n)
+            self.force_table = table
+        return table
+
+    def _start(self, g, mats, F, t_start_idx, t_end_idx):
+        """New device solver, initial state, initial acceleration and the run's first steps."""
+        pat, Md, Cd, Kd = mats
+        n = pat.n
+        dt = self.time[1] - self.time[0]
+        n_t = len(self.time)
+        table = self._force(n, n_t, F)
         rec = np.arange(n) if self.receivers is None else np.asarray(self.receivers)
         n_out = len(range(0, n_t, self.output_interval))
         # the reference solver's u[0, :] and v[0, :] are writable initial conditions
         ic = None
         if getattr(self, "u", None) is not None and (np.any(self.u[0]) or np.any(self.v[0])):
             ic = (np.array(self.u[0], dtype=float), np.array(self.v[0], dtype=float))
-        attempts = ["fsai", "csr"] if (isinstance(M, GenerateMatrix) and self.layout == "node-block"
-                                       and M.adj_ptr is not None) else ["csr"]
+        attempts = ["fsai", "csr"] if (g is not None and self.layout == "node-block" and g.adj_ptr is not None) \
+            else ["csr"]
         for kind in attempts:
             if kind == "csr":
                 solver = NewmarkGPU(pat, Md, Cd, Kd, dt, self.rtol, self.max_iter)
             else:
-                solver = NodeBlockNewmark(M, dt, self.rtol, self.max_iter, precond=kind, spmv=self.spmv)
-            solver.set_force(table)
+                solver = NodeBlockNewmark(g, dt, self.rtol, self.max_iter, precond=kind, spmv=self.spmv)
+            solver.set_force(table, stream=self.stream_force)
             solver.set_output(self.output_interval, rec, n_out)
             if ic is not None:
                 solver.set_state(*ic)
+            solver.push_force(0, 0)  # the initial acceleration reads the force at t = 0
             solver.initial_acceleration()
+            solver.push_force(t_start_idx, t_end_idx)
             solver.run(t_start_idx, t_end_idx)
             rc, tot, mx = solver.status()
             self.preconditioner = kind
@@ -408,12 +488,68 @@ class NewmarkExplicit:
                 solver.close()
                 continue
             break
-        if rc != 0:
-            raise nat.ScatterGpuError("time loop", rc, nat.load().sc_status_string(rc).decode(), "")
-        out = solver.outputs()
-        self.iterations = (tot, mx)
-        if self.receivers is None:
-            self.u, self.v, self.a = out["u"], out["v"], out["a"]
+        return solver, rc, tot, mx, (0, t_end_idx)
+
+    def calculate(self, M, C, K, F, t_start_idx, t_end_idx):
+        """Run steps t_start_idx .. t_end_idx on the GPU.  M, C, K: scipy matrices, or the
+        GenerateMatrix that produced them (its device arrays are used without a copy)."""
+        if isinstance(M, GenerateMatrix):
+            g = M
         else:
-            self.u_rec, self.v_rec, self.a_rec = out["u"], out["v"], out["a"]
-        solver.close()
+            g = generator_of(M, C, K)
+        key = (id(g) if g is not None else (id(M), id(C), id(K)), id(self.time), id(self.force_table),
+               self.layout, self.spmv, self.output_interval)
+        live = self._live
+        if live is not None and live[0] == key and t_start_idx == live[2] and t_end_idx >= t_start_idx:
+            solver = live[1]
+            solver.push_force(t_start_idx, t_end_idx)
+            solver.run(t_start_idx, t_end_idx)
+            rc, tot, mx = solver.status()
+            rows = (t_start_idx, t_end_idx)
+        else:
+            self.close()
+            mats = (g.pattern, g.M_d, g.C_d, g.K_d) if g is not None else _device_matrices(M, C, K)
+            solver, rc, tot, mx, rows = self._start(g, mats, F, t_start_idx, t_end_idx)
+            key = key[:2] + (id(self.force_table),) + key[3:]
+        if rc != 0:
+            solver.close()
+            self._live = None
+            raise nat.ScatterGpuError("time loop", rc, nat.load().sc_status_string(rc).decode(), "")
+        # the matrices stay referenced while the run is live, so their ids stay theirs
+        self._live = (key, solver, t_end_idx, (M, C, K))
+        self.iterations = (tot, mx)
+        self._copy_outputs(solver, rows)
+
+    def _copy_outputs(self, solver, rows):
+        """Output rows of steps rows[0] .. rows[1] from the device into the host arrays."""
+        k = self.output_interval
+        r0 = -(-rows[0] // k)
+        r1 = min(rows[1] // k, solver.n_out - 1)
+        if r1 < r0:
+            return
+        nr = solver.n_rec
+        if self.receivers is None:
+            dst = {"u": self.u, "v": self.v, "a": self.a}
+        else:
+            if getattr(self, "u_rec", None) is None or self.u_rec.shape != (solver.n_out, nr):
+                self.u_rec, self.v_rec, self.a_rec = (np.zeros((solver.n_out, nr)) for _ in range(3))
+            dst = {"u": self.u_rec, "v": self.v_rec, "a": self.a_rec}
+        for name, rows_h in solver.output_rows(r0, r1).items():
+            if rows_h is not None:
+                dst[name][r0:r1 + 1] = rows_h
+
+    @property
+    def device_solver(self):
+        """The live device solver (NodeBlockNewmark or NewmarkGPU), or None."""
+        return None if self._live is None else self._live[1]
+
+    def close(self):
+        if getattr(self, "_live", None) is not None:
+            self._live[1].close()
+            self._live = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -9,12 +9,18 @@ Same constructor and methods as the reference (scatter/system_matrix.py:16-198,2
     m.K, m.M, m.C            # scipy CSR (downloaded on first access)
 
 The matrices live on the GPU in CSR over the reference's equation numbering, all three on
-the element-graph pattern (the reference's M pattern).  The reference additionally drops
-entries of K and C whose element sums cancel to exactly 0.0 in its own rounding
-(scipy sparse additions at system_matrix.py:198,375-376); those are round-off-level
-entries and are kept here as stored values, so the pattern of every matrix here is a
-superset of the reference's K/C patterns and equal to its M pattern.
+the element-graph pattern (the reference's M pattern).  The scipy matrices handed out
+follow the reference's sparsity semantics: ``.M`` keeps the element graph with its stored
+zeros (system_matrix.py:98-121), while ``.K`` and ``.C`` drop the entries whose assembled
+value is exactly 0.0, as the reference's scipy additions do (system_matrix.py:198,375-376).
+
+The scipy matrices are read-only views of what is on the device and remember the
+generator that made them, so a time integrator given ``(m.M, m.C, m.K)`` -- the
+reference's own call form, scatter/scatter.py:159 -- can run on the device arrays
+directly (``generator_of``).
 """
+import weakref
+
 import numpy as np
 import scipy.sparse as sp
 import torch
@@ -233,8 +239,21 @@ class GenerateMatrix:
     # -------------------------------------------------------------- scipy views
     def _scipy(self, key, values):
         if key not in self._cache:
-            self._cache[key] = self.pattern.to_scipy(values)
+            A = self.pattern.to_scipy(values)
+            if key in ("K", "C"):
+                A.eliminate_zeros()  # scipy's sparse + sparse drops exact zeros
+            for arr in (A.data, A.indices, A.indptr):
+                arr.flags.writeable = False  # a view of the device matrix: edits would not reach it
+            A._scatter_gb300_source = (weakref.ref(self), key)
+            self._cache[key] = A
         return self._cache[key]
+
+    def device_values(self, A):
+        """The device value array behind a scipy matrix this generator handed out, or None."""
+        src = getattr(A, "_scatter_gb300_source", None)
+        if src is None or src[0]() is not self or self._cache.get(src[1]) is not A:
+            return None
+        return {"K": self.K_d, "M": self.M_d, "C": self.C_d}[src[1]]
 
     @property
     def K(self):
@@ -247,3 +266,16 @@ class GenerateMatrix:
     @property
     def C(self):
         return self._scipy("C", self.C_d)
+
+
+def generator_of(M, C, K):
+    """The GenerateMatrix whose current .M, .C, .K are exactly these scipy objects, or None.
+
+    Each matrix handed out carries a weak link to its generator; the link only counts while
+    the object is still the generator's current one (any later assembly step replaces it)."""
+    src = getattr(M, "_scatter_gb300_source", None)
+    g = src[0]() if src is not None else None
+    if g is None:
+        return None
+    ok = (g.device_values(M) is g.M_d and g.device_values(C) is g.C_d and g.device_values(K) is g.K_d)
+    return g if ok else None

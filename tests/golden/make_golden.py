@@ -1,9 +1,9 @@
 """Generate the golden fixtures in this folder from the reference implementation.
 
-Run in a container where the reference source tree is present (default
-``/root/reference``, override with ``SCATTER_REF``)::
+Run where the reference source tree is present, with ``SCATTER_REF`` naming its
+root (the folder that holds ``scatter/`` and ``integration_tests/``)::
 
-    python tests/golden/make_golden.py
+    SCATTER_REF=/path/to/scatter python tests/golden/make_golden.py
 
 What it writes (``*.npz``, all small):
 
@@ -13,7 +13,10 @@ What it writes (``*.npz``, all small):
 * ``mat_<case>.npz`` -- the reference's assembled K, M, C (CSR) after
   ``generate_stiffness_and_mass``, ``absorbing_boundaries`` and
   ``damping_Rayleigh`` (scatter/system_matrix.py:35-121,166-198,256-376), plus
-  the absorbing-boundary parts alone.
+  the absorbing-boundary parts alone.  ``K_dropped`` / ``C_dropped`` list the
+  entries (row * n_eq + col, ascending) of M's pattern -- the element graph --
+  that K and C do not store: the reference's scipy additions drop the entries
+  whose sums come out exactly 0.0 (system_matrix.py:198,375-376).
 * ``elem_<etype>.npz`` -- element Ke, Me from ``VolumeElement`` /
   ``SurfaceElement`` (scatter/discretisation.py:8-433) for a few elements.
 * ``load_<case>.npz`` -- the dense force vector per time step from
@@ -41,7 +44,7 @@ import types
 import numpy as np
 import scipy.sparse as sp
 
-REF = os.environ.get("SCATTER_REF", "/root/reference")
+REF = os.environ.get("SCATTER_REF", "")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -239,6 +242,14 @@ def pattern_hash(a):
     return h.hexdigest()
 
 
+def pattern_keys(a):
+    """Stored entries of a sparse matrix as sorted keys row * n + col (int64)."""
+    a = sp.csr_matrix(a)
+    a.sum_duplicates()
+    rows = np.repeat(np.arange(a.shape[0], dtype=np.int64), np.diff(a.indptr))
+    return np.sort(rows * a.shape[1] + a.indices.astype(np.int64))
+
+
 def csr_parts(prefix, a, out, full):
     a = sp.csr_matrix(a)
     a.sort_indices()
@@ -293,6 +304,12 @@ def gen_case(name, spec):
     g.damping_Rayleigh(damping)
     csr_parts("K", g.K, mats_out, full)
     csr_parts("C", g.C, mats_out, full)
+    mkeys = pattern_keys(g.M)
+    for key, X in (("K", g.K), ("C", g.C)):
+        kept = pattern_keys(X)
+        if not np.isin(kept, mkeys).all():
+            raise RuntimeError(f"{name}: {key} stores an entry outside M's pattern")
+        mats_out[key + "_dropped"] = np.setdiff1d(mkeys, kept)
     np.savez_compressed(os.path.join(HERE, f"mat_{name}.npz"), **mats_out)
 
     # loads: dense vector per step, stored as COO over (step, eq)
@@ -399,6 +416,8 @@ def gen_histories():
 
 
 if __name__ == "__main__":
+    if not REF or not os.path.isdir(os.path.join(REF, "scatter")):
+        raise SystemExit("set SCATTER_REF to the reference source tree (the folder holding scatter/)")
     gen_elements()
     for name, spec in CASES.items():
         gen_case(name, spec)

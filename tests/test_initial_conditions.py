@@ -18,8 +18,11 @@ class FakeDeviceSolver:
         self.calls = []
         FakeDeviceSolver.made.append(self)
 
-    def set_force(self, table):
+    def set_force(self, table, stream=False):
         self.calls.append("set_force")
+
+    def push_force(self, t_begin, t_end):
+        pass
 
     def set_output(self, interval, rec, n_out, what=("u", "v", "a")):
         self.n_out, self.n_rec = n_out, len(rec)
@@ -37,8 +40,8 @@ class FakeDeviceSolver:
     def status(self):
         return 0, 0, 0
 
-    def outputs(self):
-        z = np.zeros((self.n_out, self.n_rec))
+    def output_rows(self, r0, r1):
+        z = np.zeros((r1 - r0 + 1, self.n_rec))
         return {"u": z, "v": z, "a": z}
 
     def close(self):
