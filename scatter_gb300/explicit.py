@@ -48,8 +48,8 @@ class ExplicitLumped:
         n_out = len(range(0, len(self.time), self.output_interval))
         self.output_time = self.time[::self.output_interval][:n_out]
         self.u = np.zeros((n_out, self.number_equations))
-        self.v = np.zeros_like(self.u)
-        self.a = np.zeros_like(self.u)
+        self.v = np.zeros(self.u.shape)  # zero pages: a receivers-only run never writes them
+        self.a = np.zeros(self.u.shape)
 
     def update(self, t_idx):
         self.t_idx = t_idx

@@ -432,9 +432,19 @@ class NewmarkExplicit:
         self.time = np.asarray(time, dtype=float)
         n_out = len(range(0, len(self.time), self.output_interval))
         self.output_time = self.time[::self.output_interval][:n_out]
-        self.u = np.zeros((n_out, self.number_equations))
-        self.v = np.zeros_like(self.u)
-        self.a = np.zeros_like(self.u)
+        # u, v, a [n_out, n_eq] are made on first use: a run that records receivers only never
+        # touches them (at 1.79 M equations and 10,001 outputs each would be 134 GiB)
+        self._hist = {}
+        self._hist_shape = (n_out, self.number_equations)
+
+    def _history(self, key):
+        if key not in self._hist:
+            self._hist[key] = np.zeros(self._hist_shape)  # zero pages, committed as written
+        return self._hist[key]
+
+    u = property(lambda self: self._history("u"), lambda self, x: self._hist.__setitem__("u", x))
+    v = property(lambda self: self._history("v"), lambda self, x: self._hist.__setitem__("v", x))
+    a = property(lambda self: self._history("a"), lambda self, x: self._hist.__setitem__("a", x))
 
     def update(self, t_idx):
         self.t_idx = t_idx
@@ -461,7 +471,8 @@ class NewmarkExplicit:
         n_out = len(range(0, n_t, self.output_interval))
         # the reference solver's u[0, :] and v[0, :] are writable initial conditions
         ic = None
-        if getattr(self, "u", None) is not None and (np.any(self.u[0]) or np.any(self.v[0])):
+        hist = getattr(self, "_hist", {})
+        if any(k in hist and np.any(hist[k][0]) for k in ("u", "v")):
             ic = (np.array(self.u[0], dtype=float), np.array(self.v[0], dtype=float))
         attempts = ["fsai", "csr"] if (g is not None and self.layout == "node-block" and g.adj_ptr is not None) \
             else ["csr"]
