@@ -5,7 +5,8 @@
  * integration + assembly in scatter/system_matrix.py, the Lysmer boundaries and Rayleigh
  * damping in the same file, and the Newmark time loop that scatter/scatter.py:120-159
  * drives through PuggleSolvers.  Each entry point below replaces one of those pieces; the
- * reference-side binding (ctypes) is shown in INTEGRATION.md.
+ * reference calls them through a ctypes binding (scatter_gb300/_native.py loads this library
+ * and raises on any non-zero status).
  *
  * Conventions
  *   - every pointer is a DEVICE pointer unless its name ends in _host;
@@ -101,7 +102,10 @@ int sc_exclusive_scan_i64(int64_t n, const int64_t* in, int64_t* out, int64_t* w
  *   - n is at most SC_SCAN_NOALLOC_MAX_N; larger n returns SC_CAPACITY (message in
  *     sc_last_error) before any launch;
  *   - the first call on a device looks up that array's address (cudaGetSymbolAddress) with
- *     the device current; make that first call before any stream capture on the device;
+ *     the device current and keeps it for the life of the process; make that first call
+ *     before any stream capture on the device.  A cudaDeviceReset (or anything else that
+ *     tears down and recreates the device's primary context) reloads the module and leaves
+ *     the kept address stale, so do not use this entry point after one;
  *   - every call shares the array, which keeps what the last call wrote; nothing in it needs
  *     to start at zero.  Calls whose work overlaps on the GPU (different streams, or another
  *     host thread, without ordering between them) race on it: order them.

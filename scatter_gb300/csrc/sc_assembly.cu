@@ -623,7 +623,9 @@ constexpr int kNoAllocDevices = 64;
 std::mutex g_tile_sums_lock;
 int64_t* g_tile_sums_ptr[kNoAllocDevices] = {};
 
-// Address of the array on the current device, looked up on the first call per device.
+// Address of the array on the current device, looked up on the first call per device and
+// kept for the process (a device reset that recreates the context leaves it stale; the header
+// tells callers not to use the entry point after one).
 int tile_sums_on_current_device(int64_t** out) {
   int dev = -1;
   int rc = check(cudaGetDevice(&dev), "sc_exclusive_scan_i64_noalloc: current device");
