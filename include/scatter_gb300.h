@@ -193,11 +193,18 @@ int sc_newmark_destroy(sc_newmark* h);
 
 /* ------------------------------------------------------------------ random fields
  * Input of the batched path (the reference draws per-element fields with gstools' SRF,
- * scatter/random_fields.py:59-120, and maps them log-normally, :73-77).  Gaussian covariance
- * exp(-(pi/4)|r/l|^2) by the randomisation (spectral) method with n_modes modes per
- * realisation, drawn from a counter-based generator so a field depends only on (seed, r).
- *   sc_rf_modes:     modes [R][n_modes][5] (k_x, k_y, k_z, Z1, Z2), float32
- *   sc_rf_lognormal: out [n_pts][R] = exp(mu_ln + sigma_ln g_r(x_p)), xyz [n_pts][3] float32 */
+ * scatter/random_fields.py:59-120, and maps them log-normally, :73-77).  The randomisation
+ * (spectral) method with n_modes modes per realisation, drawn from a counter-based generator
+ * so a field depends only on (seed, r).
+ *   sc_rf_modes_model: the covariance models of random_fields.py:79-86 as functions of the
+ *                    scaled distance h = |R^T (x - y) / l|: model 0 Gaussian exp(-(pi/4) h^2),
+ *                    1 Exponential exp(-h), 2 Matern(nu); rot_host: 9 doubles, row-major R
+ *                    (the rotation by `angles`, :80-86), NULL for none
+ *   sc_rf_modes:     the Gaussian model without rotation
+ *   sc_rf_lognormal: out [n_pts][R] = exp(mu_ln + sigma_ln g_r(x_p)), xyz [n_pts][3] float32
+ * modes [R][n_modes][5] (k_x, k_y, k_z, Z1, Z2), float32 */
+int sc_rf_modes_model(uint64_t seed, int R, int n_modes, int model, double nu, double lx, double ly, double lz,
+                      const double* rot_host, float* modes, void* stream);
 int sc_rf_modes(uint64_t seed, int R, int n_modes, double lx, double ly, double lz, float* modes, void* stream);
 int sc_rf_lognormal(int n_pts, const float* xyz, int R, int n_modes, const float* modes, double mu_ln,
                     double sigma_ln, float* out, void* stream);

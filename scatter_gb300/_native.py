@@ -44,6 +44,7 @@ SIGNATURES = {
     "sc_newmark_status": (I, [P, ctypes.POINTER(L), ctypes.POINTER(I)]),
     "sc_newmark_time_spmv": (I, [P, I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(L)]),
     "sc_newmark_destroy": (I, [P]),
+    "sc_rf_modes_model": (I, [ctypes.c_uint64, I, I, I, D, D, D, D, P, P, P]),
     "sc_rf_modes": (I, [ctypes.c_uint64, I, I, D, D, D, P, P]),
     "sc_rf_lognormal": (I, [I, P, I, I, P, D, D, P, P]),
     "sc_batch_create": (I, [ctypes.POINTER(P), P, P, P, P]),

@@ -5,14 +5,23 @@
 // third-party package absent here; its log-normal transform is kept:
 //   sigma_ln^2 = ln(1 + (sd/mean)^2), mu_ln = ln(mean^2 / sqrt(mean^2 + sd^2))  (:73-75)
 //   E = exp(mu_ln + g(x)) at element centroids                                    (:100-104)
-// g is a zero-mean Gaussian field with covariance sigma_ln^2 exp(-(pi/4) |r/l|^2) (axis
-// lengths l = (lx, ly, lz)), drawn by the randomisation (spectral) method of Kraichnan
-// (1970) / Hesse et al. (2014):
-//   g(x) = sqrt(sigma^2 / N) sum_j [Z1_j cos(k_j . x) + Z2_j sin(k_j . x)],
-//   k_j,axis ~ N(0, pi / (2 l_axis^2)),  Z ~ N(0, 1),
-// with every normal drawn from a counter-based generator (splitmix64 finaliser of
-// Steele, Lea & Flood 2014 over (seed, realisation, mode, index), Box-Muller), so a field
-// depends only on (seed, realisation) and is reproducible on any device.
+// g is a zero-mean Gaussian field with one of the covariance models the reference offers
+// (:79-88), as functions of the scaled distance h = |R^T (x - y) / l| (axis lengths
+// l = (lx, ly, lz) in the frame rotated by R):
+//   Gaussian     rho = exp(-(pi/4) h^2)
+//   Exponential  rho = exp(-h)
+//   Matern(nu)   rho = 2^(1-nu) / Gamma(nu) (sqrt(nu) h)^nu K_nu(sqrt(nu) h)
+// drawn by the randomisation (spectral) method of Kraichnan (1970) / Hesse et al. (2014):
+//   g(x) = sqrt(sigma^2 / N) sum_j [Z1_j cos(k_j . x) + Z2_j sin(k_j . x)],  Z ~ N(0, 1),
+// with the wave vectors k_j = R (kappa_j / l) and kappa_j drawn from each model's spectral
+// density in scaled coordinates:
+//   Gaussian     kappa = sqrt(pi/2) Z3                (normal)
+//   Exponential  kappa = Z3 / |Z'|                    (multivariate Cauchy: density ~ (1 + kappa^2)^-(d+1)/2)
+//   Matern(nu)   kappa = Z3 sqrt(nu / (2 G)), G ~ Gamma(nu, 1)   (multivariate t, 2 nu degrees
+//                of freedom: density ~ (nu + kappa^2)^-(nu + d/2)); G by Marsaglia & Tsang (2000)
+// Every uniform comes from a counter-based generator (splitmix64 finaliser of Steele, Lea &
+// Flood 2014 over (seed, realisation, mode, index)), normals by Box-Muller, so a field depends
+// only on (seed, realisation) and is reproducible on any device.
 #include <math.h>
 
 #include "sc_common.cuh"
@@ -32,10 +41,43 @@ __device__ inline double uniform01(uint64_t seed, int r, int j, int k) {
   return ((double)(h >> 11) + 0.5) * (1.0 / 9007199254740992.0);
 }
 
+__device__ inline double normal01(uint64_t seed, int r, int j, int k) {  // Box-Muller, uniforms k, k + 1
+  const double u1 = uniform01(seed, r, j, k), u2 = uniform01(seed, r, j, k + 1);
+  return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+// Gamma(a, 1) by Marsaglia & Tsang (2000), a >= 1 directly, a < 1 as Gamma(a + 1) U^(1/a);
+// uniforms from index 16 on, 3 per attempt, at most 64 attempts (the acceptance rate is
+// above 95 % per attempt, so running out has probability below 1e-80)
+__device__ inline double gamma_draw(uint64_t seed, int r, int j, double a) {
+  const double boost = a < 1.0 ? pow(uniform01(seed, r, j, 15), 1.0 / a) : 1.0;
+  const double aa = a < 1.0 ? a + 1.0 : a;
+  const double d = aa - 1.0 / 3.0, c = 1.0 / sqrt(9.0 * d);
+  double g = d;
+  for (int t = 0; t < 64; ++t) {
+    const double x = normal01(seed, r, j, 16 + 3 * t);
+    const double v1 = 1.0 + c * x;
+    if (v1 <= 0.0) continue;
+    const double v = v1 * v1 * v1;
+    const double u = uniform01(seed, r, j, 18 + 3 * t);
+    if (log(u) < 0.5 * x * x + d - d * v + d * log(v)) {
+      g = d * v;
+      break;
+    }
+  }
+  return g * boost;
+}
+
+struct RfModel {
+  int model;        // 0 Gaussian, 1 Exponential, 2 Matern
+  double nu;        // Matern smoothness
+  double il[3];     // 1 / axis lengths
+  double rot[9];    // R, row-major: k = R kappa_scaled
+};
+
 // modes[r][j] = (k_x, k_y, k_z, Z1, Z2)
-__global__ void k_rf_modes(uint64_t seed, int R, int N, double lx, double ly, double lz, float* modes) {
+__global__ void k_rf_modes(uint64_t seed, int R, int N, RfModel m, float* modes) {
   const double two_pi = 6.283185307179586;
-  const double sx = sqrt(M_PI / 2.0) / lx, sy = sqrt(M_PI / 2.0) / ly, sz = sqrt(M_PI / 2.0) / lz;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < (int64_t)R * N;
        q += (int64_t)gridDim.x * blockDim.x) {
     const int r = (int)(q / N), j = (int)(q - (q / N) * N);
@@ -46,12 +88,21 @@ __global__ void k_rf_modes(uint64_t seed, int R, int N, double lx, double ly, do
       n[2 * p] = rad * cos(two_pi * u2);
       n[2 * p + 1] = rad * sin(two_pi * u2);
     }
-    float* m = modes + q * 5;
-    m[0] = (float)(n[0] * sx);
-    m[1] = (float)(n[1] * sy);
-    m[2] = (float)(n[2] * sz);
-    m[3] = (float)n[3];
-    m[4] = (float)n[4];
+    double scale;
+    if (m.model == 0) {
+      scale = sqrt(M_PI / 2.0);
+    } else if (m.model == 1) {
+      scale = 1.0 / fabs(normal01(seed, r, j, 6));
+    } else {
+      scale = sqrt(m.nu / (2.0 * gamma_draw(seed, r, j, m.nu)));
+    }
+    double kl[3];
+    for (int a = 0; a < 3; ++a) kl[a] = n[a] * scale * m.il[a];
+    float* out = modes + q * 5;
+    for (int a = 0; a < 3; ++a)
+      out[a] = (float)(m.rot[3 * a] * kl[0] + m.rot[3 * a + 1] * kl[1] + m.rot[3 * a + 2] * kl[2]);
+    out[3] = (float)n[3];
+    out[4] = (float)n[4];
   }
 }
 
@@ -93,12 +144,24 @@ __global__ void k_rf_eval(int n_pts, const float* __restrict__ xyz, int R, int N
 
 using namespace sc;
 
+extern "C" int sc_rf_modes_model(uint64_t seed, int R, int n_modes, int model, double nu, double lx, double ly,
+                                 double lz, const double* rot_host, float* modes, void* stream) {
+  if (R <= 0 || n_modes <= 0 || !modes || !(lx > 0) || !(ly > 0) || !(lz > 0)) return SC_BAD_ARG;
+  if (model < 0 || model > 2 || (model == 2 && !(nu > 0 && nu <= 1e3))) return SC_BAD_ARG;
+  RfModel m;
+  m.model = model;
+  m.nu = nu;
+  m.il[0] = 1.0 / lx;
+  m.il[1] = 1.0 / ly;
+  m.il[2] = 1.0 / lz;
+  for (int i = 0; i < 9; ++i) m.rot[i] = rot_host ? rot_host[i] : (i % 4 == 0 ? 1.0 : 0.0);
+  k_rf_modes<<<grid_for((int64_t)R * n_modes, 256), 256, 0, (cudaStream_t)stream>>>(seed, R, n_modes, m, modes);
+  return check_launch("k_rf_modes");
+}
+
 extern "C" int sc_rf_modes(uint64_t seed, int R, int n_modes, double lx, double ly, double lz, float* modes,
                            void* stream) {
-  if (R <= 0 || n_modes <= 0 || !modes || !(lx > 0) || !(ly > 0) || !(lz > 0)) return SC_BAD_ARG;
-  k_rf_modes<<<grid_for((int64_t)R * n_modes, 256), 256, 0, (cudaStream_t)stream>>>(seed, R, n_modes, lx, ly, lz,
-                                                                                     modes);
-  return check_launch("k_rf_modes");
+  return sc_rf_modes_model(seed, R, n_modes, 0, 0.0, lx, ly, lz, nullptr, modes, stream);
 }
 
 extern "C" int sc_rf_lognormal(int n_pts, const float* xyz, int R, int n_modes, const float* modes, double mu_ln,

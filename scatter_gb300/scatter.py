@@ -50,7 +50,7 @@ def scatter(mesh_file, outfile_folder, materials, boundaries, inp_settings, load
         rf = RF(random_props, materials, outfile_folder, model.element_type)
         mat_idx = [m[1] for m in model.materials if m[2] == random_props["material"]][0]
         elements = model.elem[model.materials_index == mat_idx]
-        rf.generate_rf(model.nodes, elements, model.dimension)
+        rf.generate_gstools_rf(model.nodes, elements, model.dimension, angles=0.0)
         rf.dump()
         rf.update_material_list(materials, model, mat_idx)
         materials.update(rf.new_material)

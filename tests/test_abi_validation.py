@@ -59,6 +59,10 @@ def test_size_checks(lib):
     assert lib.sc_rf_modes(1, 0, 8, 1.0, 1.0, 1.0, FAKE, None) == SC_BAD_ARG
     assert lib.sc_rf_modes(1, 4, 8, 1.0, 0.0, 1.0, FAKE, None) == SC_BAD_ARG
     assert lib.sc_rf_lognormal(0, FAKE, 4, 8, FAKE, 0.0, 1.0, FAKE, None) == SC_BAD_ARG
+    # covariance model codes 0..2 only; the Matern model needs 0 < nu
+    assert lib.sc_rf_modes_model(1, 4, 8, 3, 1.0, 1.0, 1.0, 1.0, None, FAKE, None) == SC_BAD_ARG
+    assert lib.sc_rf_modes_model(1, 4, 8, 2, 0.0, 1.0, 1.0, 1.0, None, FAKE, None) == SC_BAD_ARG
+    assert lib.sc_rf_modes_model(1, 4, 8, 1, 1.0, 1.0, -1.0, 1.0, None, FAKE, None) == SC_BAD_ARG
     assert lib.sc_element_matrices(0, 2, 5, None, None, None, None, None, None, None) == SC_BAD_ARG
     assert lib.sc_element_matrices(0, 2, -1, None, None, None, None, None, None, None) == SC_BAD_ARG
     assert lib.sc_combine(-1, 1.0, None, 1.0, None, 1.0, None, FAKE, None) == SC_BAD_ARG

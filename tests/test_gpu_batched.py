@@ -30,6 +30,25 @@ def test_random_field_matches_oracle(cuda):
     assert np.abs(np.log(f_gpu) - np.log(f_ref)).max() <= 2e-4
 
 
+@pytest.mark.parametrize("model,angles", [("Exponential", 0.0), ("Matern", 0.0), ("Gaussian", [0.5, -0.3, 1.1]),
+                                          ("Matern", [0.2, 0.0, 0.7])])
+def test_random_field_models_match_oracle(cuda, model, angles):
+    """The other covariance models and the rotation by angles (random_fields.py:79-88) on the
+    GPU against the oracle's restatement of the same draws."""
+    from oracle import random_fields as orf
+    from scatter_gb300 import device as dv
+    from scatter_gb300.random_fields import lognormal_fields, rotation
+
+    rng = np.random.default_rng(5)
+    pts = rng.uniform(0, 10, size=(300, 3))
+    np.testing.assert_allclose(rotation(3, angles), orf.rotation(3, angles), rtol=0, atol=1e-15)
+    f_gpu = dv.host(lognormal_fields(pts, seed=77, R=3, lengths=(4.0, 1.5, 6.0), mean=50e6, sd=12.5e6, n_modes=64,
+                                     model=model, angles=angles))
+    f_ref = orf.lognormal_field(pts, 77, 3, 64, (4.0, 1.5, 6.0), 50e6, 12.5e6, model=model,
+                                rot=orf.rotation(3, angles))
+    assert np.abs(np.log(f_gpu) - np.log(f_ref)).max() <= 2e-4
+
+
 def test_random_field_statistics(cuda):
     from scatter_gb300 import device as dv
     from scatter_gb300.random_fields import lognormal_fields, lognormal_params

@@ -4,6 +4,7 @@ lengths, log-normal transform of :73-77).  gstools itself is absent, so this che
 statistics, not gstools' bits: the log-field's mean and spread, and its correlation
 exp(-(pi/4)(r/l)^2) along each axis with that axis's length."""
 import numpy as np
+import pytest
 
 from oracle import random_fields as orf
 
@@ -51,3 +52,57 @@ def test_fields_are_reproducible_and_independent_across_realisations():
     # realisation r depends only on (seed, r): the first 2 of 4 equal a 2-realisation draw
     d = orf.lognormal_field(pts, 99, 2, 16, LENGTHS, MEAN, SD)
     np.testing.assert_array_equal(a[:, :2], d)
+
+
+def _corr_along_axes(model, lengths, rot=None, seed=2024, R=512, N=64, pts=None):
+    pts = np.array(pts if pts is not None else [[0, 0, 0], [lengths[0], 0, 0], [0, lengths[1], 0], [0, 0, lengths[2]],
+                                                 [2 * lengths[0], 0, 0]], dtype=float)
+    g = np.log(orf.lognormal_field(pts, seed, R, N, lengths, MEAN, SD, model=model, rot=rot))
+    return [np.corrcoef(g[0], g[k])[0, 1] for k in range(1, len(pts))]
+
+
+@pytest.mark.parametrize("model", ["Exponential", "Matern"])
+def test_other_models_correlation(model):
+    """Exponential exp(-h) and Matern (nu = 1) h K_1(h), the other models the reference offers
+    (random_fields.py:81-84): correlation at one length along each axis and at two along x."""
+    rho = _corr_along_axes(model, LENGTHS)
+    want1, want2 = orf.correlation(model, [1.0, 2.0])
+    for k in range(3):
+        assert abs(rho[k] - want1) <= 0.1, (model, k, rho[k], want1)
+    assert abs(rho[3] - want2) <= 0.1, (model, rho[3], want2)
+
+
+def test_models_have_the_lognormal_marginal():
+    mu, sig = orf.lognormal_params(MEAN, SD)
+    for model in ("Exponential", "Matern"):
+        g = np.log(orf.lognormal_field(np.zeros((1, 3)), 5, 1024, 64, LENGTHS, MEAN, SD, model=model))[0]
+        assert abs(g.mean() - mu) <= 4 * sig / np.sqrt(1024), model
+        assert abs(g.std() / sig - 1) <= 0.1, model
+
+
+def test_angles_rotate_the_anisotropy_frame():
+    """lengths (6, 1, 1) rotated by pi/2 in the (x, y) plane: the long axis points along y."""
+    rot = orf.rotation(3, [np.pi / 2, 0.0, 0.0])
+    np.testing.assert_allclose(rot @ [1.0, 0, 0], [0, 1.0, 0], atol=1e-15)
+    rho = _corr_along_axes("Gaussian", (6.0, 1.0, 1.0), rot=rot, pts=[[0, 0, 0], [0, 6, 0], [6, 0, 0]])
+    assert abs(rho[0] - np.exp(-np.pi / 4)) <= 0.1
+    assert abs(rho[1]) <= 0.1
+    # 2D: one angle, in the (x, y) plane
+    np.testing.assert_allclose(orf.rotation(2, 0.4), orf.rotation(3, [0.4, 0, 0]))
+
+
+def test_gamma_draws_have_the_gamma_moments():
+    for a in (0.5, 1.0, 2.5):
+        g = np.array([orf.gamma_draw(11, 0, j, a) for j in range(4000)])
+        assert abs(g.mean() - a) <= 4 * np.sqrt(a / 4000), a
+        assert abs(g.var() / a - 1) <= 0.15, a
+
+
+def test_linear_model_is_refused_beyond_1d(tmp_path):
+    from scatter_gb300.random_fields import RF
+
+    props = {"theta": 5, "seed_number": 1, "material": "soil", "key_material": "Young", "std_value": 1e6,
+             "aniso_x": 1, "aniso_z": 1, "model_name": "Linear"}
+    rf = RF(props, {"soil": {"Young": 1e7, "poisson": 0.3, "density": 1900}}, str(tmp_path), "hexa8")
+    with pytest.raises(ValueError, match="1D only"):
+        rf.generate_gstools_rf(np.array([[1, 0, 0, 0.0]]), np.array([[1]]), 3)
