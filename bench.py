@@ -438,8 +438,8 @@ def batched_run(k, w, R=256):
             "realisations": R, "n_eq": n, "elements": n_el, "steps": k, "warmup": w, "ms_per_step": ms_b / k,
             "single_ms_per_step": ms_s / k, "rel_l2_vs_fp64_max": max(rels.values()),
             "rel_l2_vs_fp64": rels, "rel_l2_rtol": 1e-5,
-            "tuned_shape": {"kernel": "uniform hexa8 grid (k_batch_step_hex8g)" if grid_kernel else
-                            "incidence lists (k_batch_step)", "realisations_per_thread": rpt,
+            "tuned_shape": {"kernel": BatchedExplicit.KERNELS[grid_kernel],
+                            ("column_segment_points" if grid_kernel == 2 else "realisations_per_thread"): rpt,
                             "threads_per_block": tpb, "tuned_ms": tuned_ms},
             "workload": "256 log-normal E realisations, box 40x20x10 m hexa8 0.5 m, Lysmer, Ricker 20 Hz, dt 5e-5",
             "single": "plain FP64-class explicit GPU path (node-block graph, threads per row tuned: "

@@ -334,7 +334,8 @@ int sc_batch_create(sc_batch** h, const sc_batch_desc* desc, double* u, double* 
 /* The step kernel and its shape (realisations per thread, threads per block) are picked at
  * create time, and again by sc_batch_set_hex8_grid, by timing the candidates on scratch
  * copies of the state (no reference counterpart); this reports the choice, its per-step time
- * and whether it is the uniform hexa8 grid kernel (grid_kernel = 1). */
+ * and which kernel it is: 0 the incidence-list kernel, 1 the uniform hexa8 grid kernel, 2 the
+ * tensor-core kernel (realisations_per_thread then reports its column segment length). */
 int sc_batch_config(sc_batch* h, int* realisations_per_thread, int* threads_per_block, float* ms_per_step,
                     int* grid_kernel);
 /* Uniform hexa8 grids (no reference counterpart; the meshes scatter/mesher.py reads from
@@ -349,12 +350,27 @@ int sc_batch_config(sc_batch* h, int* realisations_per_thread, int* threads_per_
  * kernels, so they give bitwise the same results).  Device arrays owned by the caller; the
  * tuner then times both kernels. */
 int sc_batch_set_hex8_grid(sc_batch* h, int n_tiles, const int* halo, const int* elem8);
+/* The tensor-core step on a uniform hexa8 grid (no reference counterpart): the element
+ * products D = W K1 for 128 realisations at a time on tcgen05 (TF32 in three hi/lo products,
+ * FP32 accumulation; about 2^-21 of each product, so its results agree with the other kernels
+ * to that rounding, not bitwise).  The lattice (as above) is cut into columns of 4 x 4 points
+ * across its first two axes; nzp is the number of points along the third.  nodes
+ * [n_col][nzp][36] int32: the node at point (hx, hy) of the column's 6 x 6 ring (its points grown
+ * by one on each side) in plane z, at hx + 6 hy, -1 where none; elems [n_col][nzp - 1][25]
+ * int32: the element whose local node 0 sits at ring point (ex, ey) of plane z, at ex + 5 ey,
+ * -1 where none.  Columns numbered as the caller likes.  Needs R a multiple of 128.  Device
+ * arrays owned by the caller; the tuner then times every kernel.  sc_batch_status
+ * synchronises the stream and returns SC_CUDA_ERROR if a tensor-core step gave up waiting for
+ * its tensor-core work (its results are then not valid). */
+int sc_batch_set_hex8_columns(sc_batch* h, int n_col, int nzp, const int* nodes, const int* elems);
+int sc_batch_status(sc_batch* h);
 /* testing aids: force a shape of the incidence-list kernel (realisations per thread in
  * {1, 2, 4, 8} dividing R, by 4 for 4 and 8; threads per block a multiple of R / rpt, at most
  * 256), or of the uniform hexa8 grid kernel (1 or 2 realisations per thread, 128 or 256
- * threads per block) */
+ * threads per block), or the tensor-core kernel with column segments of seg points */
 int sc_batch_set_shape(sc_batch* h, int realisations_per_thread, int threads_per_block);
 int sc_batch_set_grid_shape(sc_batch* h, int realisations_per_thread, int threads_per_block);
+int sc_batch_set_tc_shape(sc_batch* h, int seg);
 int sc_batch_set_force(sc_batch* h, int n_t, const int64_t* f_ptr, const int* f_slot, const double* f_val);
 /* receivers record v [n_out][n_rec][R] every out_interval steps */
 int sc_batch_set_output(sc_batch* h, int out_interval, int n_rec, const int* rec_slot, double* out_v, int64_t n_out);

@@ -53,6 +53,9 @@ SIGNATURES = {
     "sc_batch_set_hex8_grid": (I, [P, I, P, P]),
     "sc_batch_set_shape": (I, [P, I, I]),
     "sc_batch_set_grid_shape": (I, [P, I, I]),
+    "sc_batch_set_hex8_columns": (I, [P, I, I, P, P]),
+    "sc_batch_set_tc_shape": (I, [P, I]),
+    "sc_batch_status": (I, [P]),
     "sc_batch_set_force": (I, [P, I, P, P, P]),
     "sc_batch_set_output": (I, [P, I, I, P, P, L]),
     "sc_batch_run": (I, [P, I, I]),

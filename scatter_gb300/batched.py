@@ -62,15 +62,11 @@ HEX8_NAT = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 
 HEX8_TILE = (4, 4, 2)  # lattice points per tile along xi, eta, zeta (the kernel's kTX, kTY, kTZ)
 
 
-def hex8_grid_tables(xyz, elem_idx, tile=HEX8_TILE):
-    """(halo [n_tiles, (tx+2)(ty+2)(tz+2)], elem8 [n_nodes, 8]) of a uniform hexa8 grid, None
-    for other meshes.  The nodes must sit on an integer lattice along the natural axes of the
-    first element (every element the same shape and orientation), each element's local node l
-    at its first node's lattice point plus the natural offset of l, at most one node per
-    lattice point.  halo lists per tile the nodes of the tile grown by one point on every side
-    (-1 where there is none), point (hx, hy, hz) at hx + (tx+2) (hy + (ty+2) hz); tiles are
-    numbered x fastest.  elem8 [a, la] is the element in which node a is local node la."""
-    n_nodes, E = len(xyz), len(elem_idx)
+def hex8_lattice(xyz, elem_idx):
+    """Integer lattice coordinates [n_nodes, 3] (from 0) of a uniform hexa8 grid along the
+    natural axes of its first element, or None when the mesh is not one (the conditions are
+    those of hex8_grid_tables)."""
+    n_nodes = len(xyz)
     e0 = elem_idx[0]
     A = np.stack([xyz[e0[1]] - xyz[e0[0]], xyz[e0[3]] - xyz[e0[0]], xyz[e0[4]] - xyz[e0[0]]], axis=1)
     if abs(np.linalg.det(A)) <= 1e-12 * np.abs(A).max() ** 3:
@@ -83,13 +79,71 @@ def hex8_grid_tables(xyz, elem_idx, tile=HEX8_TILE):
     Li -= Li.min(axis=0)
     if np.any(Li[elem_idx] != Li[elem_idx[:, :1]] + HEX8_NAT[None]):
         return None
+    ext = Li.max(axis=0) + 1
+    key = Li[:, 0] + ext[0] * (Li[:, 1] + ext[1] * Li[:, 2])
+    if len(np.unique(key)) != n_nodes:
+        return None
+    return Li
+
+
+HEX8_COLUMN = (4, 4)  # lattice points per column across the first two axes (the kernel's kCX, kCY)
+
+
+def hex8_column_tables(xyz, elem_idx, cross=HEX8_COLUMN):
+    """(nodes [n_col, nzp, 36], elems [n_col, nzp - 1, 25], nzp) for the tensor-core step on a
+    uniform hexa8 grid, None for other meshes.  Columns of cross[0] x cross[1] lattice points
+    across the first two lattice axes, numbered first axis fastest; per column and plane z
+    (third axis) the nodes of the column's ring -- its points grown by one on each side,
+    point (hx, hy) at hx + (cross[0] + 2) hy -- and the elements whose local node 0 is at ring
+    point (ex, ey) < (cross[0] + 1, cross[1] + 1), at ex + (cross[0] + 1) ey; -1 where none."""
+    Li = hex8_lattice(xyz, elem_idx)
+    if Li is None:
+        return None
+    ext = Li.max(axis=0) + 1
+    cx, cy = cross
+    nc = -(-ext[:2] // np.array(cross))
+    box = np.array([nc[0] * cx + 2, nc[1] * cy + 2, ext[2]])  # one point of margin across
+    def key(x, y, z):
+        return (x + 1) + box[0] * ((y + 1) + box[1] * z)
+    dense_n = np.full(int(np.prod(box)), -1, dtype=np.int64)
+    dense_n[key(Li[:, 0], Li[:, 1], Li[:, 2])] = np.arange(len(Li))
+    dense_e = np.full(int(np.prod(box)), -1, dtype=np.int64)
+    L0 = Li[elem_idx[:, 0]]
+    dense_e[key(L0[:, 0], L0[:, 1], L0[:, 2])] = np.arange(len(elem_idx))
+    C = np.arange(int(np.prod(nc)))
+    x0, y0 = (C % nc[0]) * cx, (C // nc[0]) * cy
+    nzp = int(ext[2])
+    hx, hy = np.meshgrid(np.arange(cx + 2), np.arange(cy + 2), indexing="xy")
+    hx, hy = hx.ravel(), hy.ravel()  # point hx + (cx + 2) hy
+    z = np.arange(nzp)
+    px = x0[:, None, None] - 1 + hx[None, None, :]
+    py = y0[:, None, None] - 1 + hy[None, None, :]
+    nodes = dense_n[key(px, py, z[None, :, None])]
+    ex, ey = np.meshgrid(np.arange(cx + 1), np.arange(cy + 1), indexing="xy")
+    ex, ey = ex.ravel(), ey.ravel()
+    qx = x0[:, None, None] - 1 + ex[None, None, :]
+    qy = y0[:, None, None] - 1 + ey[None, None, :]
+    elems = dense_e[key(qx, qy, z[None, :-1, None])]
+    return nodes.astype(np.int32), elems.astype(np.int32), nzp
+
+
+def hex8_grid_tables(xyz, elem_idx, tile=HEX8_TILE):
+    """(halo [n_tiles, (tx+2)(ty+2)(tz+2)], elem8 [n_nodes, 8]) of a uniform hexa8 grid, None
+    for other meshes.  The nodes must sit on an integer lattice along the natural axes of the
+    first element (every element the same shape and orientation), each element's local node l
+    at its first node's lattice point plus the natural offset of l, at most one node per
+    lattice point.  halo lists per tile the nodes of the tile grown by one point on every side
+    (-1 where there is none), point (hx, hy, hz) at hx + (tx+2) (hy + (ty+2) hz); tiles are
+    numbered x fastest.  elem8 [a, la] is the element in which node a is local node la."""
+    n_nodes, E = len(xyz), len(elem_idx)
+    Li = hex8_lattice(xyz, elem_idx)
+    if Li is None:
+        return None
     tile = np.asarray(tile)
     ext = Li.max(axis=0) + 1
     nt = -(-ext // tile)
     box = nt * tile + 2  # padded lattice: one point of margin on every side
     key = (Li[:, 0] + 1) + box[0] * ((Li[:, 1] + 1) + box[1] * (Li[:, 2] + 1))
-    if len(np.unique(key)) != n_nodes:
-        return None
     dense = np.full(int(np.prod(box)), -1, dtype=np.int64)
     dense[key] = np.arange(n_nodes)
     elem8 = np.full((n_nodes, 8), -1, dtype=np.int64)
@@ -108,8 +162,10 @@ def hex8_grid_tables(xyz, elem_idx, tile=HEX8_TILE):
 
 
 class BatchedExplicit:
-    def __init__(self, model, young, nu, rho, damping, absorbing, k_div, dt, order=2):
-        """young: per-element, per-realisation E [n_elem, R] (numpy or CUDA float32)."""
+    def __init__(self, model, young, nu, rho, damping, absorbing, k_div, dt, order=2, tensor_cores=True):
+        """young: per-element, per-realisation E [n_elem, R] (numpy or CUDA float32).
+        tensor_cores: offer the tensor-core step kernel to the tuner (uniform hexa8 grids, R a
+        multiple of 128)."""
         dv.require_cuda()
         etype = str(model.element_type)
         if int(model.dimension) != 3:
@@ -184,6 +240,16 @@ class BatchedExplicit:
             self._elem8 = dv.to_dev(self.grid_tables[1], torch.int32)
             nat.call("sc_batch_set_hex8_grid", self.h, len(self.grid_tables[0]), self._halo.data_ptr(),
                      self._elem8.data_ptr())
+        # ... and, for whole groups of 128 realisations, the tensor-core kernel
+        self.column_tables = None
+        if self.grid_tables is not None and R % 128 == 0 and tensor_cores:
+            self.column_tables = hex8_column_tables(nodes[:, 1:].astype(float), elem_idx)
+        if self.column_tables is not None:
+            cn, ce, nzp = self.column_tables
+            self._col_nodes = dv.to_dev(cn, torch.int32)
+            self._col_elems = dv.to_dev(ce, torch.int32)
+            nat.call("sc_batch_set_hex8_columns", self.h, len(cn), nzp, self._col_nodes.data_ptr(),
+                     self._col_elems.data_ptr())
 
     def _lysmer(self, model, props, absorbing, k_div, order, N):
         etype = str(model.element_type)
@@ -221,17 +287,25 @@ class BatchedExplicit:
         self.l_c = dv.to_dev(c.astype(np.float32), torch.float32)
         self.l_s = dv.to_dev(sv.astype(np.float32), torch.float32)
 
+    KERNELS = {0: "incidence lists (k_batch_step)", 1: "uniform hexa8 grid (k_batch_step_hex8g)",
+               2: "tensor cores (k_batch_step_tc)"}
+
     def config(self):
-        """(realisations per thread, threads per block, tuned ms per step, grid kernel) of the
-        step kernel; grid kernel is True for the uniform hexa8 grid kernel."""
+        """(realisations per thread, threads per block, tuned ms per step, kernel) of the step
+        kernel; kernel 0 incidence lists, 1 the uniform hexa8 grid kernel, 2 the tensor-core
+        kernel (whose first value is then its column segment length)."""
         rpt, tpb, ms, grid = ctypes.c_int(), ctypes.c_int(), ctypes.c_float(), ctypes.c_int()
         nat.call("sc_batch_config", self.h, ctypes.byref(rpt), ctypes.byref(tpb), ctypes.byref(ms), ctypes.byref(grid))
-        return rpt.value, tpb.value, ms.value, bool(grid.value)
+        return rpt.value, tpb.value, ms.value, grid.value
 
     def set_shape(self, realisations_per_thread, threads_per_block, grid=False):
         """Override the tuned kernel and shape (testing aid)."""
         fn = "sc_batch_set_grid_shape" if grid else "sc_batch_set_shape"
         nat.call(fn, self.h, int(realisations_per_thread), int(threads_per_block))
+
+    def set_tensor_core_shape(self, segment):
+        """Select the tensor-core kernel with column segments of `segment` points (testing aid)."""
+        nat.call("sc_batch_set_tc_shape", self.h, int(segment))
 
     def set_force(self, table: ForceTable):
         eq = dv.to_dev(table.f_eq, torch.int64)
@@ -253,6 +327,10 @@ class BatchedExplicit:
 
     def run(self, t_begin, t_end):
         nat.call("sc_batch_run", self.h, int(t_begin), int(t_end))
+
+    def status(self):
+        """Synchronise; raises if a tensor-core step gave up waiting for its tensor-core work."""
+        nat.call("sc_batch_status", self.h)
 
     def velocities(self):
         """[n_out, n_rec, R] receiver velocities (host)."""

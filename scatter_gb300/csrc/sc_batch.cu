@@ -16,6 +16,7 @@
 // rate; the caller's FP64 u, v are converted in at the start of a run and out at its end.
 // w = u + beta v and v are also kept as FP32 ping-pong copies that neighbours read.  RPT and the nodes per block come from a short
 // timing of the candidates on scratch copies of the state when the handle is created.
+#include <utility>
 #include <vector>
 
 #include "sc_common.cuh"
@@ -509,6 +510,359 @@ __global__ void __launch_bounds__(256) k_batch_step_hex8g(Args g, const __grid_c
   step_epilogue(g, step);
 }
 
+// ------------------------------------------------------------------ tensor-core step (uniform hexa8 grids)
+// The element products on the 5th-generation tensor cores.  Per element e and 128 realisations
+// (one CTA of 128 threads, thread t = realisation r0 + t = TMEM lane t):
+//   D[r, j] = sum_k W[r, k] K1[j, k]           (K1: the unit-E 24 x 24 element stiffness)
+//   f_node(j)[r] += E_e[r] D[r, j]             (FP32, CUDA cores)
+// W (the element's 24 w values per realisation) is written into tensor memory by the threads
+// (tcgen05.st), K1 sits in shared memory (K-major, no swizzle), D accumulates in tensor memory
+// and is read back with tcgen05.ld.  TF32 keeps 11 significant bits, so W and K1 are split into
+// hi = rna_tf32(x) and lo = x - hi and D takes the three products hi hi + hi lo + lo hi
+// (tcgen05.mma kind::tf32, M = 128, N = 32 with 8 zero columns, K = 3 x 8): the dropped lo lo
+// term and the lo parts' own TF32 rounding leave about 2^-21 of each product.
+//
+// Decomposition: the lattice (the hexa8 grid tables of hex8_grid_tables) is cut into columns
+// of kCX x kCY points across the first two lattice axes, each column into segments along the
+// third (the sweep axis).  A CTA owns one segment of one column for one group of 128
+// realisations and sweeps it layer by layer: element layer k (between point planes k and k + 1)
+// has kCEX x kCEY element positions touching the owned points; their forces on owned points go
+// to register accumulators of planes k and k + 1; after layer k, plane k is complete and its
+// owned nodes are updated (node_update, as in the other kernels).  Elements on the ring are
+// computed by both neighbouring columns (25 element positions per 16 owned points).
+// The element loop is software-pipelined over two TMEM buffers: element i's W is staged and its
+// MMAs issued while element i - 1's D is read back.  Waits on the MMA barriers are bounded:
+// after kTcSpin tries the CTA sets *err, stops and frees its tensor memory.
+constexpr int kCX = 4, kCY = 4;
+constexpr int kCHX = kCX + 2, kCHY = kCY + 2, kCHN = kCHX * kCHY;  // the ring plane: 6 x 6 points
+constexpr int kCEX = kCX + 1, kCEY = kCY + 1, kCEN = kCEX * kCEY;  // element positions per layer: 5 x 5
+constexpr int kTcThreads = 128;
+constexpr uint32_t kTcCols = 256;  // A buffers at columns 0 and 64 (hi +0, lo +32), D buffers at 128 and 160
+constexpr uint32_t kTcIdesc = (1u << 4)             // D: FP32
+                              | (2u << 7)            // A: TF32
+                              | (2u << 10)           // B: TF32
+                              | ((32u >> 3) << 17)   // N = 32
+                              | ((128u >> 4) << 24);  // M = 128
+constexpr int kTcSpin = 1 << 22;
+
+struct TcTables {
+  const int* nodes;  // [n_col][nzp][kCHN]: node at ring point (hx, hy) of plane z, -1 where none
+  const int* elems;  // [n_col][nzp - 1][kCEN]: element whose local node 0 is at ring point (ex, ey) of layer z
+  int nzp, seg, n_segs;
+  int* err;          // set when an MMA barrier wait gives up
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start, leading (K direction) and stride (M/N direction) byte
+// offsets, the fixed version bit, no swizzle
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ float tf32_hi(float x) {
+  uint32_t h;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+  return __uint_as_float(h);
+}
+
+__device__ __forceinline__ void tc_st8(uint32_t taddr, const float* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
+               "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]));
+}
+
+__device__ __forceinline__ void tc_ld24(uint32_t taddr, float* d) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3]), "=f"(d[4]), "=f"(d[5]), "=f"(d[6]), "=f"(d[7]), "=f"(d[8]),
+        "=f"(d[9]), "=f"(d[10]), "=f"(d[11]), "=f"(d[12]), "=f"(d[13]), "=f"(d[14]), "=f"(d[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=f"(d[16]), "=f"(d[17]), "=f"(d[18]), "=f"(d[19]), "=f"(d[20]), "=f"(d[21]), "=f"(d[22]), "=f"(d[23])
+               : "r"(taddr + 16));
+  // the registers are valid only after the wait: tie them to it so no use moves above it
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3]), "+f"(d[4]), "+f"(d[5]), "+f"(d[6]), "+f"(d[7]),
+                 "+f"(d[8]), "+f"(d[9]), "+f"(d[10]), "+f"(d[11]), "+f"(d[12]), "+f"(d[13]), "+f"(d[14]), "+f"(d[15]),
+                 "+f"(d[16]), "+f"(d[17]), "+f"(d[18]), "+f"(d[19]), "+f"(d[20]), "+f"(d[21]), "+f"(d[22]), "+f"(d[23])
+               :
+               : "memory");
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
+  for (int it = 0; it < kTcSpin; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tc_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// the element at position P = (ex, ey) of a layer: local node l at ring point
+// (ex + nat_x(l), ey + nat_y(l)) of plane k + nat_z(l); owned when that point is inside
+template <int P, int L>
+struct TcNode {
+  static constexpr int hx = P % kCEX + hex8_nat(L, 0), hy = P / kCEX + hex8_nat(L, 1), hz = hex8_nat(L, 2);
+  static constexpr bool owned = hx >= 1 && hx <= kCX && hy >= 1 && hy <= kCY;
+  static constexpr int p = owned ? (hy - 1) * kCX + (hx - 1) : 0;
+  static constexpr int ring = hy * kCHX + hx;
+};
+
+// the 24 w values of position P's element for this thread's realisation
+template <int P>
+__device__ __forceinline__ void tc_gather(const int* s_nodes, const float* __restrict__ w_in, int R, int r,
+                                          float (&wv)[24]) {
+#pragma unroll
+  for (int l = 0; l < 8; ++l) {
+    int node;
+    switch (l) {  // static ring offsets per local node
+#define TC_NODE_CASE(L) \
+  case L: node = s_nodes[TcNode<P, L>::hz * kCHN + TcNode<P, L>::ring]; break;
+      TC_NODE_CASE(0) TC_NODE_CASE(1) TC_NODE_CASE(2) TC_NODE_CASE(3)
+      TC_NODE_CASE(4) TC_NODE_CASE(5) TC_NODE_CASE(6) TC_NODE_CASE(7)
+#undef TC_NODE_CASE
+    }
+    const float* p = w_in + (int64_t)node * 3 * R + r;
+    wv[3 * l] = __ldg(p);
+    wv[3 * l + 1] = __ldg(p + R);
+    wv[3 * l + 2] = __ldg(p + 2 * R);
+  }
+}
+
+// E D of position P's element into the accumulators of its owned nodes
+template <int P, int L>
+__device__ __forceinline__ void tc_scatter_one(float E, const float (&d)[24], float (&cur)[kCX * kCY][3],
+                                               float (&nxt)[kCX * kCY][3]) {
+  using N = TcNode<P, L>;
+  if constexpr (N::owned) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if constexpr (N::hz == 0) cur[N::p][c] = fmaf(E, d[3 * L + c], cur[N::p][c]);
+      else nxt[N::p][c] = fmaf(E, d[3 * L + c], nxt[N::p][c]);
+    }
+  }
+}
+
+template <int P>
+__device__ __forceinline__ void tc_scatter(float E, const float (&d)[24], float (&cur)[kCX * kCY][3],
+                                           float (&nxt)[kCX * kCY][3]) {
+  tc_scatter_one<P, 0>(E, d, cur, nxt);
+  tc_scatter_one<P, 1>(E, d, cur, nxt);
+  tc_scatter_one<P, 2>(E, d, cur, nxt);
+  tc_scatter_one<P, 3>(E, d, cur, nxt);
+  tc_scatter_one<P, 4>(E, d, cur, nxt);
+  tc_scatter_one<P, 5>(E, d, cur, nxt);
+  tc_scatter_one<P, 6>(E, d, cur, nxt);
+  tc_scatter_one<P, 7>(E, d, cur, nxt);
+}
+
+struct TcState {
+  uint32_t tmem, mbar0, sb;  // TMEM base, first MMA barrier (the second at +8), K1 tiles in shared memory
+  uint32_t par;              // bit b: parity to wait for on barrier b
+  bool ok;                   // this thread's waits have all succeeded (after a failure it waits no more)
+  int* fail;                 // shared: set by any thread whose wait gave up; read only after a barrier
+};
+
+// iteration P of a layer: stage and issue element P (buffer P % 2), then read back element P - 1
+template <int P>
+__device__ __forceinline__ void tc_iteration(TcState& st, const int* s_nodes, const int* s_elems,
+                                             const float* __restrict__ w_in, const float* __restrict__ young, int R,
+                                             int r, float& E_prev, float (&cur)[kCX * kCY][3],
+                                             float (&nxt)[kCX * kCY][3]) {
+  const int lane_base = (threadIdx.x & ~31) << 16;  // this warp's TMEM lane quadrant
+  if constexpr (P < kCEN) {
+    const int e = s_elems[P];
+    float E = 0.f;
+    if (e >= 0) {
+      constexpr uint32_t a_col = (P & 1) * 64;
+      float wv[24];
+      tc_gather<P>(s_nodes, w_in, R, r, wv);
+      E = __ldg(young + (int64_t)e * R + r);
+      float hi[8], lo[8];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          hi[j] = tf32_hi(wv[8 * q + j]);
+          lo[j] = wv[8 * q + j] - hi[j];
+        }
+        tc_st8(st.tmem + lane_base + a_col + 8 * q, hi);
+        tc_st8(st.tmem + lane_base + a_col + 32 + 8 * q, lo);
+      }
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    }
+    tc_sync();
+    if (e >= 0 && threadIdx.x == 0) {
+      constexpr uint32_t a_col = (P & 1) * 64, d_col = 128 + (P & 1) * 32;
+#pragma unroll
+      for (int pass = 0; pass < 3; ++pass) {
+        const uint32_t a_off = pass == 2 ? 32 : 0;        // A lo in the last pass
+        const uint32_t b_off = pass == 1 ? 3 * 1024 : 0;  // K1 lo in the middle pass
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+          const uint64_t bd = tc_sdesc(st.sb + b_off + s * 1024, 128, 256);
+          const uint32_t acc = (pass | s) ? 1u : 0u;
+          asm volatile(
+              "{\n.reg .pred pp;\nsetp.ne.u32 pp, %4, 0;\n"
+              "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, pp;\n}" ::"r"(st.tmem + d_col),
+              "r"(st.tmem + a_col + a_off + 8 * s), "l"(bd), "r"(kTcIdesc), "r"(acc)
+              : "memory");
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       st.mbar0 + 8 * (P & 1))
+                   : "memory");
+    }
+    if constexpr (P > 0) {
+      if (s_elems[P - 1] >= 0 && st.ok) {
+        constexpr int b = (P - 1) & 1;
+        st.ok = tc_wait(st.mbar0 + 8 * b, (st.par >> b) & 1);
+        if (!st.ok) *st.fail = 1;
+        st.par ^= 1u << b;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        float d[24];
+        tc_ld24(st.tmem + lane_base + 128 + b * 32, d);
+        tc_scatter<P - 1>(E_prev, d, cur, nxt);
+      }
+    }
+    E_prev = E;
+  } else {
+    // after the last position: read back element kCEN - 1
+    if (s_elems[kCEN - 1] >= 0 && st.ok) {
+      constexpr int b = (kCEN - 1) & 1;
+      st.ok = tc_wait(st.mbar0 + 8 * b, (st.par >> b) & 1);
+      if (!st.ok) *st.fail = 1;
+      st.par ^= 1u << b;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      float d[24];
+      tc_ld24(st.tmem + lane_base + 128 + b * 32, d);
+      tc_scatter<kCEN - 1>(E_prev, d, cur, nxt);
+    }
+  }
+}
+
+template <int... Ps>
+__device__ __forceinline__ void tc_layer(std::integer_sequence<int, Ps...>, TcState& st, const int* s_nodes,
+                                         const int* s_elems, const float* __restrict__ w_in,
+                                         const float* __restrict__ young, int R, int r, float (&cur)[kCX * kCY][3],
+                                         float (&nxt)[kCX * kCY][3]) {
+  float E_prev = 0.f;
+  (tc_iteration<Ps>(st, s_nodes, s_elems, w_in, young, R, r, E_prev, cur, nxt), ...);
+}
+
+// the owned nodes of point plane (ring plane) s_plane: node update with the accumulated forces
+template <int... Ps>
+__device__ __forceinline__ void tc_update_plane(std::integer_sequence<int, Ps...>, const Args& g, const int* s_plane,
+                                                int r, const float (&acc)[kCX * kCY][3], const float* __restrict__ w_in,
+                                                float* __restrict__ w_out, const float* __restrict__ vf_in,
+                                                float* __restrict__ vf_out, int step, bool rec_now) {
+  (
+      [&] {
+        const int a = s_plane[(Ps / kCX + 1) * kCHX + (Ps % kCX) + 1];
+        if (a >= 0) {
+          const float f[3][1] = {{acc[Ps][0]}, {acc[Ps][1]}, {acc[Ps][2]}};
+          node_update<1>(g, a, r, f, w_in, w_out, vf_in, vf_out, step, rec_now);
+        }
+      }(),
+      ...);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 2) k_batch_step_tc(Args g, const __grid_constant__ K1Hex8 k1,
+                                                                 TcTables tt, const float* __restrict__ w_in,
+                                                                 float* __restrict__ w_out,
+                                                                 const float* __restrict__ vf_in,
+                                                                 float* __restrict__ vf_out) {
+  __shared__ __align__(1024) float sB[2 * 3 * 256];  // K1 hi then lo: 3 K-slices of 32 (N) x 8 (K), 1 KB each
+  __shared__ int s_nodes[2 * kCHN];                   // ring planes k and k + 1
+  __shared__ int s_elems[kCEN];
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_fail;
+  __shared__ __align__(8) uint64_t s_mbar[2];
+  const int t = threadIdx.x;
+  const int R = g.d.R;
+  const int r = blockIdx.y * kTcThreads + t;
+  const int col = blockIdx.x / tt.n_segs, sg = blockIdx.x - col * tt.n_segs;
+  const int step = *g.t + 1;
+  const bool rec_now = record_now(g, step);
+  // K1 into the canonical K-major layout: element (k, n) of slice k / 8 at
+  // (n / 8) 256 + (k % 8 / 4) 128 + (n % 8) 16 + (k % 4) 4 bytes; B[k][n] = K1[n][k], zero for n >= 24
+  for (int i = t; i < 24 * 32; i += kTcThreads) {
+    const int k = i >> 5, n = i & 31, kk = k & 7;
+    const int off = (k >> 3) * 256 + (n >> 3) * 64 + (kk >> 2) * 32 + (n & 7) * 4 + (kk & 3);
+    const float b = n < 24 ? k1.k[n * 24 + k] : 0.f;
+    const float bh = tf32_hi(b);
+    sB[off] = bh;
+    sB[3 * 256 + off] = b - bh;
+  }
+  if (t < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&s_tmem)),
+                 "r"(kTcCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (t == 0) {
+    s_fail = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&s_mbar[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&s_mbar[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc_sync();
+  TcState st{s_tmem, smem_addr(&s_mbar[0]), smem_addr(sB), 0u, true, &s_fail};
+  const int z0 = sg * tt.seg, z1 = min(z0 + tt.seg, tt.nzp);
+  const int kbeg = max(z0 - 1, 0), kend = min(z1, tt.nzp - 1);
+  float cur[kCX * kCY][3], nxt[kCX * kCY][3];
+#pragma unroll
+  for (int p = 0; p < kCX * kCY; ++p)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) cur[p][c] = nxt[p][c] = 0.f;
+  const int* col_nodes = tt.nodes + (int64_t)col * tt.nzp * kCHN;
+  const int* col_elems = tt.elems + (int64_t)col * (tt.nzp - 1) * kCEN;
+  // every barrier below is reached by all threads: a failed wait only sets s_fail, which the
+  // threads read after a barrier, so they leave the loop together
+  for (int k = kbeg; k < kend; ++k) {
+    __syncthreads();  // the previous layer's readers of s_nodes / s_elems are done
+    if (s_fail) break;
+    for (int i = t; i < 2 * kCHN + kCEN; i += kTcThreads) {
+      if (i < 2 * kCHN) s_nodes[i] = col_nodes[(int64_t)k * kCHN + i];
+      else s_elems[i - 2 * kCHN] = col_elems[(int64_t)k * kCEN + (i - 2 * kCHN)];
+    }
+    __syncthreads();
+    tc_layer(std::make_integer_sequence<int, kCEN + 1>{}, st, s_nodes, s_elems, w_in, g.d.young, R, r, cur, nxt);
+    if (k >= z0)
+      tc_update_plane(std::make_integer_sequence<int, kCX * kCY>{}, g, s_nodes, r, cur, w_in, w_out, vf_in, vf_out,
+                      step, rec_now);
+#pragma unroll
+    for (int p = 0; p < kCX * kCY; ++p)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        cur[p][c] = nxt[p][c];
+        nxt[p][c] = 0.f;
+      }
+  }
+  // the top plane of the lattice (no layer above it) when it belongs to this segment
+  __syncthreads();
+  const bool failed = s_fail != 0;
+  if (kend < z1 && !failed)
+    tc_update_plane(std::make_integer_sequence<int, kCX * kCY>{}, g, s_nodes + kCHN, r, cur, w_in, w_out, vf_in,
+                    vf_out, step, rec_now);
+  if (failed && t == 0) atomicExch(tt.err, 1);
+  tc_sync();
+  if (t < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(st.tmem), "r"(kTcCols));
+  step_epilogue(g, step);
+}
+
 __global__ void k_mark_slots(int64_t n, const int* __restrict__ idx, unsigned char* flag) {
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
     flag[idx[q]] = 1;
@@ -583,6 +937,9 @@ struct sc_batch {
   int n_tiles = 0;
   const int *halo = nullptr, *elem8 = nullptr;  // uniform hexa8 grid tables (caller's), or null
   K1Hex8 k1{};
+  TcTables tt{};   // column tables of the tensor-core kernel (caller's), nodes == null when not enabled
+  int n_col = 0;
+  int* tc_err = nullptr;
 };
 
 static void batch_drop_graphs(sc_batch* h) {
@@ -612,9 +969,18 @@ static void launch_hex8g(const sc_batch* h, const Args& g, int threads, cudaStre
                                                                                  vi, vo);
 }
 
-// grid = 1: the uniform hexa8 grid kernel (threads per block, realisations per thread; tpn unused)
+// grid = 1: the uniform hexa8 grid kernel (threads per block, realisations per thread; tpn unused);
+// grid = 2: the tensor-core kernel (rpt = points per column segment along the sweep axis)
 static void batch_launch(const sc_batch* h, const Args& g, int grid, int rpt, int threads, int tpn, cudaStream_t st,
                          const float* wi, float* wo, const float* vi, float* vo) {
+  if (grid == 2) {
+    TcTables tt = h->tt;
+    tt.seg = rpt;
+    tt.n_segs = (tt.nzp + rpt - 1) / rpt;
+    k_batch_step_tc<<<dim3((unsigned)(h->n_col * tt.n_segs), (unsigned)(g.d.R / kTcThreads)), kTcThreads, 0, st>>>(
+        g, h->k1, tt, wi, wo, vi, vo);
+    return;
+  }
   if (grid) {
     if (rpt == 2) launch_hex8g<2>(h, g, threads, st, wi, wo, vi, vo);
     else launch_hex8g<1>(h, g, threads, st, wi, wo, vi, vo);
@@ -696,6 +1062,14 @@ static int batch_tune(sc_batch* h) {
       for (int rpt = 1; rpt <= 2; ++rpt)
         if (R % rpt == 0)
           for (int threads : {256, 128}) cands.push_back({1, rpt, threads, 0});
+    if (h->tt.nodes) {  // tensor-core kernel: segments of the whole column, a half, a third, a quarter
+      int last = 0;
+      for (int parts = 1; parts <= 4; ++parts) {
+        const int seg = (h->tt.nzp + parts - 1) / parts;
+        if (seg != last) cands.push_back({2, seg, kTcThreads, 0});
+        last = seg;
+      }
+    }
     for (size_t ci = 0; ci < cands.size() && !rc; ++ci) {
       const Cand& c = cands[ci];
       float* wh = w;
@@ -861,6 +1235,56 @@ extern "C" int sc_batch_set_grid_shape(sc_batch* h, int realisations_per_thread,
   return SC_OK;
 }
 
+// Enables the tensor-core kernel on a uniform hexa8 grid (tables as described at
+// k_batch_step_tc; R a multiple of 128) and re-runs the tuner over all kernels.
+extern "C" int sc_batch_set_hex8_columns(sc_batch* h, int n_col, int nzp, const int* nodes, const int* elems) {
+  if (!h || n_col <= 0 || nzp < 2 || !nodes || !elems || h->g.d.n_en != 8 || h->g.d.n_types != 1 || h->g.d.node_nen)
+    return SC_BAD_ARG;
+  if (h->g.d.R % kTcThreads != 0 || h->g.d.R / kTcThreads > 65535 || (int64_t)n_col * nzp > (1ll << 30))
+    return SC_BAD_ARG;
+  cudaStream_t st = h->user;
+  int rc = SC_OK;
+  if (!h->tc_err) rc = check(cudaMallocAsync((void**)&h->tc_err, sizeof(int), st), "malloc");
+  if (!rc) rc = check(cudaMemsetAsync(h->tc_err, 0, sizeof(int), st), "memset");
+  if (!rc) rc = check(cudaMemcpyAsync(h->k1.k, h->g.d.ke1, sizeof(h->k1.k), cudaMemcpyDeviceToHost, st), "k1");
+  if (!rc) rc = check(cudaStreamSynchronize(st), "sync");
+  if (rc) return rc;
+  h->tt.nodes = nodes;
+  h->tt.elems = elems;
+  h->tt.nzp = nzp;
+  h->tt.err = h->tc_err;
+  h->n_col = n_col;
+  batch_drop_graphs(h);
+  return batch_tune(h);
+}
+
+// Selects the tensor-core kernel with column segments of `seg` points (testing aid; needs
+// sc_batch_set_hex8_columns).
+extern "C" int sc_batch_set_tc_shape(sc_batch* h, int seg) {
+  if (!h || !h->tt.nodes || seg < 1) return SC_BAD_ARG;
+  h->grid = 2;
+  h->rpt = seg;
+  h->threads = kTcThreads;
+  h->tpn = 0;
+  batch_drop_graphs(h);
+  return SC_OK;
+}
+
+// Synchronises the stream; SC_CUDA_ERROR when a tensor-core step gave up waiting for its MMAs
+// (its results are then not valid), else the stream's status.
+extern "C" int sc_batch_status(sc_batch* h) {
+  if (!h) return SC_BAD_ARG;
+  int rc = check(cudaStreamSynchronize(h->user), "batch sync");
+  if (rc || !h->tc_err) return rc;
+  int flag = 0;
+  if ((rc = check(cudaMemcpy(&flag, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost), "batch status"))) return rc;
+  if (flag) {
+    set_last_message("tensor-core batched step: an MMA completion wait gave up");
+    return SC_CUDA_ERROR;
+  }
+  return SC_OK;
+}
+
 extern "C" int sc_batch_set_shape(sc_batch* h, int realisations_per_thread, int threads_per_block) {
   if (!h) return SC_BAD_ARG;
   const int R = h->g.d.R, rpt = realisations_per_thread;
@@ -947,7 +1371,7 @@ extern "C" int sc_batch_destroy(sc_batch* h) {
   if (h->f32) cudaFree(h->f32);
   if (h->t) cudaFree(h->t);
   if (h->ticket) cudaFree(h->ticket);
-  void* more[] = {h->u2, h->v2, h->ml32, h->iml32, h->vneed};
+  void* more[] = {h->u2, h->v2, h->ml32, h->iml32, h->vneed, h->tc_err};
   for (void* q : more)
     if (q) cudaFree(q);
   if (h->cap) cudaStreamDestroy(h->cap);

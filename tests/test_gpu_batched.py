@@ -189,3 +189,84 @@ def test_batched_grid_kernel_on_a_notched_mesh(cuda):
     for vb, ub in results[1:]:
         np.testing.assert_array_equal(vb, results[0][0])
         np.testing.assert_array_equal(ub, results[0][1])
+
+
+def _tc_case(notched):
+    from scatter_gb300 import meshgen
+    from scatter_gb300.mesher import ReadMesh
+
+    nx, ny, nz, h = 9, 5, 6, 0.5
+    if not notched:
+        return meshgen.box_model(nx, ny, nz, h, bottom="020", x_faces="200", z_faces="002")
+    nodes, elem, _ = meshgen.box_hexa8(nx, ny, nz, h)
+    X = nodes[:, 1:]
+    idx = {int(n): k for k, n in enumerate(nodes[:, 0])}
+    cen = np.stack([X[[idx[int(n)] for n in e]].mean(axis=0) for e in elem])
+    lo = X.min(axis=0)
+    keep = ~((cen[:, 0] > lo[0] + 2.0) & (cen[:, 1] > lo[1] + 1.5) & (cen[:, 2] > lo[2] + 1.0))
+    elem = elem[keep]
+    used = np.isin(nodes[:, 0], np.unique(elem))
+    m = ReadMesh.from_arrays(nodes[used], elem, "hexa8", [[3, 1, "solid"]], np.ones(len(elem), dtype=np.int64))
+    m.read_bc(meshgen.box_boundaries(nx * h, ny * h, nz * h, "111", "100", "001"))
+    m.mapping()
+    m.connectivities()
+    return m
+
+
+@pytest.mark.parametrize("notched", [False, True])
+def test_tensor_core_step(cuda, notched):
+    """The tensor-core step (tcgen05, TF32 in three hi/lo products) on 128 realisations: against
+    the CUDA-core kernel (FP32 products) for several column segment lengths, and against
+    per-realisation FP64-class explicit solves, on a box with Lysmer faces and on a notched box
+    (lattice points without nodes, nodes with fewer than 8 elements)."""
+    from scatter_gb300 import device as dv
+    from scatter_gb300.batched import BatchedExplicit
+    from scatter_gb300.explicit import ExplicitLumped
+    from scatter_gb300.force_external import ricker_table
+    from scatter_gb300.random_fields import element_centroids, lognormal_fields
+    from scatter_gb300.system_matrix import GenerateMatrix
+
+    m = _tc_case(notched)
+    R = 128
+    young = lognormal_fields(element_centroids(m), seed=21, R=R, lengths=(2.0, 1.0, 2.0), mean=50e6, sd=12.5e6)
+    nu, rho = 0.3, 1900.0
+    damping, absorbing, kdiv = [1, 0.02, 50, 0.02], [1, 1], 1e3
+    dt, n_t = 5e-5, 200
+    time = np.linspace(0, dt * (n_t - 1), n_t)
+    top = m.top_nodes()
+    table = ricker_table(m, int(top[len(top) // 3]), -1e4, 40.0, 0.002, time)
+    rec = [int(m.eq_nb_dof[m.node_index()[n], 1]) for n in top[::3]]
+
+    def run(shape):
+        b = BatchedExplicit(m, young, nu, rho, damping, absorbing, kdiv, dt)
+        assert b.column_tables is not None
+        if shape is None:
+            b.set_shape(4, 256, False)
+        else:
+            b.set_tensor_core_shape(shape)
+        b.set_force(table)
+        b.set_output(1, rec, n_t)
+        b.run(0, n_t - 1)
+        b.status()
+        out = (b.velocities(), b.state()[0])
+        b.close()
+        return out
+
+    v0, u0 = run(None)
+    assert np.abs(v0).max() > 0
+    for seg in (100, 3, 1):  # the whole column, segments of 3 points, single planes
+        vt, ut = run(seg)
+        assert rel_l2(vt, v0) <= 2e-6, seg
+        assert rel_l2(ut, u0) <= 2e-6, seg
+    yh = dv.host(young).astype(float)
+    n_el = len(m.elem)
+    for r in (0, 77):
+        g = GenerateMatrix(m.number_eq, 2)
+        g.generate_stiffness_and_mass(m, None, element_props=(yh[:, r], np.full(n_el, nu), np.full(n_el, rho)))
+        g.absorbing_boundaries(m, None, absorbing, kdiv)
+        g.damping_Rayleigh(damping)
+        s = ExplicitLumped()
+        s.initialise(m.number_eq, time)
+        s.force_table = table
+        s.calculate(g, g, g, None, 0, n_t - 1)
+        assert rel_l2(vt[:, :, r], s.v[:, rec]) <= 1e-5

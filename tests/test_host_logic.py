@@ -279,3 +279,91 @@ def test_hex8_grid_tables_with_holes():
                 assert halo[t, p + d[0] + hx * (d[1] + hy * d[2])] == el[e, lb]
     # nodes at the re-entrant corner have fewer than 8 elements
     assert ((elem8 >= 0).sum(axis=1) < 8).sum() > 0
+
+
+def _replay_column_kernel(tables, elem_idx, Ke, w, seg):
+    """The tensor-core step's decomposition replayed on the CPU: per column and segment, the
+    element layers kbeg .. kend - 1, each element position's forces Ke w added to the owned
+    points of planes k and k + 1, plane k kept after layer k when it is in the segment, and the
+    top plane kept after the last layer.  Returns the forces [n_nodes, 3] and how many times
+    each node was finished."""
+    from scatter_gb300.batched import HEX8_COLUMN, HEX8_NAT
+
+    nodes, elems, nzp = tables
+    cx, cy = HEX8_COLUMN
+    chx = cx + 2
+    f = np.zeros((len(w), 3))
+    done = np.zeros(len(w), dtype=int)
+    n_segs = -(-nzp // seg)
+    for col in range(len(nodes)):
+        for sg in range(n_segs):
+            z0, z1 = sg * seg, min(sg * seg + seg, nzp)
+            kbeg, kend = max(z0 - 1, 0), min(z1, nzp - 1)
+            cur, nxt = np.zeros((cx * cy, 3)), np.zeros((cx * cy, 3))
+
+            def finish(plane, acc):
+                for p in range(cx * cy):
+                    a = nodes[col, plane, (p // cx + 1) * chx + p % cx + 1]
+                    if a >= 0:
+                        f[a] += acc[p]
+                        done[a] += 1
+
+            for k in range(kbeg, kend):
+                for P in range((cx + 1) * (cy + 1)):
+                    e = elems[col, k, P]
+                    if e < 0:
+                        continue
+                    ex, ey = P % (cx + 1), P // (cx + 1)
+                    ring = [nodes[col, k + HEX8_NAT[l, 2], (ey + HEX8_NAT[l, 1]) * chx + ex + HEX8_NAT[l, 0]]
+                            for l in range(8)]
+                    assert ring == list(elem_idx[e])
+                    d = Ke[e] @ w[elem_idx[e]].ravel()
+                    for l in range(8):
+                        hx, hy = ex + HEX8_NAT[l, 0], ey + HEX8_NAT[l, 1]
+                        if 1 <= hx <= cx and 1 <= hy <= cy:
+                            (cur if HEX8_NAT[l, 2] == 0 else nxt)[(hy - 1) * cx + hx - 1] += d[3 * l:3 * l + 3]
+                if k >= z0:
+                    finish(k, cur)
+                cur, nxt = nxt, np.zeros((cx * cy, 3))
+            if kend < z1:
+                finish(kend, cur)
+    return f, done
+
+
+@pytest.mark.parametrize("notched", [False, True])
+def test_hex8_column_tables_cover_every_element_once(notched):
+    """The tensor-core step's column tables and decomposition: on a box and on an L-shaped box,
+    every node is finished exactly once per step for every segment length, and the forces it
+    gathers equal the assembled K w."""
+    from oracle import assembly as asm
+    from oracle import elements as el
+    from scatter_gb300.batched import hex8_column_tables
+    from scatter_gb300.system_matrix import model_arrays
+
+    m = meshgen.box_model(9, 5, 6, 0.5)
+    nodes, _, elem_idx, _ = model_arrays(m)
+    xyz = nodes[:, 1:].astype(float)
+    if notched:
+        c = xyz[elem_idx].mean(axis=1)
+        keep = ~((c[:, 0] > 2.0) & (c[:, 2] < c[:, 2].min() + 1.5))
+        el_k = elem_idx[keep]
+        used = np.unique(el_k)
+        remap = -np.ones(len(xyz), dtype=np.int64)
+        remap[used] = np.arange(len(used))
+        elem_idx, xyz = remap[el_k], xyz[used]
+    tables = hex8_column_tables(xyz, elem_idx)
+    assert tables is not None
+    N, E = len(xyz), len(elem_idx)
+    rng = np.random.default_rng(0)
+    Ke, _ = el.element_matrices("hexa8", xyz[elem_idx], rng.uniform(1, 2, E), np.full(E, 0.3), np.ones(E))
+    eq = np.arange(3 * N, dtype=float).reshape(N, 3)
+    K = asm.assemble(eq[elem_idx].reshape(E, 24), Ke, 3 * N)
+    w = rng.standard_normal((N, 3))
+    want = (K @ w.ravel()).reshape(N, 3)
+    for seg in sorted({tables[2], -(-tables[2] // 2), 3, 1}):
+        f, done = _replay_column_kernel(tables, elem_idx, Ke, w, seg)
+        assert np.all(done == 1), seg
+        np.testing.assert_allclose(f, want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
+    bad = elem_idx.copy()
+    bad[3] = bad[3][[1, 0, 3, 2, 5, 4, 7, 6]]
+    assert hex8_column_tables(xyz, bad) is None
