@@ -10,7 +10,8 @@ is one Newmark time step (graph launch: force, predictor, residual, device-side 
 update).  Synthetic seeded inputs; no dataset.
 
     python bench.py [--steps K] [--warmup W] [--gpus N] [--impl gb300|reference]
-    python bench.py --section batched|ragged|adjoint|csr [--dims nx,ny,nz]   # one added workload
+    python bench.py --section batched|ragged|adjoint|csr [--dims nx,ny,nz]   # one added workload (--dims: a
+                                                                             # smaller box for the batched and csr ones)
 
 Prints one JSON line.  --impl reference times the CPU restatement of the reference path
 (oracle/: numpy assembly + C Newmark/PCG loop on all host threads) on the same workload.
@@ -356,7 +357,7 @@ def _events():
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
-def batched_run(k, w, R=256):
+def batched_run(k, w, R=256, dims=(80, 40, 20)):
     """Batching workload: R = 256 seeded log-normal Young's modulus realisations (mean 50 MPa,
     CoV 0.25, Gaussian covariance, correlation lengths 5 / 1 / 5 m in x / y (vertical) / z),
     nu = 0.3, rho = 1900, box 40 x 20 x 10 m hexa8 at 0.5 m (80 x 40 x 20 elements), Lysmer
@@ -372,7 +373,7 @@ def batched_run(k, w, R=256):
     from scatter_gb300.solvers import NodeBlockNewmark
     from scatter_gb300.system_matrix import GenerateMatrix
 
-    m = meshgen.box_model(80, 40, 20, 0.5, bottom="020", x_faces="200", z_faces="002")
+    m = meshgen.box_model(*dims, 0.5, bottom="020", x_faces="200", z_faces="002")
     n_t = 3001
     if w + k + 1 > n_t:
         raise SystemExit("batched steps + warmup exceed the 3000-step history")
@@ -396,6 +397,21 @@ def batched_run(k, w, R=256):
     torch.cuda.synchronize()
     ms_b = e0.elapsed_time(e1)
     vb_all = b.velocities()[: w + k + 1]  # [step, receiver, realisation]
+    # the tensor-core kernel (a tuner candidate) timed on its own at its best column segment
+    tc_ms = None
+    if b.column_tables is not None:
+        nzp = b.column_tables[2]
+        tc_ms = {}
+        for seg in sorted({nzp, -(-nzp // 2), -(-nzp // 3)}):
+            b.set_tensor_core_shape(seg)
+            b.run(0, 3)
+            e0, e1 = _events()
+            e0.record()
+            b.run(3, 13)
+            e1.record()
+            torch.cuda.synchronize()
+            b.status()
+            tc_ms[seg] = e0.elapsed_time(e1) / 10
     young_h = dv.host(young).astype(float)
     b.close()
     del b
@@ -441,6 +457,7 @@ def batched_run(k, w, R=256):
             "tuned_shape": {"kernel": BatchedExplicit.KERNELS[grid_kernel],
                             ("column_segment_points" if grid_kernel == 2 else "realisations_per_thread"): rpt,
                             "threads_per_block": tpb, "tuned_ms": tuned_ms},
+            "tensor_core_kernel_ms_per_step": tc_ms,
             "workload": "256 log-normal E realisations, box 40x20x10 m hexa8 0.5 m, Lysmer, Ricker 20 Hz, dt 5e-5",
             "single": "plain FP64-class explicit GPU path (node-block graph, threads per row tuned: "
                       f"{single_tpr}), realisation 0 timed, same steps; receiver velocities of realisations "
@@ -798,7 +815,8 @@ def main():
 
         _native.load()
         if args.section == "batched":
-            out = batched_run(min(args.steps, 2990), args.warmup)
+            dims = tuple(int(x) for x in args.dims.split(",")) if args.dims else (80, 40, 20)
+            out = batched_run(min(args.steps, 2990), args.warmup, dims=dims)
         elif args.section == "ragged":
             out = ragged_run(min(args.steps, 1990), args.warmup)
         elif args.section == "csr":

@@ -526,14 +526,19 @@ __global__ void __launch_bounds__(256) k_batch_step_hex8g(Args g, const __grid_c
 // of kCX x kCY points across the first two lattice axes, each column into segments along the
 // third (the sweep axis).  A CTA owns one segment of one column for one group of 128
 // realisations and sweeps it layer by layer: element layer k (between point planes k and k + 1)
-// has kCEX x kCEY element positions touching the owned points; their forces on owned points go
-// to register accumulators of planes k and k + 1; after layer k, plane k is complete and its
+// has kCEX x kCEY element positions touching the owned points; their forces on owned points are
+// added to shared-memory accumulators of planes k and k + 1 (each thread its own realisation's
+// column, so no two threads touch the same word); after layer k, plane k is complete and its
 // owned nodes are updated (node_update, as in the other kernels).  Elements on the ring are
 // computed by both neighbouring columns (25 element positions per 16 owned points).
-// The element loop is software-pipelined over two TMEM buffers: element i's W is staged and its
-// MMAs issued while element i - 1's D is read back.  Waits on the MMA barriers are bounded:
-// after kTcSpin tries the CTA sets *err, stops and frees its tensor memory.
-constexpr int kCX = 4, kCY = 4;
+// The ring planes of w are copied into shared memory by asynchronous bulk copies (512 bytes
+// per node and DOF, completing on one barrier per plane slot), three slots deep: layer k reads
+// planes k and k + 1 while plane k + 2 arrives.  The update state of the plane finished by the
+// layer is prefetched into L2 when the layer starts.  The element loop is software-pipelined
+// over two TMEM buffers: element i's W is staged and its MMAs issued before element i - 1's D is
+// read back.  Waits on barriers are bounded: after kTcSpin tries a thread records the failure,
+// the CTA leaves its sweep at the next layer, frees its tensor memory and sets *err.
+constexpr int kCX = 4, kCY = 4, kCP = kCX * kCY;
 constexpr int kCHX = kCX + 2, kCHY = kCY + 2, kCHN = kCHX * kCHY;  // the ring plane: 6 x 6 points
 constexpr int kCEX = kCX + 1, kCEY = kCY + 1, kCEN = kCEX * kCEY;  // element positions per layer: 5 x 5
 constexpr int kTcThreads = 128;
@@ -544,13 +549,34 @@ constexpr uint32_t kTcIdesc = (1u << 4)             // D: FP32
                               | ((32u >> 3) << 17)   // N = 32
                               | ((128u >> 4) << 24);  // M = 128
 constexpr int kTcSpin = 1 << 22;
+constexpr int kPlaneFloats = kCHN * 3 * kTcThreads;    // one ring plane of w: [point][dof][realisation]
+constexpr int kAccFloats = kCP * 3 * kTcThreads;       // one plane of force accumulators: [point][dof][realisation]
+constexpr size_t kTcSmem = sizeof(float) * (3 * kPlaneFloats + 2 * kAccFloats);  // 215,040 bytes
 
 struct TcTables {
   const int* nodes;  // [n_col][nzp][kCHN]: node at ring point (hx, hy) of plane z, -1 where none
   const int* elems;  // [n_col][nzp - 1][kCEN]: element whose local node 0 is at ring point (ex, ey) of layer z
   int nzp, seg, n_segs;
-  int* err;          // set when an MMA barrier wait gives up
+  int* err;          // set when a barrier wait gives up
 };
+
+// local node l of the element at position P: ring point, plane (0: k, 1: k + 1) and owned point
+// (-1 when outside the owned 4 x 4), packed as ring | plane << 8 | (owned + 1) << 9
+struct TcPos {
+  short code[kCEN][8];
+};
+__host__ __device__ constexpr TcPos tc_positions() {
+  TcPos t{};
+  for (int P = 0; P < kCEN; ++P)
+    for (int l = 0; l < 8; ++l) {
+      const int hx = P % kCEX + hex8_nat(l, 0), hy = P / kCEX + hex8_nat(l, 1), hz = hex8_nat(l, 2);
+      const bool owned = hx >= 1 && hx <= kCX && hy >= 1 && hy <= kCY;
+      const int p = owned ? (hy - 1) * kCX + (hx - 1) : -1;
+      t.code[P][l] = (short)((hy * kCHX + hx) | (hz << 8) | ((p + 1) << 9));
+    }
+  return t;
+}
+__constant__ TcPos c_tc_pos = tc_positions();
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -610,192 +636,53 @@ __device__ __forceinline__ void tc_sync() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// the element at position P = (ex, ey) of a layer: local node l at ring point
-// (ex + nat_x(l), ey + nat_y(l)) of plane k + nat_z(l); owned when that point is inside
-template <int P, int L>
-struct TcNode {
-  static constexpr int hx = P % kCEX + hex8_nat(L, 0), hy = P / kCEX + hex8_nat(L, 1), hz = hex8_nat(L, 2);
-  static constexpr bool owned = hx >= 1 && hx <= kCX && hy >= 1 && hy <= kCY;
-  static constexpr int p = owned ? (hy - 1) * kCX + (hx - 1) : 0;
-  static constexpr int ring = hy * kCHX + hx;
-};
-
-// the 24 w values of position P's element for this thread's realisation
-template <int P>
-__device__ __forceinline__ void tc_gather(const int* s_nodes, const float* __restrict__ w_in, int R, int r,
-                                          float (&wv)[24]) {
-#pragma unroll
-  for (int l = 0; l < 8; ++l) {
-    int node;
-    switch (l) {  // static ring offsets per local node
-#define TC_NODE_CASE(L) \
-  case L: node = s_nodes[TcNode<P, L>::hz * kCHN + TcNode<P, L>::ring]; break;
-      TC_NODE_CASE(0) TC_NODE_CASE(1) TC_NODE_CASE(2) TC_NODE_CASE(3)
-      TC_NODE_CASE(4) TC_NODE_CASE(5) TC_NODE_CASE(6) TC_NODE_CASE(7)
-#undef TC_NODE_CASE
-    }
-    const float* p = w_in + (int64_t)node * 3 * R + r;
-    wv[3 * l] = __ldg(p);
-    wv[3 * l + 1] = __ldg(p + R);
-    wv[3 * l + 2] = __ldg(p + 2 * R);
-  }
-}
-
-// E D of position P's element into the accumulators of its owned nodes
-template <int P, int L>
-__device__ __forceinline__ void tc_scatter_one(float E, const float (&d)[24], float (&cur)[kCX * kCY][3],
-                                               float (&nxt)[kCX * kCY][3]) {
-  using N = TcNode<P, L>;
-  if constexpr (N::owned) {
+// plane z of the column's ring into plane slot `dst` (one thread): one 512-byte bulk copy per
+// node and DOF, completing on `mbar`
+__device__ __forceinline__ void tc_load_plane(const int* __restrict__ ring_nodes, const float* __restrict__ w_in,
+                                              int R, int r0, float* dst, uint32_t mbar) {
+  uint32_t bytes = 0;
+  for (int i = 0; i < kCHN; ++i) bytes += ring_nodes[i] >= 0 ? 3u * 512u : 0u;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+  for (int i = 0; i < kCHN; ++i) {
+    const int node = ring_nodes[i];
+    if (node < 0) continue;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      if constexpr (N::hz == 0) cur[N::p][c] = fmaf(E, d[3 * L + c], cur[N::p][c]);
-      else nxt[N::p][c] = fmaf(E, d[3 * L + c], nxt[N::p][c]);
+      const float* src = w_in + ((int64_t)node * 3 + c) * R + r0;
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], 512, [%2];" ::"r"(
+              smem_addr(dst + (i * 3 + c) * kTcThreads)),
+          "l"(src), "r"(mbar)
+          : "memory");
     }
   }
 }
 
-template <int P>
-__device__ __forceinline__ void tc_scatter(float E, const float (&d)[24], float (&cur)[kCX * kCY][3],
-                                           float (&nxt)[kCX * kCY][3]) {
-  tc_scatter_one<P, 0>(E, d, cur, nxt);
-  tc_scatter_one<P, 1>(E, d, cur, nxt);
-  tc_scatter_one<P, 2>(E, d, cur, nxt);
-  tc_scatter_one<P, 3>(E, d, cur, nxt);
-  tc_scatter_one<P, 4>(E, d, cur, nxt);
-  tc_scatter_one<P, 5>(E, d, cur, nxt);
-  tc_scatter_one<P, 6>(E, d, cur, nxt);
-  tc_scatter_one<P, 7>(E, d, cur, nxt);
-}
-
-struct TcState {
-  uint32_t tmem, mbar0, sb;  // TMEM base, first MMA barrier (the second at +8), K1 tiles in shared memory
-  uint32_t par;              // bit b: parity to wait for on barrier b
-  bool ok;                   // this thread's waits have all succeeded (after a failure it waits no more)
-  int* fail;                 // shared: set by any thread whose wait gave up; read only after a barrier
-};
-
-// iteration P of a layer: stage and issue element P (buffer P % 2), then read back element P - 1
-template <int P>
-__device__ __forceinline__ void tc_iteration(TcState& st, const int* s_nodes, const int* s_elems,
-                                             const float* __restrict__ w_in, const float* __restrict__ young, int R,
-                                             int r, float& E_prev, float (&cur)[kCX * kCY][3],
-                                             float (&nxt)[kCX * kCY][3]) {
-  const int lane_base = (threadIdx.x & ~31) << 16;  // this warp's TMEM lane quadrant
-  if constexpr (P < kCEN) {
-    const int e = s_elems[P];
-    float E = 0.f;
-    if (e >= 0) {
-      constexpr uint32_t a_col = (P & 1) * 64;
-      float wv[24];
-      tc_gather<P>(s_nodes, w_in, R, r, wv);
-      E = __ldg(young + (int64_t)e * R + r);
-      float hi[8], lo[8];
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          hi[j] = tf32_hi(wv[8 * q + j]);
-          lo[j] = wv[8 * q + j] - hi[j];
-        }
-        tc_st8(st.tmem + lane_base + a_col + 8 * q, hi);
-        tc_st8(st.tmem + lane_base + a_col + 32 + 8 * q, lo);
-      }
-      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-    }
-    tc_sync();
-    if (e >= 0 && threadIdx.x == 0) {
-      constexpr uint32_t a_col = (P & 1) * 64, d_col = 128 + (P & 1) * 32;
-#pragma unroll
-      for (int pass = 0; pass < 3; ++pass) {
-        const uint32_t a_off = pass == 2 ? 32 : 0;        // A lo in the last pass
-        const uint32_t b_off = pass == 1 ? 3 * 1024 : 0;  // K1 lo in the middle pass
-#pragma unroll
-        for (int s = 0; s < 3; ++s) {
-          const uint64_t bd = tc_sdesc(st.sb + b_off + s * 1024, 128, 256);
-          const uint32_t acc = (pass | s) ? 1u : 0u;
-          asm volatile(
-              "{\n.reg .pred pp;\nsetp.ne.u32 pp, %4, 0;\n"
-              "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, pp;\n}" ::"r"(st.tmem + d_col),
-              "r"(st.tmem + a_col + a_off + 8 * s), "l"(bd), "r"(kTcIdesc), "r"(acc)
-              : "memory");
-        }
-      }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       st.mbar0 + 8 * (P & 1))
-                   : "memory");
-    }
-    if constexpr (P > 0) {
-      if (s_elems[P - 1] >= 0 && st.ok) {
-        constexpr int b = (P - 1) & 1;
-        st.ok = tc_wait(st.mbar0 + 8 * b, (st.par >> b) & 1);
-        if (!st.ok) *st.fail = 1;
-        st.par ^= 1u << b;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        float d[24];
-        tc_ld24(st.tmem + lane_base + 128 + b * 32, d);
-        tc_scatter<P - 1>(E_prev, d, cur, nxt);
-      }
-    }
-    E_prev = E;
-  } else {
-    // after the last position: read back element kCEN - 1
-    if (s_elems[kCEN - 1] >= 0 && st.ok) {
-      constexpr int b = (kCEN - 1) & 1;
-      st.ok = tc_wait(st.mbar0 + 8 * b, (st.par >> b) & 1);
-      if (!st.ok) *st.fail = 1;
-      st.par ^= 1u << b;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      float d[24];
-      tc_ld24(st.tmem + lane_base + 128 + b * 32, d);
-      tc_scatter<kCEN - 1>(E_prev, d, cur, nxt);
-    }
-  }
-}
-
-template <int... Ps>
-__device__ __forceinline__ void tc_layer(std::integer_sequence<int, Ps...>, TcState& st, const int* s_nodes,
-                                         const int* s_elems, const float* __restrict__ w_in,
-                                         const float* __restrict__ young, int R, int r, float (&cur)[kCX * kCY][3],
-                                         float (&nxt)[kCX * kCY][3]) {
-  float E_prev = 0.f;
-  (tc_iteration<Ps>(st, s_nodes, s_elems, w_in, young, R, r, E_prev, cur, nxt), ...);
-}
-
-// the owned nodes of point plane (ring plane) s_plane: node update with the accumulated forces
-template <int... Ps>
-__device__ __forceinline__ void tc_update_plane(std::integer_sequence<int, Ps...>, const Args& g, const int* s_plane,
-                                                int r, const float (&acc)[kCX * kCY][3], const float* __restrict__ w_in,
-                                                float* __restrict__ w_out, const float* __restrict__ vf_in,
-                                                float* __restrict__ vf_out, int step, bool rec_now) {
-  (
-      [&] {
-        const int a = s_plane[(Ps / kCX + 1) * kCHX + (Ps % kCX) + 1];
-        if (a >= 0) {
-          const float f[3][1] = {{acc[Ps][0]}, {acc[Ps][1]}, {acc[Ps][2]}};
-          node_update<1>(g, a, r, f, w_in, w_out, vf_in, vf_out, step, rec_now);
-        }
-      }(),
-      ...);
-}
-
-__global__ void __launch_bounds__(kTcThreads, 2) k_batch_step_tc(Args g, const __grid_constant__ K1Hex8 k1,
+__global__ void __launch_bounds__(kTcThreads, 1) k_batch_step_tc(Args g, const __grid_constant__ K1Hex8 k1,
                                                                  TcTables tt, const float* __restrict__ w_in,
                                                                  float* __restrict__ w_out,
                                                                  const float* __restrict__ vf_in,
                                                                  float* __restrict__ vf_out) {
+  extern __shared__ __align__(1024) float tc_dyn[];  // 3 ring planes of w, then 2 planes of accumulators
   __shared__ __align__(1024) float sB[2 * 3 * 256];  // K1 hi then lo: 3 K-slices of 32 (N) x 8 (K), 1 KB each
-  __shared__ int s_nodes[2 * kCHN];                   // ring planes k and k + 1
+  __shared__ int s_nodes[2 * kCHN];                   // ring planes k and k + 1 (node indices)
   __shared__ int s_elems[kCEN];
   __shared__ uint32_t s_tmem;
   __shared__ int s_fail;
-  __shared__ __align__(8) uint64_t s_mbar[2];
+  __shared__ __align__(8) uint64_t s_mbar[2];   // MMA completion, per TMEM buffer
+  __shared__ __align__(8) uint64_t s_pbar[3];   // plane arrival, per plane slot
+  float* planes = tc_dyn;
+  float* accs = tc_dyn + 3 * kPlaneFloats;
   const int t = threadIdx.x;
   const int R = g.d.R;
-  const int r = blockIdx.y * kTcThreads + t;
+  const int r0 = blockIdx.y * kTcThreads, r = r0 + t;
   const int col = blockIdx.x / tt.n_segs, sg = blockIdx.x - col * tt.n_segs;
   const int step = *g.t + 1;
   const bool rec_now = record_now(g, step);
+  const int* col_nodes = tt.nodes + (int64_t)col * tt.nzp * kCHN;
+  const int* col_elems = tt.elems + (int64_t)col * (tt.nzp - 1) * kCEN;
+  const int z0 = sg * tt.seg, z1 = min(z0 + tt.seg, tt.nzp);
+  const int kbeg = max(z0 - 1, 0), kend = min(z1, tt.nzp - 1);
   // K1 into the canonical K-major layout: element (k, n) of slice k / 8 at
   // (n / 8) 256 + (k % 8 / 4) 128 + (n % 8) 16 + (k % 4) 4 bytes; B[k][n] = K1[n][k], zero for n >= 24
   for (int i = t; i < 24 * 32; i += kTcThreads) {
@@ -806,60 +693,183 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_batch_step_tc(Args g, const _
     sB[off] = bh;
     sB[3 * 256 + off] = b - bh;
   }
+  for (int i = t; i < 2 * kAccFloats; i += kTcThreads) accs[i] = 0.f;
   if (t < 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&s_tmem)),
                  "r"(kTcCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
+  const uint32_t mbar0 = smem_addr(&s_mbar[0]), pbar0 = smem_addr(&s_pbar[0]);
   if (t == 0) {
     s_fail = 0;
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&s_mbar[0])));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&s_mbar[1])));
+    for (int q = 0; q < 2; ++q) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar0 + 8 * q));
+    for (int q = 0; q < 3; ++q) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(pbar0 + 8 * q));
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   tc_sync();
-  TcState st{s_tmem, smem_addr(&s_mbar[0]), smem_addr(sB), 0u, true, &s_fail};
-  const int z0 = sg * tt.seg, z1 = min(z0 + tt.seg, tt.nzp);
-  const int kbeg = max(z0 - 1, 0), kend = min(z1, tt.nzp - 1);
-  float cur[kCX * kCY][3], nxt[kCX * kCY][3];
-#pragma unroll
-  for (int p = 0; p < kCX * kCY; ++p)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) cur[p][c] = nxt[p][c] = 0.f;
-  const int* col_nodes = tt.nodes + (int64_t)col * tt.nzp * kCHN;
-  const int* col_elems = tt.elems + (int64_t)col * (tt.nzp - 1) * kCEN;
-  // every barrier below is reached by all threads: a failed wait only sets s_fail, which the
-  // threads read after a barrier, so they leave the loop together
+  const uint32_t tmem = s_tmem, sb = smem_addr(sB);
+  const uint32_t lane_base = (uint32_t)(t & ~31) << 16;  // this warp's TMEM lane quadrant
+  uint32_t mpar = 0, ppar = 0;                          // parity bits of the MMA and plane barriers
+  bool ok = true;
+  // what thread 0 started and what this thread has waited for (a failure exit drains the rest)
+  int n_commit[2] = {0, 0}, n_mwait[2] = {0, 0}, last_loaded = kbeg + 1, last_waited = kbeg - 1;
+  // planes kbeg and kbeg + 1 start arriving
+  if (t == 0) {
+    for (int z = kbeg; z <= kbeg + 1; ++z)
+      tc_load_plane(col_nodes + (int64_t)z * kCHN, w_in, R, r0, planes + (z % 3) * kPlaneFloats, pbar0 + 8 * (z % 3));
+  }
+  int cur = 0;  // accumulator plane of point plane k (the other one is k + 1)
   for (int k = kbeg; k < kend; ++k) {
-    __syncthreads();  // the previous layer's readers of s_nodes / s_elems are done
+    __syncthreads();  // the previous layer's readers of s_nodes, s_elems and plane slot (k - 1) % 3 are done
     if (s_fail) break;
     for (int i = t; i < 2 * kCHN + kCEN; i += kTcThreads) {
       if (i < 2 * kCHN) s_nodes[i] = col_nodes[(int64_t)k * kCHN + i];
       else s_elems[i - 2 * kCHN] = col_elems[(int64_t)k * kCEN + (i - 2 * kCHN)];
     }
-    __syncthreads();
-    tc_layer(std::make_integer_sequence<int, kCEN + 1>{}, st, s_nodes, s_elems, w_in, g.d.young, R, r, cur, nxt);
-    if (k >= z0)
-      tc_update_plane(std::make_integer_sequence<int, kCX * kCY>{}, g, s_nodes, r, cur, w_in, w_out, vf_in, vf_out,
-                      step, rec_now);
-#pragma unroll
-    for (int p = 0; p < kCX * kCY; ++p)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        cur[p][c] = nxt[p][c];
-        nxt[p][c] = 0.f;
+    if (k + 2 <= kend) {  // the next layer's upper plane, into the slot plane k - 1 used
+      if (t == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc_load_plane(col_nodes + (int64_t)(k + 2) * kCHN, w_in, R, r0, planes + ((k + 2) % 3) * kPlaneFloats,
+                      pbar0 + 8 * ((k + 2) % 3));
       }
+      last_loaded = k + 2;
+    }
+    __syncthreads();
+    // the update state of plane k into L2 while the layer computes (two lanes per warp cover a
+    // warp's 256 bytes of pairs)
+    if (k >= z0 && (t & 15) == 0) {
+      for (int p = 0; p < kCP; ++p) {
+        const int a = s_nodes[(p / kCX + 1) * kCHX + (p % kCX) + 1];
+        if (a < 0) continue;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const int64_t ir = ((int64_t)a * 3 + c) * R + r;
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(g.u2 + ir));
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(g.v2 + ir));
+        }
+      }
+    }
+    // planes k and k + 1 present (plane k was waited for in the previous layer, except the first)
+    for (int z = (k == kbeg ? k : k + 1); z <= k + 1 && ok; ++z) {
+      const int slot = z % 3;
+      ok = tc_wait(pbar0 + 8 * slot, (ppar >> slot) & 1);
+      ppar ^= 1u << slot;
+      last_waited = z;
+      if (!ok) s_fail = 1;
+    }
+    const float* pl[2] = {planes + (k % 3) * kPlaneFloats + t, planes + ((k + 1) % 3) * kPlaneFloats + t};
+    float* acc[2] = {accs + cur * kAccFloats + t, accs + (cur ^ 1) * kAccFloats + t};
+    float E_prev = 0.f;
+    for (int P = 0; P <= kCEN; ++P) {
+      const int e = P < kCEN ? s_elems[P] : -1;
+      const uint32_t b = P & 1;
+      float E = 0.f;
+      if (e >= 0) {
+        const short* code = c_tc_pos.code[P];
+        float hi[8], lo[8];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int kk = 8 * q + j, l = kk / 3, c = kk % 3;
+            const int cd = code[l];
+            const float x = pl[(cd >> 8) & 1][((cd & 255) * 3 + c) * kTcThreads];
+            hi[j] = tf32_hi(x);
+            lo[j] = x - hi[j];
+          }
+          tc_st8(tmem + lane_base + b * 64 + 8 * q, hi);
+          tc_st8(tmem + lane_base + b * 64 + 32 + 8 * q, lo);
+        }
+        E = __ldg(g.d.young + (int64_t)e * R + r);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      }
+      tc_sync();
+      if (e >= 0 && t == 0) {
+        const uint32_t d_col = 128 + b * 32;
+#pragma unroll
+        for (int pass = 0; pass < 3; ++pass) {
+          const uint32_t a_off = pass == 2 ? 32 : 0;        // A lo in the last pass
+          const uint32_t b_off = pass == 1 ? 3 * 1024 : 0;  // K1 lo in the middle pass
+#pragma unroll
+          for (int sl = 0; sl < 3; ++sl) {
+            const uint64_t bd = tc_sdesc(sb + b_off + sl * 1024, 128, 256);
+            const uint32_t accum = (pass | sl) ? 1u : 0u;
+            asm volatile(
+                "{\n.reg .pred pp;\nsetp.ne.u32 pp, %4, 0;\n"
+                "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, pp;\n}" ::"r"(tmem + d_col),
+                "r"(tmem + b * 64 + a_off + 8 * sl), "l"(bd), "r"(kTcIdesc), "r"(accum)
+                : "memory");
+          }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         mbar0 + 8 * b)
+                     : "memory");
+        ++n_commit[b];
+      }
+      // element P - 1: its forces into the accumulators of its owned points
+      if (P > 0 && s_elems[P - 1] >= 0 && ok) {
+        const uint32_t pb = (P - 1) & 1;
+        ok = tc_wait(mbar0 + 8 * pb, (mpar >> pb) & 1);
+        mpar ^= 1u << pb;
+        ++n_mwait[pb];
+        if (!ok) s_fail = 1;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        float d[24];
+        tc_ld24(tmem + lane_base + 128 + pb * 32, d);
+        const short* code = c_tc_pos.code[P - 1];
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+          const int cd = code[l], p = (cd >> 9) - 1;
+          if (p < 0) continue;
+          float* a = acc[(cd >> 8) & 1] + p * 3 * kTcThreads;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) a[c * kTcThreads] = fmaf(E_prev, d[3 * l + c], a[c * kTcThreads]);
+        }
+      }
+      E_prev = E;
+    }
+    if (k >= z0) {
+      for (int p = 0; p < kCP; ++p) {
+        const int a = s_nodes[(p / kCX + 1) * kCHX + (p % kCX) + 1];
+        if (a < 0) continue;
+        const float* ap = acc[0] + p * 3 * kTcThreads;
+        const float f[3][1] = {{ap[0]}, {ap[kTcThreads]}, {ap[2 * kTcThreads]}};
+        node_update<1>(g, a, r, f, w_in, w_out, vf_in, vf_out, step, rec_now);
+      }
+    }
+    for (int i = 0; i < kAccFloats; i += kTcThreads) acc[0][i] = 0.f;  // this thread's column of plane k
+    cur ^= 1;
   }
   // the top plane of the lattice (no layer above it) when it belongs to this segment
   __syncthreads();
   const bool failed = s_fail != 0;
-  if (kend < z1 && !failed)
-    tc_update_plane(std::make_integer_sequence<int, kCX * kCY>{}, g, s_nodes + kCHN, r, cur, w_in, w_out, vf_in,
-                    vf_out, step, rec_now);
-  if (failed && t == 0) atomicExch(tt.err, 1);
+  if (kend < z1 && !failed) {
+    for (int p = 0; p < kCP; ++p) {
+      const int a = s_nodes[kCHN + (p / kCX + 1) * kCHX + (p % kCX) + 1];
+      if (a < 0) continue;
+      const float* ap = accs + cur * kAccFloats + t + p * 3 * kTcThreads;
+      const float f[3][1] = {{ap[0]}, {ap[kTcThreads]}, {ap[2 * kTcThreads]}};
+      node_update<1>(g, a, r, f, w_in, w_out, vf_in, vf_out, step, rec_now);
+    }
+  }
+  // after a failure: wait (bounded) for the bulk copies and MMAs thread 0 started that nobody
+  // waited for, so none is in flight when the CTA frees its tensor memory and exits
+  if (t == 0 && failed) {
+    atomicExch(tt.err, 1);
+    for (int z = last_waited + 1; z <= last_loaded; ++z) {
+      const int slot = z % 3;
+      tc_wait(pbar0 + 8 * slot, (ppar >> slot) & 1);
+      ppar ^= 1u << slot;
+    }
+    for (int q = 0; q < 2; ++q)
+      for (; n_mwait[q] < n_commit[q]; ++n_mwait[q]) {
+        tc_wait(mbar0 + 8 * q, (mpar >> q) & 1);
+        mpar ^= 1u << q;
+      }
+  }
   tc_sync();
-  if (t < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(st.tmem), "r"(kTcCols));
+  if (t < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols));
   step_epilogue(g, step);
 }
 
@@ -977,8 +987,8 @@ static void batch_launch(const sc_batch* h, const Args& g, int grid, int rpt, in
     TcTables tt = h->tt;
     tt.seg = rpt;
     tt.n_segs = (tt.nzp + rpt - 1) / rpt;
-    k_batch_step_tc<<<dim3((unsigned)(h->n_col * tt.n_segs), (unsigned)(g.d.R / kTcThreads)), kTcThreads, 0, st>>>(
-        g, h->k1, tt, wi, wo, vi, vo);
+    k_batch_step_tc<<<dim3((unsigned)(h->n_col * tt.n_segs), (unsigned)(g.d.R / kTcThreads)), kTcThreads, kTcSmem,
+                      st>>>(g, h->k1, tt, wi, wo, vi, vo);
     return;
   }
   if (grid) {
@@ -1248,6 +1258,8 @@ extern "C" int sc_batch_set_hex8_columns(sc_batch* h, int n_col, int nzp, const 
   if (!rc) rc = check(cudaMemsetAsync(h->tc_err, 0, sizeof(int), st), "memset");
   if (!rc) rc = check(cudaMemcpyAsync(h->k1.k, h->g.d.ke1, sizeof(h->k1.k), cudaMemcpyDeviceToHost, st), "k1");
   if (!rc) rc = check(cudaStreamSynchronize(st), "sync");
+  if (!rc) rc = check(cudaFuncSetAttribute(k_batch_step_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem),
+                      "smem attribute");
   if (rc) return rc;
   h->tt.nodes = nodes;
   h->tt.elems = elems;
