@@ -255,6 +255,7 @@ def run_gb300(args):
     achieved = bytes_spmv / (ms_spmv * 1e-3) / 1e9
     traffic = profile_traffic()
     v_gpu = solver.outputs()["v"][1:W + K_steps + 1]  # receiver velocities after steps 1 .. W + K
+    residual_fp64 = solver.residual_fp64()
     solver.close()
 
     # end to end through the drop-in call: the same steps as the timed region, from a fresh
@@ -282,6 +283,7 @@ def run_gb300(args):
                      "extrapolating the accelerations, order adapted on the device, rtol 1e-12; node-block operator, "
                      "SpMV products in FP32 pairs, residual, dot products and state FP64",
            "nnz": nnz, "cg_iters_per_step": iters / K_steps, "cg_iters_max": it_max,
+           "residual": "FP64 (handed over)" if residual_fp64 else "FP32 pairs on the K pair planes",
            "setup_s": {"host_mesh_and_loads": round(t_host, 2), "gpu_assembly_lysmer_rayleigh": round(t_assembly, 3),
                        "gpu_solver_setup_fsai": round(t_solver_setup, 3)},
            "fsai_fallback_rows": solver.fsai_fallback_rows,

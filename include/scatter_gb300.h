@@ -245,8 +245,17 @@ int sc_nb_set_predictor(sc_nb_newmark* h, int order);
  * (A as hi + lo FP32 pairs, exact TwoProd/TwoSum accumulation, ~2^-46 relative per product;
  * the residual, dot products and state stay FP64).  bit 1: run the explicit scheme in FP64
  * instead of its default FP32-pair state and products (sc_nb_explicit_run); the adjoint needs
- * the default. */
+ * the default.  bit 2: always form the step's residual r = b - A x0 in FP64 (K q1 and the mass
+ * term in FP64, A x0 in pairs).  By default, with the pair SpMV, the residual is formed in one
+ * pass over K and mass pair planes as f - K (q1 + aK x0) - M (q2 + aM x0) - Cabs (y1 + aC x0),
+ * with A = aM M + aK K + aC Cabs (~48 bits per term, no FP64 product); a step that finds the
+ * elastic and inertial terms cancelling the load by more than 30x (slow motion) switches every
+ * later step to the FP64 residual, see sc_nb_residual_fp64.  Options outside 0..7 are rejected. */
 int sc_nb_set_options(sc_nb_newmark* h, int options);
+/* Whether the step's residual runs in FP64 (always with option bit 2 or the FP64 SpMV, else
+ * once the pair residual has handed over); synchronises the stream (no reference
+ * counterpart). */
+int sc_nb_residual_fp64(sc_nb_newmark* h, int* fp64);
 int sc_nb_set_force(sc_nb_newmark* h, int n_t, const int64_t* f_ptr, const int* f_slot, const double* f_val);
 int sc_nb_set_output(sc_nb_newmark* h, int out_interval, int n_rec, const int* rec_slot, double* out_u,
                      double* out_v, double* out_a, int64_t n_out);

@@ -25,6 +25,8 @@ struct Scal {
   // adaptive warm-start order: current order, probing direction, window and hold counters
   int pord, pdir, win_n, win_it, probing, hold;
   double ref_avg;  // mean iterations per step of the reference window
+  int res_fp64;       // 1: the residual runs in FP64 (for good, once the pair residual saw strong cancellation)
+  int res_fp64_next;  // set by the pair residual; k_advance copies it into res_fp64 at the end of the step
 };
 
 struct Args {
@@ -51,6 +53,13 @@ struct Args {
   const float2* APS;       // A as FP32 (hi, lo) pairs (hi + lo = A to 48 bits) for the pair-arithmetic SpMV
   const float2* KPS;       // K as FP32 pairs, for the explicit step and the adjoint (built on first use)
   float2* p2;              // p as (hi, lo) FP32 pairs, written with p
+  // the pair residual (k_residual_kp): r = f - K (q1 + aK x0) - M (q2 + aM x0) - Cabs (y1 + aC x0)
+  const float2* MSP;       // the consistent-mass plane as FP32 pairs
+  float* rrec;             // per node, what the pair residual gathers (k_predict writes it): kRecFloats
+                           // floats, at [0, 2D) q1 + aK x0 as (hi, lo) pairs, [2D, 4D) q2 + aM x0 as
+                           // pairs, [4D, 5D) q1 and [5D, 6D) q2 in FP32 (for |b| and the cancellation check)
+  double* zc;              // y1 + aC x0 (dashpot rows)
+  int res_pair;            // 1: k_predict writes the vectors above and the step runs k_residual_kp
   int spmv_pair;           // 1: PCG SpMV in FP32-pair arithmetic, 0: FP64
   int keep_l2;             // 1: matrix planes fit in L2, loaded with the default (keep) policy;
                            // 0: streamed with evict-first loads
@@ -76,6 +85,16 @@ struct Args {
   double *out_u, *out_v, *out_a;
   int64_t n_out;
 };
+
+// floats per node of the pair residual's record (whole 16-byte pieces)
+__host__ __device__ constexpr int kRecFloats(int D) { return D == 3 ? 20 : 12; }
+
+// node n's D values of an FP32 slot vector
+template <int D>
+__device__ __forceinline__ void ldvec(const float* v, int64_t n, float (&o)[D]) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) o[d] = v[n * D + d];
+}
 
 __device__ inline bool last_block(unsigned int* ticket) {
   __shared__ bool am_last;
@@ -257,6 +276,8 @@ struct sc_nb_newmark {
   cudaGraphExec_t ex_exec[2] = {nullptr, nullptr};
   cudaGraph_t ex_graph[2] = {nullptr, nullptr};
   float adj_ms[4] = {0.f, 0.f, 0.f, 0.f};  // last sc_nb_adjoint: forward, recompute, backward, reverse sweep (ms)
+  int res_pair = 1;                        // pair residual allowed (sc_nb_set_options bit 2 clears it)
+  void* res_mem[6] = {};                   // its mass pairs and vectors, made on first use
 };
 
 // sc_explicit.cu

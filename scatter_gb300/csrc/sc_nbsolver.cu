@@ -58,12 +58,16 @@ __global__ void k_predict(Args g) {
   const int p = warm_start_order(g.s, g.pred_order);
   double cf[kHistMax + 1];
   warm_start_coeffs(p, cf);
+  // while the pair residual runs, q1, q2 and the pair copy of x0 are read by no one
+  const bool fp64_res = !g.res_pair || g.s->res_fp64;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
     const double ai = g.a[i], vi = g.v[i];
     const double vp = vi + h * ai;
     const double up = g.u[i] + dt * vi + qq * ai;
-    g.q1[i] = up + g.beta_r * vp;
-    g.q2[i] = g.alpha_r * vp;
+    if (fp64_res) {
+      g.q1[i] = up + g.beta_r * vp;
+      g.q2[i] = g.alpha_r * vp;
+    }
     g.y1[i] = vp;
     // x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k}, terms summed in a fixed order
     double x0 = cf[0] * ai;
@@ -72,13 +76,29 @@ __global__ void k_predict(Args g) {
       if (k <= p) x0 += cf[k] * g.ah[k - 1][i];
     if (g.fixed[i]) x0 = 0.0;
     g.x0[i] = x0;
-    if (g.spmv_pair) g.p2[i] = split_pair(x0);  // p2 is scratch until p is first written
+    if (g.spmv_pair && fp64_res) g.p2[i] = split_pair(x0);  // p2 is scratch until p is first written
+    if (g.res_pair) {
+      const double q1 = up + g.beta_r * vp, q2 = g.alpha_r * vp;
+      const int D = g.D;
+      const int64_t node = i / D, c = i - node * D;
+      float* rec = g.rrec + node * kRecFloats(D);
+      const float2 zk = split_pair(fma(g.aK, x0, q1)), zm = split_pair(fma(g.aM, x0, q2));
+      rec[2 * c] = zk.x;
+      rec[2 * c + 1] = zk.y;
+      rec[2 * D + 2 * c] = zm.x;
+      rec[2 * D + 2 * c + 1] = zm.y;
+      rec[4 * D + c] = (float)q1;
+      rec[5 * D + c] = (float)q2;
+      g.zc[i] = fma(g.aC, x0, vp);
+    }
   }
 }
 
-// r = b - A x0 with b = f - K q1 - M q2 - Cabs y1; bb = |b|^2.  x = x0.
+// r = b - A x0 with b = f - K q1 - M q2 - Cabs y1; bb = |b|^2.  x = x0.  gate = 1: only when the
+// pair residual has handed over to this one (Scal::res_fp64), else the kernel returns at once.
 template <int D, bool kPair>
-__global__ void __launch_bounds__(kThreads) k_residual(Args g) {
+__global__ void __launch_bounds__(kThreads) k_residual(Args g, int gate) {
+  if (gate && !g.s->res_fp64) return;
   __shared__ double sh[32];
   double pbb = 0.0;
   SELL_ROW_LOOP(g.sf_ptr) {
@@ -189,6 +209,111 @@ __global__ void __launch_bounds__(kThreads) k_residual(Args g) {
   }
 }
 
+// The residual in FP32-pair arithmetic, one pass over the K pair planes and the mass pairs.
+// With A = aM M + aK K + aC Cabs,
+//   r = b - A x0 = f - K (q1 + aK x0) - M (q2 + aM x0) - Cabs (y1 + aC x0),
+// so r needs no A pass and no FP64 product: the pair products keep about 48 bits, and r is
+// exact to that rounding of its own terms.  b = f - K q1 - M q2 - Cabs y1 only scales the
+// tolerance, so it is formed from the pairs' hi parts in FP32.  When the elastic and inertial
+// terms cancel the load strongly (|K q1 + M q2| above kResRatio |b|, slow motion), 48 bits of
+// the terms would no longer carry r to the tolerance: the last block then sets
+// Scal::res_fp64 and every later step runs the FP64 residual instead (this step's r is still
+// good to about kResRatio 2^-48 of |b|).  gate: returns at once when res_fp64 is set.
+constexpr double kResRatio = 30.0;
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_residual_kp(Args g) {
+  if (g.s->res_fp64) return;
+  __shared__ double sh[32];
+  double pbb = 0.0, pkq = 0.0;
+  SELL_ROW_LOOP(g.sf_ptr) {
+    SELL_ROW_BEGIN(g.sf_ptr)
+    float rh[D], rl[D], bq[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) rh[c] = rl[c] = bq[c] = 0.f;
+    for (int64_t q = 0; q < nq; ++q) {
+      int cl[4];
+      cols4(g.sf_col, p0 + 128 * q, cl, g.keep_l2);
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {  // two entries at a time (registers)
+        const int64_t pos = p0 + 128 * q + 2 * hh;
+        float2 zk[2][D], zm[2][D];
+        float q1[2][D], q2[2][D];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          constexpr int NV = kRecFloats(D) / 4;
+          const float4* rp = reinterpret_cast<const float4*>(g.rrec + (int64_t)cl[2 * hh + e] * kRecFloats(D));
+          float rv[4 * NV];
+#pragma unroll
+          for (int k = 0; k < NV; ++k) {
+            const float4 a = rp[k];
+            rv[4 * k] = a.x; rv[4 * k + 1] = a.y; rv[4 * k + 2] = a.z; rv[4 * k + 3] = a.w;
+          }
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            zk[e][d] = make_float2(rv[2 * d], rv[2 * d + 1]);
+            zm[e][d] = make_float2(rv[2 * D + 2 * d], rv[2 * D + 2 * d + 1]);
+            q1[e][d] = rv[4 * D + d];
+            q2[e][d] = rv[5 * D + d];
+          }
+        }
+        float2 m2[2];
+        ld2(g.MSP + pos, m2, g.keep_l2);
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          pair_fma(m2[0].x, m2[0].y, zm[0][c], rh[c], rl[c]);
+          pair_fma(m2[1].x, m2[1].y, zm[1][c], rh[c], rl[c]);
+          bq[c] = fmaf(m2[1].x, q2[1][c], fmaf(m2[0].x, q2[0][c], bq[c]));
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            float2 k2[2];
+            ld2(g.KPS + (int64_t)(c * D + d) * g.sf_n + pos, k2, g.keep_l2);
+            pair_fma(k2[0].x, k2[0].y, zk[0][d], rh[c], rl[c]);
+            pair_fma(k2[1].x, k2[1].y, zk[1][d], rh[c], rl[c]);
+            bq[c] = fmaf(k2[1].x, q1[1][d], fmaf(k2[0].x, q1[0][d], bq[c]));
+          }
+        }
+      }
+    }
+    if (row < g.n_nodes) {
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        const int64_t i = row * D + c;
+        double bv = 0.0, rv = 0.0;
+        if (!g.fixed[i]) {
+          double cb = 0.0, cz = 0.0;  // Lysmer dashpots (boundary rows only)
+          for (int64_t k = g.cab_ptr[i]; k < g.cab_ptr[i + 1]; ++k) {
+            const int jj = g.cab_col[k];
+            cb = fma(g.cab_val[k], g.y1[jj], cb);
+            cz = fma(g.cab_val[k], g.zc[jj], cz);
+          }
+          bv = g.f[i] - (double)bq[c] - cb;
+          rv = g.f[i] - ((double)rh[c] + (double)rl[c]) - cz;
+          pkq += (double)bq[c] * (double)bq[c];
+        }
+        g.r[i] = rv;
+        g.r32[i] = (float)rv;
+        g.x[i] = g.x0[i];
+        pbb += bv * bv;
+      }
+    }
+  }
+  double t = block_sum(pbb, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 2] = t;
+  t = block_sum(pkq, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 3] = t;
+  if (last_block(&g.s->ticket)) {
+    const double bb = reduce_parts(g.part, 2, sh);
+    const double kq = reduce_parts(g.part, 3, sh);
+    if (threadIdx.x == 0) {
+      g.s->bb = bb;
+      if (kq > kResRatio * kResRatio * bb) g.s->res_fp64_next = 1;  // k_advance makes it current
+      g.s->it = 0;
+      g.s->ticket = 0;
+    }
+  }
+}
+
 // t = G r  (lower pattern, FP16 factor planes, FP32 products and result)
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_prec_lower(Args g) {
@@ -203,9 +328,7 @@ __global__ void __launch_bounds__(kThreads) k_prec_lower(Args g) {
       cols4(g.sl_col, pos, cl, g.keep_l2);
       float ra[4][D];
 #pragma unroll
-      for (int e = 0; e < 4; ++e)
-#pragma unroll
-        for (int d = 0; d < D; ++d) ra[e][d] = g.r32[(int64_t)cl[e] * D + d];
+      for (int e = 0; e < 4; ++e) ldvec<D>(g.r32, cl[e], ra[e]);
 #pragma unroll
       for (int c = 0; c < D; ++c)
 #pragma unroll
@@ -240,9 +363,7 @@ __global__ void __launch_bounds__(kThreads) k_prec_upper(Args g, int mode, cudaG
       cols4(g.su_col, pos, cl, g.keep_l2);
       float ta[4][D];
 #pragma unroll
-      for (int e = 0; e < 4; ++e)
-#pragma unroll
-        for (int d = 0; d < D; ++d) ta[e][d] = g.t32[(int64_t)cl[e] * D + d];
+      for (int e = 0; e < 4; ++e) ldvec<D>(g.t32, cl[e], ta[e]);
 #pragma unroll
       for (int c = 0; c < D; ++c)
 #pragma unroll
@@ -306,6 +427,9 @@ __global__ void __launch_bounds__(kThreads) k_prec_upper_nograph(Args g) {
       const int64_t pos = p0 + 128 * q;
       int cl[4];
       cols4(g.su_col, pos, cl, g.keep_l2);
+      float ta[4][D];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) ldvec<D>(g.t32, cl[e], ta[e]);
 #pragma unroll
       for (int c = 0; c < D; ++c)
 #pragma unroll
@@ -313,7 +437,7 @@ __global__ void __launch_bounds__(kThreads) k_prec_upper_nograph(Args g) {
           float gv[4];
           ld4(g.GTS + (int64_t)(c * D + d) * g.su_n + pos, gv, g.keep_l2);
 #pragma unroll
-          for (int e = 0; e < 4; ++e) s[c] = fmaf(gv[e], g.t32[(int64_t)cl[e] * D + d], s[c]);
+          for (int e = 0; e < 4; ++e) s[c] = fmaf(gv[e], ta[e][d], s[c]);
         }
     }
     if (row < g.n_nodes) {
@@ -534,6 +658,7 @@ __global__ void k_advance(Args g) {
     s->total_iters += s->it;
     if (s->it > s->max_seen) s->max_seen = s->it;
     s->t += 1;
+    if (s->res_fp64_next) s->res_fp64 = 1;  // the next step's predictor and residual see it
     warm_start_advance(s, g.pred_order);
   }
 }
@@ -822,6 +947,7 @@ __global__ void k_init_scal(Scal* s, double tol2, int max_it) {
   s->t = 0;
   s->fsai_fallback = 0;
   s->ticket = 0;
+  s->res_fp64 = s->res_fp64_next = 0;
   warm_start_init(s);
 }
 
@@ -860,8 +986,14 @@ int build_graph(sc_nb_newmark* h) {
       break;
     k_force<<<1, 256, 0, cs>>>(g);
     k_predict<<<vbk, 256, 0, cs>>>(g);
-    if (g.spmv_pair) k_residual<D, true><<<nbk, kThreads, 0, cs>>>(g);
-    else k_residual<D, false><<<nbk, kThreads, 0, cs>>>(g);
+    if (g.res_pair) {
+      k_residual_kp<D><<<nbk, kThreads, 0, cs>>>(g);
+      k_residual<D, true><<<nbk, kThreads, 0, cs>>>(g, 1);
+    } else if (g.spmv_pair) {
+      k_residual<D, true><<<nbk, kThreads, 0, cs>>>(g, 0);
+    } else {
+      k_residual<D, false><<<nbk, kThreads, 0, cs>>>(g, 0);
+    }
     k_prec_lower<D><<<nbk, kThreads, 0, cs>>>(g);
     k_prec_upper<D, 0><<<nbk, kThreads, 0, cs>>>(g, 1, hc);
     cudaStreamCaptureStatus stt;
@@ -1164,9 +1296,10 @@ extern "C" int sc_nb_set_predictor(sc_nb_newmark* h, int order) {
 }
 
 extern "C" int sc_nb_set_options(sc_nb_newmark* h, int options) {
-  if (!h) return SC_BAD_ARG;
+  if (!h || options < 0 || options > 7) return SC_BAD_ARG;
   h->g.spmv_pair = (options & 1) ? 0 : 1;
   h->explicit_pair = (options & 2) ? 0 : 1;
+  h->res_pair = (options & 4) ? 0 : 1;
   drop_graph(h);
   drop_explicit_graphs(h);
   return SC_OK;
@@ -1215,8 +1348,14 @@ static int eager_step(sc_nb_newmark* h) {
   cudaGraphConditionalHandle none = 0;
   k_force<<<1, 256, 0, st>>>(g);
   k_predict<<<vbk, 256, 0, st>>>(g);
-  if (g.spmv_pair) k_residual<D, true><<<nbk, kThreads, 0, st>>>(g);
-  else k_residual<D, false><<<nbk, kThreads, 0, st>>>(g);
+  if (g.res_pair) {
+    k_residual_kp<D><<<nbk, kThreads, 0, st>>>(g);
+    k_residual<D, true><<<nbk, kThreads, 0, st>>>(g, 1);
+  } else if (g.spmv_pair) {
+    k_residual<D, true><<<nbk, kThreads, 0, st>>>(g, 0);
+  } else {
+    k_residual<D, false><<<nbk, kThreads, 0, st>>>(g, 0);
+  }
   k_prec_lower<D><<<nbk, kThreads, 0, st>>>(g);
   k_prec_upper<D, 1><<<nbk, kThreads, 0, st>>>(g, 1, none);
   int done = 0;
@@ -1239,9 +1378,43 @@ static int eager_step(sc_nb_newmark* h) {
   return check_launch("eager step");
 }
 
+// The pair residual's planes and vectors, made on first use: K as pairs (shared with the explicit
+// scheme), the mass plane as pairs, the per-node records and zc.  It runs with the pair SpMV only.
+static int residual_prepare(sc_nb_newmark* h) {
+  Args& g = h->g;
+  const int want = h->res_pair && g.spmv_pair ? 1 : 0;
+  if (want == g.res_pair && (!want || h->res_mem[0])) return SC_OK;
+  g.res_pair = 0;
+  if (!want) return SC_OK;
+  cudaStream_t st = h->user;
+  const int64_t ns = g.n_s, n2 = (int64_t)g.D * g.D * g.sf_n;
+  int rc;
+  auto M = [&](void** p, size_t b) { return check(cudaMallocAsync(p, b, st), "residual malloc"); };
+  if (!h->KPS) {
+    if ((rc = M((void**)&h->KPS, 8 * n2))) return rc;
+    k_split_pairs<<<grid_for(n2, 256, 152 * 32), 256, 0, st>>>(n2, g.KS, h->KPS);
+  }
+  g.KPS = h->KPS;
+  if (!h->res_mem[0]) {
+    const size_t sizes[3] = {(size_t)(8 * g.sf_n), (size_t)(4 * (int64_t)g.n_nodes * kRecFloats(g.D)),
+                             (size_t)(8 * ns)};
+    for (int k = 0; k < 3; ++k)
+      if ((rc = M(&h->res_mem[k], sizes[k]))) return rc;
+    k_split_pairs<<<grid_for(g.sf_n, 256, 152 * 32), 256, 0, st>>>(g.sf_n, g.MSS, (float2*)h->res_mem[0]);
+    cudaMemsetAsync(h->res_mem[1], 0, sizes[1], st);  // the records' pad floats
+  }
+  g.MSP = (const float2*)h->res_mem[0];
+  g.rrec = (float*)h->res_mem[1];
+  g.zc = (double*)h->res_mem[2];
+  g.res_pair = 1;
+  drop_graph(h);
+  return check_launch("residual prepare");
+}
+
 extern "C" int sc_nb_run(sc_nb_newmark* h, int t_begin, int t_end) {
   if (!h || t_begin < 0 || t_end < t_begin) return SC_BAD_ARG;
   int rc;
+  if ((rc = residual_prepare(h))) return rc;
   const char* eager = getenv("SCATTER_GB300_EAGER");
   if (eager && eager[0] == '1') {
     cudaStream_t st = h->user;
@@ -1360,7 +1533,8 @@ __global__ void k_copy(int64_t n, const double* __restrict__ x, double* __restri
     y[i] = x[i];
 }
 
-__global__ void k_copy_r(int64_t n, const double* __restrict__ x, double* __restrict__ r, float* __restrict__ r32) {
+__global__ void k_copy_r(int64_t n, int D, const double* __restrict__ x, double* __restrict__ r,
+                         float* __restrict__ r32) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     r[i] = x[i];
     r32[i] = (float)x[i];
@@ -1379,7 +1553,7 @@ extern "C" int sc_nb_apply(sc_nb_newmark* h, int which, const double* x, double*
     case 4: k_apply_cab<<<grid_for(g.n_s, 256), 256, 0, st>>>(g, x, y); break;
     case 3: {
       // r <- x, t = G r, z = G^T t (the solver's own kernels), y <- z
-      k_copy_r<<<grid_for(g.n_s, 256), 256, 0, st>>>(g.n_s, x, g.r, g.r32);
+      k_copy_r<<<grid_for(g.n_s, 256), 256, 0, st>>>(g.n_s, g.D, x, g.r, g.r32);
       if (g.D == 3) {
         k_prec_lower<3><<<h->node_blocks, kThreads, 0, st>>>(g);
         k_prec_upper_nograph<3><<<h->node_blocks, kThreads, 0, st>>>(g);
@@ -1396,11 +1570,24 @@ extern "C" int sc_nb_apply(sc_nb_newmark* h, int which, const double* x, double*
   return rc;
 }
 
+extern "C" int sc_nb_residual_fp64(sc_nb_newmark* h, int* fp64) {
+  if (!h || !fp64) return SC_BAD_ARG;
+  int rc = check(cudaStreamSynchronize(h->user), "sync");
+  if (rc) return rc;
+  Scal s;
+  if ((rc = check(cudaMemcpy(&s, h->g.s, sizeof(s), cudaMemcpyDeviceToHost), "read"))) return rc;
+  *fp64 = h->g.res_pair ? s.res_fp64 : 1;
+  return SC_OK;
+}
+
 extern "C" int sc_nb_destroy(sc_nb_newmark* h) {
   if (!h) return SC_OK;
   drop_graph(h);
   drop_explicit_graphs(h);
   for (int i = 0; i < h->n_sell_mem; ++i) cudaFree(h->sell_mem[i]);
+  cudaStreamSynchronize(h->user);
+  for (void* q : h->res_mem)
+    if (q) cudaFree(q);
   free_explicit(h);
   if (h->cap) cudaStreamDestroy(h->cap);
   if (h->cap2) cudaStreamDestroy(h->cap2);

@@ -219,7 +219,8 @@ class NodeBlockNewmark:
     State in slot space (slot = node * dim + dof); the eq <-> slot maps translate force
     entries, receivers and outputs from/to the reference's equation numbering."""
 
-    def __init__(self, g, dt, rtol=1e-12, max_iter=1000, precond="fsai", spmv="pair", explicit="pair"):
+    def __init__(self, g, dt, rtol=1e-12, max_iter=1000, precond="fsai", spmv="pair", explicit="pair",
+                 residual="pair"):
         if g.adj_ptr is None:
             raise ValueError("GenerateMatrix has no node structure")
         self.g = g
@@ -268,8 +269,17 @@ class NodeBlockNewmark:
                  {"fsai": 0, "jacobi": 1}[precond], self.u.data_ptr(), self.v.data_ptr(), self.a.data_ptr(), self.ws.data_ptr(), wsb, dv.stream_ptr())
         self.h = h
         self.dt = dt
-        # bit 0: PCG SpMV in FP64 instead of FP32 pairs; bit 1: explicit K w in FP64
-        nat.call("sc_nb_set_options", self.h, {"pair": 0, "fp64": 1}[spmv] | {"pair": 0, "fp64": 2}[explicit])
+        # bit 0: PCG SpMV in FP64 instead of FP32 pairs; bit 1: explicit K w in FP64; bit 2: the
+        # step's residual always in FP64 (by default it runs in pairs and hands over to FP64 by
+        # itself when the load is nearly balanced by the elastic and inertial forces)
+        nat.call("sc_nb_set_options", self.h, {"pair": 0, "fp64": 1}[spmv] | {"pair": 0, "fp64": 2}[explicit] |
+                 {"pair": 0, "fp64": 4}[residual])
+
+    def residual_fp64(self):
+        """True when the step's residual runs in FP64 (synchronises)."""
+        f = ctypes.c_int()
+        nat.call("sc_nb_residual_fp64", self.h, ctypes.byref(f))
+        return bool(f.value)
 
     def set_predictor(self, order):
         """Order (1..8) of the extrapolated accelerations each step's PCG starts from; 0 (the
@@ -412,10 +422,11 @@ class NewmarkExplicit:
     device (pinned memory) instead of the whole history at set-up.  ``close()`` frees the
     device solver."""
 
-    def __init__(self, rtol=1e-12, max_iter=1000, layout="node-block", spmv="pair"):
+    def __init__(self, rtol=1e-12, max_iter=1000, layout="node-block", spmv="pair", residual="pair"):
         self.output_interval = 1
         self.layout = layout  # "node-block" (matrices from GenerateMatrix) or "csr"
         self.spmv = spmv  # node-block PCG operator arithmetic: "pair" (FP32 pairs) or "fp64"
+        self.residual = residual  # node-block step residual: "pair" (hands over to FP64 by itself) or "fp64"
         self.update_rhs_at_time_step_func = None
         self.rtol = rtol
         self.max_iter = max_iter
@@ -480,7 +491,8 @@ class NewmarkExplicit:
             if kind == "csr":
                 solver = NewmarkGPU(pat, Md, Cd, Kd, dt, self.rtol, self.max_iter)
             else:
-                solver = NodeBlockNewmark(g, dt, self.rtol, self.max_iter, precond=kind, spmv=self.spmv)
+                solver = NodeBlockNewmark(g, dt, self.rtol, self.max_iter, precond=kind, spmv=self.spmv,
+                                          residual=self.residual)
             solver.set_force(table, stream=self.stream_force)
             solver.set_output(self.output_interval, rec, n_out)
             if ic is not None:
@@ -509,7 +521,7 @@ class NewmarkExplicit:
         else:
             g = generator_of(M, C, K)
         key = (id(g) if g is not None else (id(M), id(C), id(K)), id(self.time), id(self.force_table),
-               self.layout, self.spmv, self.output_interval)
+               self.layout, self.spmv, self.residual, self.output_interval)
         live = self._live
         if live is not None and live[0] == key and t_start_idx == live[2] and t_end_idx >= t_start_idx:
             solver = live[1]

@@ -81,3 +81,9 @@ def test_status_strings_are_distinct(lib):
     texts = [lib.sc_status_string(c) for c in range(6)]
     assert len(set(texts)) == 6 and all(texts)
     assert lib.sc_status_string(99) == b"unknown status"
+
+
+def test_node_block_option_and_residual_checks(lib):
+    assert lib.sc_nb_set_options(None, 0) == SC_BAD_ARG
+    flag = ctypes.c_int()
+    assert lib.sc_nb_residual_fp64(None, ctypes.byref(flag)) == SC_BAD_ARG

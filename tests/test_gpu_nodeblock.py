@@ -170,3 +170,55 @@ def test_csr_warm_start_order_changes_iterations_not_the_answer(cuda):
     for order, (u, _) in runs.items():
         assert rel_l2(u, ref) <= 1e-10, order
     assert runs[0][1] < runs[1][1]
+
+
+@pytest.mark.parametrize("residual", ["pair", "fp64"])
+def test_residual_arithmetic_and_handover(cuda, residual):
+    """The step's residual in pair arithmetic (default) and in FP64 (option), on the small
+    column settling under a constant top load with heavy Rayleigh damping: once the elastic
+    forces carry the load (slow motion), the pair residual hands over to the FP64 one, and both
+    arithmetics reach the oracle's direct solve to 1e-10 (u, v).  A wave step (the first ones)
+    stays in pairs."""
+    import column_case as cc
+    from oracle import assembly as asm
+    from oracle import newmark
+    from scatter_gb300.solvers import NodeBlockNewmark
+    from scatter_gb300.system_matrix import GenerateMatrix
+
+    damping = [1, 0.9, 50, 0.9]
+    m, _, _, top_eq = cc.build()
+    g = GenerateMatrix(m.number_eq, 2)
+    g.generate_stiffness_and_mass(m, cc.MATS)
+    g.absorbing_boundaries(m, cc.MATS, [1, 1], 1e3)
+    g.damping_Rayleigh(damping)
+    dt, n_t = 1e-3, 1500
+    time = np.linspace(0, dt * (n_t - 1), n_t)
+    from scatter_gb300.force_external import Force
+
+    top = m.top_nodes()
+    load = {"type": "heaviside", "force": [0, -cc.P0 / len(top), 0], "node": list(top), "time": time[-1],
+            "ini_steps": 5}
+    F = Force()
+    F.initialise_load(load, time, m, None)
+    s = NodeBlockNewmark(g, dt, residual=residual)
+    s.set_force(F.table)
+    s.set_output(1, np.arange(m.number_eq), n_t)
+    s.initial_acceleration()
+    s.run(0, 10)
+    early = s.residual_fp64()
+    s.run(10, n_t - 1)
+    rc, _, _ = s.status()
+    assert rc == 0
+    late = s.residual_fp64()
+    out = s.outputs()
+    s.close()
+    if residual == "pair":
+        assert not early and late  # waves first, then the settled column hands over
+    else:
+        assert early and late
+    M, C, K = cc.oracle_matrices(m)
+    C = asm.rayleigh(M, K, M * 0, damping)
+    Fd = np.stack([F.table.dense(t) for t in range(n_t)])
+    U, V, _, _ = newmark.solve(M, C, K, Fd, time, 1)
+    assert rel_l2(out["u"], U) <= 1e-10
+    assert rel_l2(out["v"], V) <= 1e-10

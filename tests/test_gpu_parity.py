@@ -287,8 +287,9 @@ def test_newmark_not_converged_status(torch_cuda):
     assert ei.value.code == 2
 
 
-@pytest.mark.parametrize("element,spmv", [("hexa8", "pair"), ("hexa8", "fp64"), ("tetra10", "pair")])
-def test_node_block_box_lysmer_moving_load(torch_cuda, element, spmv):
+@pytest.mark.parametrize("element,spmv,residual", [("hexa8", "pair", "pair"), ("hexa8", "pair", "fp64"),
+                                                    ("hexa8", "fp64", "fp64"), ("tetra10", "pair", "pair")])
+def test_node_block_box_lysmer_moving_load(torch_cuda, element, spmv, residual):
     """Box with Lysmer dashpots on sides and base and a moving point load (the benchmark's
     physics at small size): node-block GPU loop vs the oracle's direct-solve Newmark."""
     from oracle import assembly as asm
@@ -322,7 +323,7 @@ def test_node_block_box_lysmer_moving_load(torch_cuda, element, spmv):
         top = []
     F = Force()
     F.initialise_load(load, time, m, None, top_surface_elements=top)
-    s = NewmarkExplicit(spmv=spmv)
+    s = NewmarkExplicit(spmv=spmv, residual=residual)
     s.initialise(m.number_eq, time)
     s.force_table = F.table
     s.calculate(g, g, g, F.force_vector, 0, n_t - 1)
