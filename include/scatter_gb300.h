@@ -181,6 +181,11 @@ int sc_newmark_run(sc_newmark* h, int t_begin, int t_end);
 /* Warm start of each step (no reference counterpart), as sc_nb_set_predictor: order 1..8
  * fixed, 0 adaptive (the default); 1..8 then 0 keeps the history entries that are current. */
 int sc_newmark_set_predictor(sc_newmark* h, int order);
+/* options bit 0: run the PCG SpMV in FP64 (one FP64 FMA per stored value) instead of the
+ * default FP32-pair arithmetic (A and M copied once as hi + lo FP32 pairs, 8 bytes per value
+ * like FP64, products and the row sum by exact TwoProd/TwoSum, about 48 bits; the residual,
+ * dot products and state stay FP64).  No reference counterpart. */
+int sc_newmark_set_options(sc_newmark* h, int options);
 /* synchronous: CG status of the run so far (SC_OK / SC_NOT_CONVERGED / SC_BREAKDOWN),
  * total and maximum CG iterations per step */
 int sc_newmark_status(sc_newmark* h, int64_t* total_iters, int* max_iters_per_step);
@@ -236,7 +241,7 @@ int sc_nb_create(sc_nb_newmark** h, int n_nodes, int dim, const int* eqmap, cons
 /* Warm start of each Newmark step (no reference counterpart): the PCG starts from the
  * polynomial extrapolation of order p of the previous accelerations,
  * x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k} (p = 2: 3 a_n - 3 a_{n-1} + a_{n-2}).  order 1..8
- * fixes p; 0 (the default) adapts it on the device: starting from 4 it moves to a neighbouring
+ * fixes p; 0 (the default) adapts it on the device: starting from 6 it moves to a neighbouring
  * order while the mean PCG iterations over windows of 16 steps fall, steps back when they
  * rise, and holds 8 windows before probing again.  The order changes the iteration count,
  * not the answer, which meets the same tolerance. */

@@ -70,7 +70,7 @@ constexpr int kHistMax = 8;  // acceleration history kept for the warm start
 // order control (fixed order 0 = adaptive): start at kPredStart, then compare the mean PCG
 // iterations of windows of kPredWin steps, keep climbing while a probed neighbour order is
 // better, step back when it is worse and hold there kPredHold windows
-constexpr int kPredStart = 4, kPredWin = 16, kPredHold = 8;
+constexpr int kPredStart = 6, kPredWin = 16, kPredHold = 8;
 
 // cf[k] = (-1)^k C(p+1, k+1) for k <= p, 0 beyond: exact integers, in a fixed order
 __device__ __forceinline__ void warm_start_coeffs(int p, double* cf) {
@@ -150,6 +150,34 @@ __device__ inline void warm_start_advance(S* s, int fixed) {
       s->pdir = -s->pdir;
     }
   }
+}
+
+// (hi, lo) FP32 pair of a double: hi + lo reproduces x to 48 bits
+__device__ inline float2 split_pair(double x) {
+  const float hi = (float)x;
+  return make_float2(hi, (float)(x - (double)hi));
+}
+
+// hi/lo accumulation of a * p in FP32-pair arithmetic (a = ah + al, p = p.x + p.y): the
+// product's rounding error (fmaf) and the sum's (two-sum) go to lo; _rn intrinsics keep the
+// compiler from contracting the error terms
+__device__ __forceinline__ void pair_fma(float ah, float al, float2 pv, float& hi, float& lo) {
+  const float pr = __fmul_rn(ah, pv.x);
+  const float pe = fmaf(ah, pv.x, -pr);
+  const float t = __fadd_rn(hi, pr);
+  const float bp = __fsub_rn(t, hi);
+  const float e2 = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(pr, bp));
+  hi = t;
+  lo += (pe + e2) + fmaf(ah, pv.y, al * pv.x);
+}
+
+// (hi, lo) += (h2, l2), the rounding error of the hi sum kept in lo
+__device__ __forceinline__ void pair_add(float& hi, float& lo, float h2, float l2) {
+  const float t = __fadd_rn(hi, h2);
+  const float bp = __fsub_rn(t, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(h2, bp));
+  hi = t;
+  lo = __fadd_rn(__fadd_rn(lo, l2), e);
 }
 
 }  // namespace sc

@@ -125,11 +125,6 @@ __device__ inline void warp_sum3(double* s) {
   for (int c = 0; c < D; ++c) s[c] = warp_sum(s[c]);
 }
 
-// (hi, lo) FP32 pair of a double: hi + lo reproduces x to 48 bits
-__device__ inline float2 split_pair(double x) {
-  const float hi = (float)x;
-  return make_float2(hi, (float)(x - (double)hi));
-}
 
 // Per-step block kernels: one thread per node row over the sliced-ELL copies.  A warp is one
 // slice of 32 consecutive node rows.  The slice's width W (its longest row, rounded up to a
@@ -192,28 +187,6 @@ __device__ __forceinline__ void ld2(const float2* p, float2 (&v)[2], int keep) {
 #define SELL_ROW_LOOP_T(tpr)                                                                            \
   for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / (tpr); row < g.n_slices * 32; \
        row += (int64_t)gridDim.x * blockDim.x / (tpr))
-
-// hi/lo accumulation of a * p in FP32-pair arithmetic (a = ah + al, p = p.x + p.y): the
-// product's rounding error (fmaf) and the sum's (two-sum) go to lo; _rn intrinsics keep the
-// compiler from contracting the error terms
-__device__ __forceinline__ void pair_fma(float ah, float al, float2 pv, float& hi, float& lo) {
-  const float pr = __fmul_rn(ah, pv.x);
-  const float pe = fmaf(ah, pv.x, -pr);
-  const float t = __fadd_rn(hi, pr);
-  const float bp = __fsub_rn(t, hi);
-  const float e2 = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(pr, bp));
-  hi = t;
-  lo += (pe + e2) + fmaf(ah, pv.y, al * pv.x);
-}
-
-// (hi, lo) += (h2, l2), the rounding error of the hi sum kept in lo
-__device__ __forceinline__ void pair_add(float& hi, float& lo, float h2, float l2) {
-  const float t = __fadd_rn(hi, h2);
-  const float bp = __fsub_rn(t, hi);
-  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(h2, bp));
-  hi = t;
-  lo = __fadd_rn(__fadd_rn(lo, l2), e);
-}
 
 // combine the TPR lanes' partial sums of a row; every lane ends with the group leader's result
 template <int TPR>

@@ -71,6 +71,7 @@ struct NmArgs {
   const int* rec_eq;
   double *out_u, *out_v, *out_a;
   int64_t n_out;
+  float2* p2;  // p as (hi, lo) FP32 pairs for the pair SpMV, written with p (null: FP64 SpMV)
 };
 
 // returns true in every thread of the last block to arrive
@@ -155,6 +156,7 @@ __global__ void __launch_bounds__(kRowThreads) k_residual(NmArgs g, const double
       g.r[row] = r;
       g.z[row] = z;
       g.p[row] = z;
+      if (g.p2) g.p2[row] = split_pair(z);
       prz += r * z;
       prr += r * r;
       pbb += rhs * rhs;
@@ -184,9 +186,12 @@ __global__ void __launch_bounds__(kRowThreads) k_residual(NmArgs g, const double
 }
 
 // w = Op p ; partial p.w ; last block: alpha = rz / pw.  kInGraph = false is the same
-// kernel for standalone timing (it does not touch the graph conditional).
-template <bool kInGraph>
+// kernel for standalone timing (it does not touch the graph conditional).  kPair: the operator
+// as FP32 (hi, lo) pairs (Op2, 8 bytes per value like FP64) and p as pairs (g.p2); the products
+// and the row's 4-lane sum in pair arithmetic (about 48 bits), no FP64 instruction per entry.
+template <bool kInGraph, bool kPair>
 __global__ void __launch_bounds__(kRowThreads) k_spmv(NmArgs g, const double* __restrict__ Op,
+                                                      const float2* __restrict__ Op2,
                                                       cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
   const int lane = threadIdx.x & 31, sub = lane % kRowLanes;
@@ -197,11 +202,28 @@ __global__ void __launch_bounds__(kRowThreads) k_spmv(NmArgs g, const double* __
     const int64_t row = rb + lane / kRowLanes;
     const bool live = row < g.n;
     double s = 0.0;
-    if (live) {
-      const int64_t k0 = g.rowptr[row], k1 = g.rowptr[row + 1];
-      for (int64_t k = k0 + sub; k < k1; k += kRowLanes) s = fma(__ldcs(Op + k), g.p[__ldcs(g.cols + k)], s);
+    if (kPair) {
+      float hi = 0.f, lo = 0.f;
+      if (live) {
+        const int64_t k0 = g.rowptr[row], k1 = g.rowptr[row + 1];
+        for (int64_t k = k0 + sub; k < k1; k += kRowLanes) {
+          const float2 a = __ldcs(Op2 + k);
+          pair_fma(a.x, a.y, g.p2[__ldcs(g.cols + k)], hi, lo);
+        }
+      }
+#pragma unroll
+      for (int o = 1; o < kRowLanes; o <<= 1) {
+        const float h2 = __shfl_xor_sync(0xffffffffu, hi, o), l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+        pair_add(hi, lo, h2, l2);
+      }
+      s = (double)hi + (double)lo;
+    } else {
+      if (live) {
+        const int64_t k0 = g.rowptr[row], k1 = g.rowptr[row + 1];
+        for (int64_t k = k0 + sub; k < k1; k += kRowLanes) s = fma(__ldcs(Op + k), g.p[__ldcs(g.cols + k)], s);
+      }
+      s = row_sum(s);
     }
-    s = row_sum(s);
     if (live && sub == 0) {
       g.w[row] = s;
       ppw += g.p[row] * s;
@@ -270,8 +292,16 @@ __global__ void k_update(NmArgs g, cudaGraphConditionalHandle hc) {
 
 __global__ void k_direction(NmArgs g) {
   const double beta = g.s->beta;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x)
-    g.p[i] = fma(beta, g.p[i], g.z[i]);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double pv = fma(beta, g.p[i], g.z[i]);
+    g.p[i] = pv;
+    if (g.p2) g.p2[i] = split_pair(pv);
+  }
+}
+
+__global__ void k_to_pairs(int64_t n, const double* __restrict__ x, float2* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = split_pair(x[i]);
 }
 
 __device__ inline void record(const NmArgs& g, int step) {
@@ -371,6 +401,9 @@ struct sc_newmark {
   cudaGraphExec_t step_exec = nullptr, init_exec = nullptr;
   cudaGraph_t step_graph = nullptr, init_graph = nullptr;
   double rtol = 1e-12;
+  int pair = 1;                                 // SpMV in FP32-pair arithmetic (sc_newmark_set_options bit 0 clears)
+  float2 *AP = nullptr, *MP = nullptr;          // A and M as pairs, made with the first graph
+  float2* p2 = nullptr;
 };
 
 namespace {
@@ -417,7 +450,12 @@ int build_pcg_graph(sc_newmark* h, const double* Op, int mode, cudaGraph_t* grap
                                                   cudaStreamCaptureModeThreadLocal),
                     "capture body")))
       break;
-    k_spmv<true><<<h->row_blocks, kRowThreads, 0, h->cap2>>>(g, Op, hc);
+    if (g.p2) {
+      const float2* Op2 = Op == g.M ? h->MP : h->AP;
+      k_spmv<true, true><<<h->row_blocks, kRowThreads, 0, h->cap2>>>(g, Op, Op2, hc);
+    } else {
+      k_spmv<true, false><<<h->row_blocks, kRowThreads, 0, h->cap2>>>(g, Op, nullptr, hc);
+    }
     k_update<<<h->vec_blocks, 256, 0, h->cap2>>>(g, hc);
     k_direction<<<h->vec_blocks, 256, 0, h->cap2>>>(g);
     cudaGraph_t body_out = nullptr;
@@ -586,6 +624,40 @@ extern "C" int sc_newmark_set_output(sc_newmark* h, int out_interval, int n_rec,
   return SC_OK;
 }
 
+namespace {
+// A and M as FP32 pairs and the pair copy of p, made before the first graph (pair SpMV only)
+int pair_prepare(sc_newmark* h) {
+  NmArgs& g = h->g;
+  if (!h->pair) {
+    g.p2 = nullptr;
+    return SC_OK;
+  }
+  if (!h->AP) {
+    cudaStream_t st = h->user;
+    int64_t nnz = 0;
+    int rc = check(cudaMemcpyAsync(&nnz, g.rowptr + g.n, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "nnz");
+    if (!rc) rc = check(cudaStreamSynchronize(st), "sync");
+    if (!rc) rc = check(cudaMallocAsync((void**)&h->AP, 8 * (nnz > 0 ? nnz : 1), st), "malloc");
+    if (!rc) rc = check(cudaMallocAsync((void**)&h->MP, 8 * (nnz > 0 ? nnz : 1), st), "malloc");
+    if (!rc) rc = check(cudaMallocAsync((void**)&h->p2, 8 * g.n, st), "malloc");
+    if (rc) return rc;
+    k_to_pairs<<<grid_for(nnz, 256, 152 * 32), 256, 0, st>>>(nnz, g.A, h->AP);
+    k_to_pairs<<<grid_for(nnz, 256, 152 * 32), 256, 0, st>>>(nnz, g.M, h->MP);
+    if ((rc = check_launch("pair planes"))) return rc;
+  }
+  g.p2 = h->p2;
+  return SC_OK;
+}
+}  // namespace
+
+// options bit 0: the SpMV in FP64 instead of FP32-pair arithmetic
+extern "C" int sc_newmark_set_options(sc_newmark* h, int options) {
+  if (!h || options < 0 || options > 1) return SC_BAD_ARG;
+  h->pair = (options & 1) ? 0 : 1;
+  drop_graphs(h);
+  return SC_OK;
+}
+
 // Polynomial order (1..kHistMax; 0: adaptive, the default) of the extrapolated accelerations
 // that start each step's PCG: it changes the iteration count, not the converged answer.
 extern "C" int sc_newmark_set_predictor(sc_newmark* h, int order) {
@@ -603,6 +675,7 @@ extern "C" int sc_newmark_initial_acceleration(sc_newmark* h) {
   cudaStream_t st = h->user;
   NmArgs& g = h->g;
   int rc;
+  if ((rc = pair_prepare(h))) return rc;
   // f = force(0); the dinv of M for this solve
   if ((rc = check(cudaMemsetAsync(g.f, 0, sizeof(double) * g.n, st), "memset f"))) return rc;
   k_set_t<<<1, 1, 0, st>>>(g.s, -1);
@@ -639,6 +712,7 @@ extern "C" int sc_newmark_initial_acceleration(sc_newmark* h) {
 extern "C" int sc_newmark_run(sc_newmark* h, int t_begin, int t_end) {
   if (!h || t_begin < 0 || t_end < t_begin) return SC_BAD_ARG;
   int rc;
+  if ((rc = pair_prepare(h))) return rc;
   if (!h->step_exec) {
     if ((rc = build_pcg_graph(h, h->g.A, 0, &h->step_graph, &h->step_exec))) return rc;
   }
@@ -671,9 +745,18 @@ extern "C" int sc_newmark_time_spmv(sc_newmark* h, int reps, float* ms_per_launc
     return rc;
   }
   cudaGraphConditionalHandle none = 0;
-  k_spmv<false><<<h->row_blocks, kRowThreads, 0, st>>>(h->g, h->g.A, none);  // warm
+  if ((rc = pair_prepare(h))) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+  }
+  auto launch = [&]() {
+    if (h->g.p2) k_spmv<false, true><<<h->row_blocks, kRowThreads, 0, st>>>(h->g, h->g.A, h->AP, none);
+    else k_spmv<false, false><<<h->row_blocks, kRowThreads, 0, st>>>(h->g, h->g.A, nullptr, none);
+  };
+  launch();  // warm
   cudaEventRecord(e0, st);
-  for (int i = 0; i < reps; ++i) k_spmv<false><<<h->row_blocks, kRowThreads, 0, st>>>(h->g, h->g.A, none);
+  for (int i = 0; i < reps; ++i) launch();
   cudaEventRecord(e1, st);
   rc = check_launch("k_spmv timing");
   if (!rc) rc = check(cudaEventSynchronize(e1), "event sync");
@@ -683,7 +766,7 @@ extern "C" int sc_newmark_time_spmv(sc_newmark* h, int reps, float* ms_per_launc
   if (bytes_per_launch) {
     int64_t nnz = 0;
     cudaMemcpy(&nnz, h->g.rowptr + h->g.n, sizeof(int64_t), cudaMemcpyDeviceToHost);
-    // values + column indices + row pointers + p (one pass) + w (write)
+    // values (8 bytes: FP64 or an FP32 pair) + column indices + row pointers + p (one pass) + w
     *bytes_per_launch = nnz * 12 + (h->g.n + 1) * 8 + h->g.n * 16;
   }
   cudaEventDestroy(e0);
@@ -699,6 +782,10 @@ extern "C" int sc_newmark_destroy(sc_newmark* h) {
   if (h->init_graph) cudaGraphDestroy(h->init_graph);
   if (h->cap) cudaStreamDestroy(h->cap);
   if (h->cap2) cudaStreamDestroy(h->cap2);
+  cudaStreamSynchronize(h->user);
+  if (h->AP) cudaFree(h->AP);
+  if (h->MP) cudaFree(h->MP);
+  if (h->p2) cudaFree(h->p2);
   delete h;
   return SC_OK;
 }

@@ -133,7 +133,7 @@ def _device_matrices(M, C, K):
 class NewmarkGPU:
     """Device state + step loop on a shared CSR pattern (thin owner of the C-ABI handle)."""
 
-    def __init__(self, pattern, M, C, K, dt, rtol=1e-12, max_iter=1000):
+    def __init__(self, pattern, M, C, K, dt, rtol=1e-12, max_iter=1000, spmv="pair"):
         self.pattern = pattern
         n = pattern.n
         self.n = n
@@ -149,6 +149,8 @@ class NewmarkGPU:
                  M.data_ptr(), C.data_ptr(), K.data_ptr(), self.A.data_ptr(), float(dt), float(rtol), int(max_iter),
                  self.u.data_ptr(), self.v.data_ptr(), self.a.data_ptr(), self.ws.data_ptr(), wsn, dv.stream_ptr())
         self.h = h
+        # bit 0: the PCG SpMV in FP64 instead of FP32 pairs
+        nat.call("sc_newmark_set_options", self.h, {"pair": 0, "fp64": 1}[spmv])
         self._keep = []
 
     def set_force(self, table: ForceTable, stream=False):
@@ -425,7 +427,7 @@ class NewmarkExplicit:
     def __init__(self, rtol=1e-12, max_iter=1000, layout="node-block", spmv="pair", residual="pair"):
         self.output_interval = 1
         self.layout = layout  # "node-block" (matrices from GenerateMatrix) or "csr"
-        self.spmv = spmv  # node-block PCG operator arithmetic: "pair" (FP32 pairs) or "fp64"
+        self.spmv = spmv  # PCG SpMV arithmetic (both layouts): "pair" (FP32 pairs) or "fp64"
         self.residual = residual  # node-block step residual: "pair" (hands over to FP64 by itself) or "fp64"
         self.update_rhs_at_time_step_func = None
         self.rtol = rtol
@@ -489,7 +491,7 @@ class NewmarkExplicit:
             else ["csr"]
         for kind in attempts:
             if kind == "csr":
-                solver = NewmarkGPU(pat, Md, Cd, Kd, dt, self.rtol, self.max_iter)
+                solver = NewmarkGPU(pat, Md, Cd, Kd, dt, self.rtol, self.max_iter, spmv=self.spmv)
             else:
                 solver = NodeBlockNewmark(g, dt, self.rtol, self.max_iter, precond=kind, spmv=self.spmv,
                                           residual=self.residual)

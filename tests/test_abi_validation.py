@@ -87,3 +87,7 @@ def test_node_block_option_and_residual_checks(lib):
     assert lib.sc_nb_set_options(None, 0) == SC_BAD_ARG
     flag = ctypes.c_int()
     assert lib.sc_nb_residual_fp64(None, ctypes.byref(flag)) == SC_BAD_ARG
+
+
+def test_csr_option_checks(lib):
+    assert lib.sc_newmark_set_options(None, 0) == SC_BAD_ARG

@@ -181,7 +181,7 @@ def test_assembly_is_deterministic(torch_cuda):
         assert torch_cuda.equal(a, b)
 
 
-def _gpu_history(name, rtol=1e-12, receivers=None, layout="node-block"):
+def _gpu_history(name, rtol=1e-12, receivers=None, layout="node-block", spmv="pair"):
     from oracle import loads
     from scatter_gb300.solvers import ForceTable, NewmarkExplicit
 
@@ -189,7 +189,7 @@ def _gpu_history(name, rtol=1e-12, receivers=None, layout="node-block"):
     load = dict(spec["load"])
     time = loads.time_grid(load["time"], spec["dt"])
     F = loads.table(load, time, model)
-    solver = NewmarkExplicit(rtol=rtol, layout=layout)
+    solver = NewmarkExplicit(rtol=rtol, layout=layout, spmv=spmv)
     solver.output_interval = 1
     solver.initialise(ns.number_eq, time)
     solver.force_table = ForceTable.from_dense(F)
@@ -213,11 +213,13 @@ def test_newmark_vs_benchmark_set_2(torch_cuda, name, layout):
     assert rel_l2(solver.v[:, e], h["vel_y"]) <= 1e-10
 
 
-@pytest.mark.parametrize("layout", LAYOUTS)
-def test_newmark_vs_oracle_full_history(torch_cuda, layout):
+@pytest.mark.parametrize("layout,spmv", [("node-block", "pair"), ("csr", "pair"), ("csr", "fp64")])
+def test_newmark_vs_oracle_full_history(torch_cuda, layout, spmv):
+    """Both layouts against the oracle's direct solve; the CSR loop in its default pair SpMV
+    and in FP64."""
     from oracle import newmark
 
-    solver, model, spec, time, F = _gpu_history("column_hexa8_abs", layout=layout)
+    solver, model, spec, time, F = _gpu_history("column_hexa8_abs", layout=layout, spmv=spmv)
     _, _, Mo, Co, Ko, _, _ = oracle_system("column_hexa8_abs")
     U, V, A, _ = newmark.solve(Mo, Co, Ko, F, time, 1)
     assert rel_l2(solver.u, U) <= 1e-10
