@@ -84,23 +84,23 @@ __device__ __forceinline__ void warm_start_coeffs(int p, double* cf) {
 }
 
 // The controller's state lives in each solver's scalar block S, which has the int fields
-// hist, pord, pdir, win_n, win_it, probing, hold, it and the double ref_avg.
+// hist, head, pord, pdir, win_n, win_it, probing, hold, it and the double ref_avg.
 template <class S>
 __device__ __forceinline__ int warm_start_order(const S* s, int fixed) {
   const int ord = fixed > 0 ? fixed : s->pord;
   return s->hist < ord ? s->hist : ord;
 }
 
-// history entries kept after a step: the fixed order's, or one beyond the adaptive order
-// (it moves by at most one per window)
-template <class S>
-__device__ __forceinline__ int warm_start_depth(const S* s, int fixed) {
-  return fixed > 0 ? fixed : min(kHistMax, s->pord + 1);
-}
+// The history is a ring of kHistMax vectors: a_{n-1-k} sits in slot (head + k) mod kHistMax,
+// and a step writes its outgoing acceleration into slot head - 1 and moves head there (one
+// write per step instead of shifting the whole history).
+static_assert((kHistMax & (kHistMax - 1)) == 0, "the history ring's index wraps with a mask");
+__device__ __forceinline__ int hist_slot(int head, int k) { return (head + k) & (kHistMax - 1); }
 
 template <class S>
 __device__ inline void warm_start_init(S* s) {
   s->hist = 0;
+  s->head = 0;
   s->pord = kPredStart;
   s->pdir = 1;
   s->win_n = s->win_it = s->probing = s->hold = 0;
@@ -112,6 +112,7 @@ __device__ inline void warm_start_init(S* s) {
 template <class S>
 __device__ inline void warm_start_advance(S* s, int fixed) {
   if (s->hist < kHistMax) s->hist += 1;
+  s->head = hist_slot(s->head, kHistMax - 1);  // the slot k_finalize just wrote
   if (fixed > 0) return;
   if (++s->win_n < kPredWin) {
     s->win_it += s->it;

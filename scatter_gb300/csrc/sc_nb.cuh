@@ -21,6 +21,7 @@ struct Scal {
   int it, max_it, max_seen, status, t, fsai_fallback;
   unsigned int ticket;
   int hist;  // valid previous accelerations (0..kHistMax) for the warm start
+  int head;  // ring slot of the most recent one (hist_slot)
   int done;  // eager mode: set when the PCG loop should stop
   // adaptive warm-start order: current order, probing direction, window and hold counters
   int pord, pdir, win_n, win_it, probing, hold;
@@ -67,7 +68,7 @@ struct Args {
   double aM, aK, aC;       // A = aM M + aK K + aC Cabs
   double dt;
   double *u, *v, *a;
-  double* ah[kHistMax];  // previous accelerations a_{n-1} .. a_{n-kHistMax} (ah[0] most recent)
+  double* ah[kHistMax];  // previous accelerations, a ring: a_{n-1-k} in ah[hist_slot(head, k)]
   int pred_order;        // order of the warm start's extrapolation (1..kHistMax), 0: adaptive (Scal::pord)
   double *q1, *q2, *y1, *x0, *x, *r, *z, *p, *w, *f;
   float* t32;

@@ -58,6 +58,9 @@ __global__ void k_predict(Args g) {
   const int p = warm_start_order(g.s, g.pred_order);
   double cf[kHistMax + 1];
   warm_start_coeffs(p, cf);
+  const double* hs[kHistMax];  // a_{n-1-k}
+#pragma unroll
+  for (int k = 0; k < kHistMax; ++k) hs[k] = g.ah[hist_slot(g.s->head, k)];
   // while the pair residual runs, q1, q2 and the pair copy of x0 are read by no one
   const bool fp64_res = !g.res_pair || g.s->res_fp64;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
@@ -73,7 +76,7 @@ __global__ void k_predict(Args g) {
     double x0 = cf[0] * ai;
 #pragma unroll
     for (int k = 1; k <= kHistMax; ++k)
-      if (k <= p) x0 += cf[k] * g.ah[k - 1][i];
+      if (k <= p) x0 += cf[k] * hs[k - 1][i];
     if (g.fixed[i]) x0 = 0.0;
     g.x0[i] = x0;
     if (g.spmv_pair && fp64_res) g.p2[i] = split_pair(x0);  // p2 is scratch until p is first written
@@ -617,18 +620,17 @@ __global__ void k_direction(Args g) {
   }
 }
 
-// u = up + dt^2/4 x ; v = vp + dt/2 x ; shift the acceleration history ; record ; t += 1
+// u = up + dt^2/4 x ; v = vp + dt/2 x ; a into the history ring (k_advance moves its head)
 __global__ void k_finalize(Args g) {
   const double dt = g.dt, h = 0.5 * dt, qq = 0.25 * dt * dt;
-  const int depth = warm_start_depth(g.s, g.pred_order);
+  double* __restrict__ slot = g.ah[hist_slot(g.s->head, kHistMax - 1)];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
     const double x = g.x[i], ai = g.a[i], vi = g.v[i];
     const double up = g.u[i] + dt * vi + qq * ai;
     const double vp = vi + h * ai;
     g.u[i] = fma(qq, x, up);
     g.v[i] = fma(h, x, vp);
-    for (int k = depth - 1; k > 0; --k) g.ah[k][i] = g.ah[k - 1][i];
-    g.ah[0][i] = ai;
+    slot[i] = ai;
     g.a[i] = x;
   }
 }

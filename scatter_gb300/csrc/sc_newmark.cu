@@ -44,6 +44,7 @@ struct NmScalars {
   long long total_iters;
   int it, max_it, max_seen, status, t;
   int hist;  // valid previous accelerations (0..kHistMax) for the warm start
+  int head;  // ring slot of the most recent one (hist_slot)
   unsigned int ticket;
   // adaptive warm-start order: current order, probing direction, window and hold counters
   int pord, pdir, win_n, win_it, probing, hold;
@@ -56,7 +57,7 @@ struct NmArgs {
   const double *M, *C, *K, *A;
   double *u, *v, *a;
   double *vp, *up, *x, *r, *z, *p, *w, *dinv, *f;
-  double* ah[kHistMax];  // previous accelerations a_{n-1} .. a_{n-kHistMax} (ah[0] most recent)
+  double* ah[kHistMax];  // previous accelerations, a ring: a_{n-1-k} in ah[hist_slot(head, k)]
   int pred_order;        // warm-start order (1..kHistMax), 0: adaptive (NmScalars::pord)
   double* part;          // [nblocks][4]
   NmScalars* s;
@@ -109,6 +110,9 @@ __global__ void k_predict(NmArgs g) {
   const int p = warm_start_order(g.s, g.pred_order);
   double cf[kHistMax + 1];
   warm_start_coeffs(p, cf);
+  const double* hs[kHistMax];  // a_{n-1-k}
+#pragma unroll
+  for (int k = 0; k < kHistMax; ++k) hs[k] = g.ah[hist_slot(g.s->head, k)];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
     const double ai = g.a[i], vi = g.v[i];
     g.vp[i] = vi + h * ai;
@@ -116,7 +120,7 @@ __global__ void k_predict(NmArgs g) {
     double x0 = cf[0] * ai;  // terms summed in a fixed order
 #pragma unroll
     for (int k = 1; k <= kHistMax; ++k)
-      if (k <= p) x0 += cf[k] * g.ah[k - 1][i];
+      if (k <= p) x0 += cf[k] * hs[k - 1][i];
     g.w[i] = x0;
   }
 }
@@ -316,16 +320,15 @@ __device__ inline void record(const NmArgs& g, int step) {
   }
 }
 
-// u = up + dt^2/4 x ; v = vp + dt/2 x ; shift the acceleration history ; a = x
+// u = up + dt^2/4 x ; v = vp + dt/2 x ; a into the history ring (k_advance moves its head) ; a = x
 __global__ void k_finalize(NmArgs g) {
   const double h = 0.5 * g.dt, q = 0.25 * g.dt * g.dt;
-  const int depth = warm_start_depth(g.s, g.pred_order);
+  double* __restrict__ slot = g.ah[hist_slot(g.s->head, kHistMax - 1)];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
     const double x = g.x[i];
     g.u[i] = fma(q, x, g.up[i]);
     g.v[i] = fma(h, x, g.vp[i]);
-    for (int k = depth - 1; k > 0; --k) g.ah[k][i] = g.ah[k - 1][i];
-    g.ah[0][i] = g.a[i];
+    slot[i] = g.a[i];
     g.a[i] = x;
   }
 }
