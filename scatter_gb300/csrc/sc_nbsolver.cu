@@ -52,6 +52,8 @@ __global__ void k_force(Args g) {
 //     = f - K (up + beta vp) - M (alpha vp) - Cabs vp
 //   x0 = warm start;  A x0 = aM M x0 + aK K x0 + aC Cabs x0
 // stored: q1 = up + beta vp, q2 = alpha vp, y1 = vp, x0.
+// One thread per node: the pair residual's record of the node leaves in whole 16-byte stores.
+template <int D>
 __global__ void k_predict(Args g) {
   const double dt = g.dt, h = 0.5 * dt, qq = 0.25 * dt * dt;
   // warm-start order p = min(history, order) and its coefficients, once per thread
@@ -63,36 +65,46 @@ __global__ void k_predict(Args g) {
   for (int k = 0; k < kHistMax; ++k) hs[k] = g.ah[hist_slot(g.s->head, k)];
   // while the pair residual runs, q1, q2 and the pair copy of x0 are read by no one
   const bool fp64_res = !g.res_pair || g.s->res_fp64;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
-    const double ai = g.a[i], vi = g.v[i];
-    const double vp = vi + h * ai;
-    const double up = g.u[i] + dt * vi + qq * ai;
-    if (fp64_res) {
-      g.q1[i] = up + g.beta_r * vp;
-      g.q2[i] = g.alpha_r * vp;
-    }
-    g.y1[i] = vp;
-    // x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k}, terms summed in a fixed order
-    double x0 = cf[0] * ai;
+  constexpr int R = kRecFloats(D);
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < g.n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
+    float rec[R];
 #pragma unroll
-    for (int k = 1; k <= kHistMax; ++k)
-      if (k <= p) x0 += cf[k] * hs[k - 1][i];
-    if (g.fixed[i]) x0 = 0.0;
-    g.x0[i] = x0;
-    if (g.spmv_pair && fp64_res) g.p2[i] = split_pair(x0);  // p2 is scratch until p is first written
-    if (g.res_pair) {
+    for (int k = 6 * D; k < R; ++k) rec[k] = 0.f;
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const int64_t i = n * D + c;
+      const double ai = g.a[i], vi = g.v[i];
+      const double vp = vi + h * ai;
+      const double up = g.u[i] + dt * vi + qq * ai;
       const double q1 = up + g.beta_r * vp, q2 = g.alpha_r * vp;
-      const int D = g.D;
-      const int64_t node = i / D, c = i - node * D;
-      float* rec = g.rrec + node * kRecFloats(D);
-      const float2 zk = split_pair(fma(g.aK, x0, q1)), zm = split_pair(fma(g.aM, x0, q2));
-      rec[2 * c] = zk.x;
-      rec[2 * c + 1] = zk.y;
-      rec[2 * D + 2 * c] = zm.x;
-      rec[2 * D + 2 * c + 1] = zm.y;
-      rec[4 * D + c] = (float)q1;
-      rec[5 * D + c] = (float)q2;
-      g.zc[i] = fma(g.aC, x0, vp);
+      if (fp64_res) {
+        g.q1[i] = q1;
+        g.q2[i] = q2;
+      }
+      g.y1[i] = vp;
+      // x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k}, terms summed in a fixed order
+      double x0 = cf[0] * ai;
+#pragma unroll
+      for (int k = 1; k <= kHistMax; ++k)
+        if (k <= p) x0 += cf[k] * hs[k - 1][i];
+      if (g.fixed[i]) x0 = 0.0;
+      g.x0[i] = x0;
+      if (g.spmv_pair && fp64_res) g.p2[i] = split_pair(x0);  // p2 is scratch until p is first written
+      if (g.res_pair) {
+        const float2 zk = split_pair(fma(g.aK, x0, q1)), zm = split_pair(fma(g.aM, x0, q2));
+        rec[2 * c] = zk.x;
+        rec[2 * c + 1] = zk.y;
+        rec[2 * D + 2 * c] = zm.x;
+        rec[2 * D + 2 * c + 1] = zm.y;
+        rec[4 * D + c] = (float)q1;
+        rec[5 * D + c] = (float)q2;
+        g.zc[i] = fma(g.aC, x0, vp);
+      }
+    }
+    if (g.res_pair) {
+      float4* rp = reinterpret_cast<float4*>(g.rrec + n * R);
+#pragma unroll
+      for (int k = 0; k < R / 4; ++k) rp[k] = make_float4(rec[4 * k], rec[4 * k + 1], rec[4 * k + 2], rec[4 * k + 3]);
     }
   }
 }
@@ -317,31 +329,58 @@ __global__ void __launch_bounds__(kThreads) k_residual_kp(Args g) {
   }
 }
 
+// s[c] += sum over the row's chunks of the factor planes (c, d) times the gathered FP32 vector's
+// d component.  Two chunks at a time, so that two chunks' column, gather and plane loads are in
+// flight together (the chunk count is the slice's, uniform across the warp); the products are
+// summed in the same order as one chunk at a time.  The kernels that use it are held to 64
+// registers (four blocks of 256 per SM): the latency of the column -> gather chain bounds them,
+// and at their natural 72 registers (three blocks) they were slower than one chunk at a time.
+template <int D>
+__device__ __forceinline__ void fsai_chunk(const __half* planes, int64_t plane_n, const float* vec, int64_t pos,
+                                           const int (&cl)[4], int keep, float (&s)[D]) {
+  float va[4][D];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) ldvec<D>(vec, cl[e], va[e]);
+#pragma unroll
+  for (int c = 0; c < D; ++c)
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      float gv[4];
+      ld4(planes + (int64_t)(c * D + d) * plane_n + pos, gv, keep);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) s[c] = fmaf(gv[e], va[e][d], s[c]);
+    }
+}
+
+template <int D>
+__device__ __forceinline__ void fsai_row(const __half* planes, int64_t plane_n, const int* col, const float* vec,
+                                         int64_t p0, int64_t nq, int keep, float (&s)[D]) {
+  int64_t q = 0;
+  for (; q + 1 < nq; q += 2) {
+    const int64_t pos = p0 + 128 * q;
+    int c0[4], c1[4];
+    cols4(col, pos, c0, keep);
+    cols4(col, pos + 128, c1, keep);
+    fsai_chunk<D>(planes, plane_n, vec, pos, c0, keep, s);
+    fsai_chunk<D>(planes, plane_n, vec, pos + 128, c1, keep, s);
+  }
+  if (q < nq) {
+    const int64_t pos = p0 + 128 * q;
+    int c0[4];
+    cols4(col, pos, c0, keep);
+    fsai_chunk<D>(planes, plane_n, vec, pos, c0, keep, s);
+  }
+}
+
 // t = G r  (lower pattern, FP16 factor planes, FP32 products and result)
 template <int D>
-__global__ void __launch_bounds__(kThreads) k_prec_lower(Args g) {
+__global__ void __launch_bounds__(kThreads, 4) k_prec_lower(Args g) {
   SELL_ROW_LOOP(g.sl_ptr) {
     SELL_ROW_BEGIN(g.sl_ptr)
     float s[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) s[c] = 0.f;
-    for (int64_t q = 0; q < nq; ++q) {
-      const int64_t pos = p0 + 128 * q;
-      int cl[4];
-      cols4(g.sl_col, pos, cl, g.keep_l2);
-      float ra[4][D];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) ldvec<D>(g.r32, cl[e], ra[e]);
-#pragma unroll
-      for (int c = 0; c < D; ++c)
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-          float gv[4];
-          ld4(g.GS + (int64_t)(c * D + d) * g.sl_n + pos, gv, g.keep_l2);
-#pragma unroll
-          for (int e = 0; e < 4; ++e) s[c] = fmaf(gv[e], ra[e][d], s[c]);
-        }
-    }
+    fsai_row<D>(g.GS, g.sl_n, g.sl_col, g.r32, p0, nq, g.keep_l2, s);
     if (row < g.n_nodes) {
 #pragma unroll
       for (int c = 0; c < D; ++c) g.t32[row * D + c] = s[c];
@@ -352,7 +391,7 @@ __global__ void __launch_bounds__(kThreads) k_prec_lower(Args g) {
 // z = G^T t ; partial r.z ; mode 0 (inside PCG): last block computes beta, rz;
 // mode 1 (after the residual): p = z, rz, rr and the conditional from |r| vs |b|.
 template <int D, int kMode>
-__global__ void __launch_bounds__(kThreads) k_prec_upper(Args g, int mode, cudaGraphConditionalHandle hc) {
+__global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
   double prz = 0.0, prr = 0.0;
   SELL_ROW_LOOP(g.su_ptr) {
@@ -360,23 +399,7 @@ __global__ void __launch_bounds__(kThreads) k_prec_upper(Args g, int mode, cudaG
     float s[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) s[c] = 0.f;
-    for (int64_t q = 0; q < nq; ++q) {
-      const int64_t pos = p0 + 128 * q;
-      int cl[4];
-      cols4(g.su_col, pos, cl, g.keep_l2);
-      float ta[4][D];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) ldvec<D>(g.t32, cl[e], ta[e]);
-#pragma unroll
-      for (int c = 0; c < D; ++c)
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-          float gv[4];
-          ld4(g.GTS + (int64_t)(c * D + d) * g.su_n + pos, gv, g.keep_l2);
-#pragma unroll
-          for (int e = 0; e < 4; ++e) s[c] = fmaf(gv[e], ta[e][d], s[c]);
-        }
-    }
+    fsai_row<D>(g.GTS, g.su_n, g.su_col, g.t32, p0, nq, g.keep_l2, s);
     if (row < g.n_nodes) {
 #pragma unroll
       for (int c = 0; c < D; ++c) {
@@ -420,29 +443,13 @@ __global__ void __launch_bounds__(kThreads) k_prec_upper(Args g, int mode, cudaG
 
 // z = G^T t only (no reductions, no graph conditional): used by sc_nb_apply
 template <int D>
-__global__ void __launch_bounds__(kThreads) k_prec_upper_nograph(Args g) {
+__global__ void __launch_bounds__(kThreads, 4) k_prec_upper_nograph(Args g) {
   SELL_ROW_LOOP(g.su_ptr) {
     SELL_ROW_BEGIN(g.su_ptr)
     float s[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) s[c] = 0.f;
-    for (int64_t q = 0; q < nq; ++q) {
-      const int64_t pos = p0 + 128 * q;
-      int cl[4];
-      cols4(g.su_col, pos, cl, g.keep_l2);
-      float ta[4][D];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) ldvec<D>(g.t32, cl[e], ta[e]);
-#pragma unroll
-      for (int c = 0; c < D; ++c)
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-          float gv[4];
-          ld4(g.GTS + (int64_t)(c * D + d) * g.su_n + pos, gv, g.keep_l2);
-#pragma unroll
-          for (int e = 0; e < 4; ++e) s[c] = fmaf(gv[e], ta[e][d], s[c]);
-        }
-    }
+    fsai_row<D>(g.GTS, g.su_n, g.su_col, g.t32, p0, nq, g.keep_l2, s);
     if (row < g.n_nodes) {
 #pragma unroll
       for (int c = 0; c < D; ++c) g.z[row * D + c] = (double)s[c];
@@ -987,7 +994,7 @@ int build_graph(sc_nb_newmark* h) {
                     "capture")))
       break;
     k_force<<<1, 256, 0, cs>>>(g);
-    k_predict<<<vbk, 256, 0, cs>>>(g);
+    k_predict<D><<<vbk, 256, 0, cs>>>(g);
     if (g.res_pair) {
       k_residual_kp<D><<<nbk, kThreads, 0, cs>>>(g);
       k_residual<D, true><<<nbk, kThreads, 0, cs>>>(g, 1);
@@ -1349,7 +1356,7 @@ static int eager_step(sc_nb_newmark* h) {
   const unsigned nbk = h->node_blocks, vbk = h->vec_blocks;
   cudaGraphConditionalHandle none = 0;
   k_force<<<1, 256, 0, st>>>(g);
-  k_predict<<<vbk, 256, 0, st>>>(g);
+  k_predict<D><<<vbk, 256, 0, st>>>(g);
   if (g.res_pair) {
     k_residual_kp<D><<<nbk, kThreads, 0, st>>>(g);
     k_residual<D, true><<<nbk, kThreads, 0, st>>>(g, 1);
