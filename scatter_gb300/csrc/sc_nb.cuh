@@ -57,8 +57,9 @@ struct Args {
   // the pair residual (k_residual_kp): r = f - K (q1 + aK x0) - M (q2 + aM x0) - Cabs (y1 + aC x0)
   const float2* MSP;       // the consistent-mass plane as FP32 pairs
   float* rrec;             // per node, what the pair residual gathers (k_predict writes it): kRecFloats
-                           // floats, at [0, 2D) q1 + aK x0 as (hi, lo) pairs, [2D, 4D) q2 + aM x0 as
-                           // pairs, [4D, 5D) q1 and [5D, 6D) q2 in FP32 (for |b| and the cancellation check)
+                           // floats; the mass part at kRecM: [0, 2D) q2 + aM x0 as (hi, lo) pairs,
+                           // [2D, 3D) q2 in FP32; the stiffness part at kRecK(D): [0, 2D) q1 + aK x0
+                           // as pairs, [2D, 3D) q1 in FP32 (q1, q2 for |b| and the cancellation check)
   double* zc;              // y1 + aC x0 (dashpot rows)
   int res_pair;            // 1: k_predict writes the vectors above and the step runs k_residual_kp
   int spmv_pair;           // 1: PCG SpMV in FP32-pair arithmetic, 0: FP64
@@ -87,8 +88,34 @@ struct Args {
   int64_t n_out;
 };
 
-// floats per node of the pair residual's record (whole 16-byte pieces)
+// floats per node of the pair residual's record (whole 16-byte pieces), and where its mass and
+// stiffness parts start
 __host__ __device__ constexpr int kRecFloats(int D) { return D == 3 ? 20 : 12; }
+constexpr int kRecM = 0;
+__host__ __device__ constexpr int kRecK(int D) { return 3 * D; }
+
+// v = rec[I, E) with the widest aligned loads (a record starts on 16 bytes)
+template <int I, int E>
+__device__ __forceinline__ void ldrec_(const float* rec, float* v) {
+  if constexpr (I < E) {
+    if constexpr (I % 4 == 0 && I + 4 <= E) {
+      const float4 t = *reinterpret_cast<const float4*>(rec + I);
+      v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+      ldrec_<I + 4, E>(rec, v + 4);
+    } else if constexpr (I % 2 == 0 && I + 2 <= E) {
+      const float2 t = *reinterpret_cast<const float2*>(rec + I);
+      v[0] = t.x; v[1] = t.y;
+      ldrec_<I + 2, E>(rec, v + 2);
+    } else {
+      v[0] = rec[I];
+      ldrec_<I + 1, E>(rec, v + 1);
+    }
+  }
+}
+template <int A, int N>
+__device__ __forceinline__ void ldrec(const float* rec, float (&v)[N]) {
+  ldrec_<A, A + N>(rec, v);
+}
 
 // node n's D values of an FP32 slot vector
 template <int D>

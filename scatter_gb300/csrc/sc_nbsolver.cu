@@ -92,12 +92,12 @@ __global__ void k_predict(Args g) {
       if (g.spmv_pair && fp64_res) g.p2[i] = split_pair(x0);  // p2 is scratch until p is first written
       if (g.res_pair) {
         const float2 zk = split_pair(fma(g.aK, x0, q1)), zm = split_pair(fma(g.aM, x0, q2));
-        rec[2 * c] = zk.x;
-        rec[2 * c + 1] = zk.y;
-        rec[2 * D + 2 * c] = zm.x;
-        rec[2 * D + 2 * c + 1] = zm.y;
-        rec[4 * D + c] = (float)q1;
-        rec[5 * D + c] = (float)q2;
+        rec[kRecM + 2 * c] = zm.x;
+        rec[kRecM + 2 * c + 1] = zm.y;
+        rec[kRecM + 2 * D + c] = (float)q2;
+        rec[kRecK(D) + 2 * c] = zk.x;
+        rec[kRecK(D) + 2 * c + 1] = zk.y;
+        rec[kRecK(D) + 2 * D + c] = (float)q1;
         g.zc[i] = fma(g.aC, x0, vp);
       }
     }
@@ -252,40 +252,35 @@ __global__ void __launch_bounds__(kThreads) k_residual_kp(Args g) {
 #pragma unroll
       for (int hh = 0; hh < 2; ++hh) {  // two entries at a time (registers)
         const int64_t pos = p0 + 128 * q + 2 * hh;
-        float2 zk[2][D], zm[2][D];
-        float q1[2][D], q2[2][D];
+        const float* rp[2] = {g.rrec + (int64_t)cl[2 * hh] * kRecFloats(D),
+                              g.rrec + (int64_t)cl[2 * hh + 1] * kRecFloats(D)};
+        // the mass part first: M is diagonal in the components, so the two entries' M records
+        // are used up before their K records are loaded (half the registers live at a time)
+        {
+          float mv[2][3 * D];
+          ldrec<kRecM, 3 * D>(rp[0], mv[0]);
+          ldrec<kRecM, 3 * D>(rp[1], mv[1]);
+          float2 m2[2];
+          ld2(g.MSP + pos, m2, g.keep_l2);
 #pragma unroll
-        for (int e = 0; e < 2; ++e) {
-          constexpr int NV = kRecFloats(D) / 4;
-          const float4* rp = reinterpret_cast<const float4*>(g.rrec + (int64_t)cl[2 * hh + e] * kRecFloats(D));
-          float rv[4 * NV];
-#pragma unroll
-          for (int k = 0; k < NV; ++k) {
-            const float4 a = rp[k];
-            rv[4 * k] = a.x; rv[4 * k + 1] = a.y; rv[4 * k + 2] = a.z; rv[4 * k + 3] = a.w;
-          }
-#pragma unroll
-          for (int d = 0; d < D; ++d) {
-            zk[e][d] = make_float2(rv[2 * d], rv[2 * d + 1]);
-            zm[e][d] = make_float2(rv[2 * D + 2 * d], rv[2 * D + 2 * d + 1]);
-            q1[e][d] = rv[4 * D + d];
-            q2[e][d] = rv[5 * D + d];
+          for (int c = 0; c < D; ++c) {
+            pair_fma(m2[0].x, m2[0].y, make_float2(mv[0][2 * c], mv[0][2 * c + 1]), rh[c], rl[c]);
+            pair_fma(m2[1].x, m2[1].y, make_float2(mv[1][2 * c], mv[1][2 * c + 1]), rh[c], rl[c]);
+            bq[c] = fmaf(m2[1].x, mv[1][2 * D + c], fmaf(m2[0].x, mv[0][2 * D + c], bq[c]));
           }
         }
-        float2 m2[2];
-        ld2(g.MSP + pos, m2, g.keep_l2);
+        float kv[2][3 * D];
+        ldrec<kRecK(D), 3 * D>(rp[0], kv[0]);
+        ldrec<kRecK(D), 3 * D>(rp[1], kv[1]);
 #pragma unroll
         for (int c = 0; c < D; ++c) {
-          pair_fma(m2[0].x, m2[0].y, zm[0][c], rh[c], rl[c]);
-          pair_fma(m2[1].x, m2[1].y, zm[1][c], rh[c], rl[c]);
-          bq[c] = fmaf(m2[1].x, q2[1][c], fmaf(m2[0].x, q2[0][c], bq[c]));
 #pragma unroll
           for (int d = 0; d < D; ++d) {
             float2 k2[2];
             ld2(g.KPS + (int64_t)(c * D + d) * g.sf_n + pos, k2, g.keep_l2);
-            pair_fma(k2[0].x, k2[0].y, zk[0][d], rh[c], rl[c]);
-            pair_fma(k2[1].x, k2[1].y, zk[1][d], rh[c], rl[c]);
-            bq[c] = fmaf(k2[1].x, q1[1][d], fmaf(k2[0].x, q1[0][d], bq[c]));
+            pair_fma(k2[0].x, k2[0].y, make_float2(kv[0][2 * d], kv[0][2 * d + 1]), rh[c], rl[c]);
+            pair_fma(k2[1].x, k2[1].y, make_float2(kv[1][2 * d], kv[1][2 * d + 1]), rh[c], rl[c]);
+            bq[c] = fmaf(k2[1].x, kv[1][2 * D + d], fmaf(k2[0].x, kv[0][2 * D + d], bq[c]));
           }
         }
       }
