@@ -255,8 +255,19 @@ int sc_nb_set_predictor(sc_nb_newmark* h, int order);
  * pass over K and mass pair planes as f - K (q1 + aK x0) - M (q2 + aM x0) - Cabs (y1 + aC x0),
  * with A = aM M + aK K + aC Cabs (~48 bits per term, no FP64 product); a step that finds the
  * elastic and inertial terms cancelling the load by more than 30x (slow motion) switches every
- * later step to the FP64 residual, see sc_nb_residual_fp64.  Options outside 0..7 are rejected. */
+ * later step to the FP64 residual, see sc_nb_residual_fp64.
+ * The FP32 matrix: with the pair SpMV, a step whose initial residual is small runs its PCG on
+ * Ah = the pairs' hi parts alone (4 B per value instead of 8).  With Al = A - Ah and
+ * L = sqrt(||Al||_1 ||Al||_inf) >= ||Al||_2 (computed at creation), the true residual of x
+ * differs from the PCG's recursive one by -Al (x - x0), so the loop stops at
+ * |r| + L |x - x0| <= rtol |b|: the answer meets the same tolerance.  A step uses Ah when the
+ * previous step's |x - x0| / |r0|, applied to this step's r0, keeps L |x - x0| below
+ * rtol |b| / 16; if the bound passes rtol |b| / 2 during the solve, the PCG restarts from x0
+ * with the pairs.  bit 3: never use Ah.  bit 4: use Ah at every step (exercises the restart).
+ * Bits 3 and 4 together, and options outside 0..31, are rejected. */
 int sc_nb_set_options(sc_nb_newmark* h, int options);
+/* steps whose PCG ran on the FP32 matrix, restarts in pairs, and L (synchronises) */
+int sc_nb_a32_status(sc_nb_newmark* h, int64_t* a32_steps, int64_t* restarts, double* lo_norm);
 /* Whether the step's residual runs in FP64 (always with option bit 2 or the FP64 SpMV, else
  * once the pair residual has handed over); synchronises the stream (no reference
  * counterpart). */
@@ -269,6 +280,8 @@ int sc_nb_run(sc_nb_newmark* h, int t_begin, int t_end);
 int sc_nb_status(sc_nb_newmark* h, int64_t* total_iters, int* max_iters_per_step, int* fsai_fallback_rows);
 /* timing aid: the step loop's block SpMV (w = A p) launched `reps` times between CUDA events */
 int sc_nb_time_spmv(sc_nb_newmark* h, int reps, float* ms_per_launch, int64_t* bytes_per_launch);
+/* the same with a32 = 1: the SpMV form that applies the FP32 matrix (A's hi planes) alone */
+int sc_nb_time_spmv_a32(sc_nb_newmark* h, int a32, int reps, float* ms_per_launch, int64_t* bytes_per_launch);
 /* Explicit central-difference steps on the same handle (no reference counterpart: the
  * reference's mass is always consistent):
  *   a_n = M_L^-1 (f_n - K (u_n + beta v_{n-1/2}) - alpha M_L v_{n-1/2} - Cabs v_{n-1/2}),

@@ -65,6 +65,7 @@ SIGNATURES = {
     "sc_nb_create": (I, [ctypes.POINTER(P), I, I, P, P, P, L, P, P, P, P, P, L, P, P, P, D, D, D, D, I, I, P, P, P, P,
                          L, P]),
     "sc_nb_set_options": (I, [P, I]),
+    "sc_nb_a32_status": (I, [P, ctypes.POINTER(L), ctypes.POINTER(L), ctypes.POINTER(ctypes.c_double)]),
     "sc_nb_residual_fp64": (I, [P, ctypes.POINTER(I)]),
     "sc_nb_set_predictor": (I, [P, I]),
     "sc_nb_set_force": (I, [P, I, P, P, P]),
@@ -72,6 +73,7 @@ SIGNATURES = {
     "sc_nb_run": (I, [P, I, I]),
     "sc_nb_status": (I, [P, ctypes.POINTER(L), ctypes.POINTER(I), ctypes.POINTER(I)]),
     "sc_nb_time_spmv": (I, [P, I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(L)]),
+    "sc_nb_time_spmv_a32": (I, [P, I, I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(L)]),
     "sc_nb_explicit_run": (I, [P, I, I]),
     "sc_nb_set_lumped_mass": (I, [P, P]),
     "sc_nb_time_explicit": (I, [P, I, ctypes.POINTER(ctypes.c_float)]),

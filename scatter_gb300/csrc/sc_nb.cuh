@@ -28,6 +28,15 @@ struct Scal {
   double ref_avg;  // mean iterations per step of the reference window
   int res_fp64;       // 1: the residual runs in FP64 (for good, once the pair residual saw strong cancellation)
   int res_fp64_next;  // set by the pair residual; k_advance copies it into res_fp64 at the end of the step
+  // the FP32 matrix (A's hi parts) in the PCG: with Ah = hi, A = Ah + Al, the solve runs on Ah
+  // and the true residual b - A x differs from the recursive one by -Al (x - x0), at most
+  // lo_norm |x - x0| (lo_norm >= ||Al||_2)
+  int a32;            // 1: this step's PCG SpMV applies Ah alone
+  int restart;        // 1: the bound failed; the next preconditioner pass restarts from x0, r0 in pairs
+  double lo_norm;     // sqrt(||Al||_1 ||Al||_inf)
+  double rr0, dd;     // |r0|^2 of the step, |x - x0|^2 after the last update
+  double rho;         // |x - x0| / |r0| of the last step that moved (-1: none yet)
+  long long a32_steps, restarts;
 };
 
 struct Args {
@@ -52,6 +61,7 @@ struct Args {
   const double *KS, *AS, *MSS;
   const __half *GS, *GTS;  // FSAI factor planes, FP16, scaled by a power of two (max |entry| in [0.5, 1))
   const float2* APS;       // A as FP32 (hi, lo) pairs (hi + lo = A to 48 bits) for the pair-arithmetic SpMV
+  const float* AHS;        // the pairs' hi parts alone: the FP32 matrix of the a32 SpMV
   const float2* KPS;       // K as FP32 pairs, for the explicit step and the adjoint (built on first use)
   float2* p2;              // p as (hi, lo) FP32 pairs, written with p
   // the pair residual (k_residual_kp): r = f - K (q1 + aK x0) - M (q2 + aM x0) - Cabs (y1 + aC x0)
@@ -74,6 +84,9 @@ struct Args {
   double *q1, *q2, *y1, *x0, *x, *r, *z, *p, *w, *f;
   float* t32;
   float* r32;  // FP32 copy of r, written with r: the lower FSAI half gathers it (no FP64 conversion per gather)
+  double* r0;   // the step's initial residual, and its FP32 copy: a restart of the PCG starts from them
+  float* r032;
+  int a32_mode;  // FP32 matrix in the PCG: 0 never, 1 when the bound allows (default), 2 every step
   double* part;
   Scal* s;
   // force (slot indices)
@@ -204,6 +217,10 @@ __device__ __forceinline__ void ld2(const double* p, double (&v)[2], int keep) {
   const double2 a = keep ? __ldg(q) : __ldcs(q);
   v[0] = a.x; v[1] = a.y;
 }
+__device__ __forceinline__ void ld2f(const float* p, float2& v, int keep) {
+  const float2* q = reinterpret_cast<const float2*>(p);
+  v = keep ? __ldg(q) : __ldcs(q);
+}
 __device__ __forceinline__ void ld2(const float2* p, float2 (&v)[2], int keep) {
   const float4* q = reinterpret_cast<const float4*>(p);
   const float4 a = keep ? __ldg(q) : __ldcs(q);
@@ -242,6 +259,11 @@ __device__ __forceinline__ double group_sum(double x) {
 
 
 static __global__ void k_set_t(Scal* s, int t) { s->t = t; }
+
+static __global__ void k_hi_parts(int64_t n, const float2* __restrict__ hl, float* __restrict__ hi) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    hi[i] = hl[i].x;
+}
 
 static __global__ void k_split_pairs(int64_t n, const double* __restrict__ x, float2* __restrict__ hl) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {

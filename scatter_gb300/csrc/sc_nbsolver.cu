@@ -207,6 +207,8 @@ __global__ void __launch_bounds__(kThreads) k_residual(Args g, int gate) {
         }
         g.r[i] = rv;
         g.r32[i] = (float)rv;
+        g.r0[i] = rv;
+        g.r032[i] = (float)rv;
         g.x[i] = g.x0[i];
         pbb += bv * bv;
       }
@@ -303,6 +305,8 @@ __global__ void __launch_bounds__(kThreads) k_residual_kp(Args g) {
         }
         g.r[i] = rv;
         g.r32[i] = (float)rv;
+        g.r0[i] = rv;
+        g.r032[i] = (float)rv;
         g.x[i] = g.x0[i];
         pbb += bv * bv;
       }
@@ -370,12 +374,13 @@ __device__ __forceinline__ void fsai_row(const __half* planes, int64_t plane_n, 
 // t = G r  (lower pattern, FP16 factor planes, FP32 products and result)
 template <int D>
 __global__ void __launch_bounds__(kThreads, 4) k_prec_lower(Args g) {
+  const float* rv = g.s->restart ? g.r032 : g.r32;  // a restart preconditions r0
   SELL_ROW_LOOP(g.sl_ptr) {
     SELL_ROW_BEGIN(g.sl_ptr)
     float s[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) s[c] = 0.f;
-    fsai_row<D>(g.GS, g.sl_n, g.sl_col, g.r32, p0, nq, g.keep_l2, s);
+    fsai_row<D>(g.GS, g.sl_n, g.sl_col, rv, p0, nq, g.keep_l2, s);
     if (row < g.n_nodes) {
 #pragma unroll
       for (int c = 0; c < D; ++c) g.t32[row * D + c] = s[c];
@@ -383,12 +388,16 @@ __global__ void __launch_bounds__(kThreads, 4) k_prec_lower(Args g) {
   }
 }
 
+constexpr double kA32Margin = 16.0;
+
 // z = G^T t ; partial r.z ; mode 0 (inside PCG): last block computes beta, rz;
 // mode 1 (after the residual): p = z, rz, rr and the conditional from |r| vs |b|.
 template <int D, int kMode>
 __global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
   double prz = 0.0, prr = 0.0;
+  // a restart (inside the PCG): x, r back to x0, r0 and a fresh direction (beta = 0)
+  const bool rs = mode == 0 && g.s->restart;
   SELL_ROW_LOOP(g.su_ptr) {
     SELL_ROW_BEGIN(g.su_ptr)
     float s[D];
@@ -400,7 +409,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cu
       for (int c = 0; c < D; ++c) {
         const int64_t i = row * D + c;
         const double z = (double)s[c];
-        const double r = g.r[i];
+        const double r = rs ? g.r0[i] : g.r[i];
+        if (rs) {
+          g.r[i] = r;
+          g.x[i] = g.x0[i];
+        }
         g.z[i] = z;
         if (mode == 1) {
           g.p[i] = z;
@@ -426,11 +439,23 @@ __global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cu
       if (mode == 1) {
         s->rz = rz;
         s->rr = rr;
+        s->rr0 = rr;
+        s->dd = 0.0;
+        s->restart = 0;
         const bool done = rr <= s->tol2 * s->bb;
+        // the FP32 matrix when the last step's |x - x0| / |r0|, scaled to this r0, keeps the
+        // bound lo_norm |x - x0| below tol |b| / kA32Margin
+        int a = 0;
+        if (g.a32_mode == 2) a = 1;
+        else if (g.a32_mode == 1 && s->rho >= 0.0)
+          a = s->lo_norm * s->rho * sqrt(rr) * kA32Margin <= sqrt(s->tol2 * s->bb) ? 1 : 0;
+        s->a32 = a;
+        if (a && !done) s->a32_steps += 1;
         pcg_continue<kMode>(hc, s, !done);
       } else {
-        s->beta = s->rz != 0.0 ? rz / s->rz : 0.0;
+        s->beta = rs ? 0.0 : (s->rz != 0.0 ? rz / s->rz : 0.0);
         s->rz = rz;
+        if (rs) s->restart = 0;
       }
     }
   }
@@ -521,8 +546,40 @@ __global__ void __launch_bounds__(kThreads) k_spmv(Args g, cudaGraphConditionalH
 // the row sums are carried as an unevaluated (hi, lo) FP32 pair with TwoSum (Knuth) and
 // converted to FP64 once per row.  Relative accuracy ~2^-46 per product, no FP64 pipe work
 // in the block loop; same bytes as the FP64 kernel (A: 2 x 4 B per value, p: 8 B pairs).
-template <int D, int kMode>
-__global__ void __launch_bounds__(kThreads) k_spmv_pair(Args g, cudaGraphConditionalHandle hc) {
+// With a32 it reads the hi parts alone (a copy, 4 B per value): w = Ah p, the FP32 matrix Ah
+// applied to p in the same pair arithmetic (to ~2^-46 for Ah itself).
+template <int D>
+__device__ __forceinline__ void spmv_chunk(const Args& g, int64_t pos, const int (&cl)[4], bool a32, float (&hi)[D],
+                                           float (&lo)[D]) {
+  float2 pv[4][D];
+#pragma unroll
+  for (int e = 0; e < 4; ++e)
+#pragma unroll
+    for (int d = 0; d < D; ++d) pv[e][d] = g.p2[(int64_t)cl[e] * D + d];
+#pragma unroll
+  for (int c = 0; c < D; ++c)
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const int64_t off = (int64_t)(c * D + d) * g.sf_n + pos;
+      if (a32) {
+        float ah[4];
+        ld4(g.AHS + off, ah, g.keep_l2);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) pair_fma(ah[e], 0.f, pv[e][d], hi[c], lo[c]);
+      } else {
+        float2 a4[4];
+        ld4(g.APS + off, a4, g.keep_l2);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) pair_fma(a4[e].x, a4[e].y, pv[e][d], hi[c], lo[c]);
+      }
+    }
+}
+
+// the SpMV's rows: pair planes one chunk at a time (kA32 = false), or the hi planes alone two
+// chunks at a time (half the bytes per chunk, so twice the loads in flight); then p.w and alpha
+constexpr bool kA32TwoChunks = true;
+template <int D, int kMode, bool kA32>
+__device__ __forceinline__ void spmv_rows(const Args& g, cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
   double ppw = 0.0;
   SELL_ROW_LOOP(g.sf_ptr) {
@@ -530,24 +587,27 @@ __global__ void __launch_bounds__(kThreads) k_spmv_pair(Args g, cudaGraphConditi
     float hi[D], lo[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) hi[c] = lo[c] = 0.f;
-    for (int64_t q = 0; q < nq; ++q) {
-      const int64_t pos = p0 + 128 * q;
-      int cl[4];
-      cols4(g.sf_col, pos, cl, g.keep_l2);
-      float2 pv[4][D];
-#pragma unroll
-      for (int e = 0; e < 4; ++e)
-#pragma unroll
-        for (int d = 0; d < D; ++d) pv[e][d] = g.p2[(int64_t)cl[e] * D + d];
-#pragma unroll
-      for (int c = 0; c < D; ++c)
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-          float2 a4[4];
-          ld4(g.APS + (int64_t)(c * D + d) * g.sf_n + pos, a4, g.keep_l2);
-#pragma unroll
-          for (int e = 0; e < 4; ++e) pair_fma(a4[e].x, a4[e].y, pv[e][d], hi[c], lo[c]);
-        }
+    if (kA32 && kA32TwoChunks) {
+      int64_t q = 0;
+      for (; q + 1 < nq; q += 2) {
+        const int64_t pos = p0 + 128 * q;
+        int c0[4], c1[4];
+        cols4(g.sf_col, pos, c0, g.keep_l2);
+        cols4(g.sf_col, pos + 128, c1, g.keep_l2);
+        spmv_chunk<D>(g, pos, c0, true, hi, lo);
+        spmv_chunk<D>(g, pos + 128, c1, true, hi, lo);
+      }
+      if (q < nq) {
+        int c0[4];
+        cols4(g.sf_col, p0 + 128 * q, c0, g.keep_l2);
+        spmv_chunk<D>(g, p0 + 128 * q, c0, true, hi, lo);
+      }
+    } else {
+      for (int64_t q = 0; q < nq; ++q) {
+        int c0[4];
+        cols4(g.sf_col, p0 + 128 * q, c0, g.keep_l2);
+        spmv_chunk<D>(g, p0 + 128 * q, c0, kA32, hi, lo);
+      }
     }
     if (row < g.n_nodes) {
 #pragma unroll
@@ -580,29 +640,68 @@ __global__ void __launch_bounds__(kThreads) k_spmv_pair(Args g, cudaGraphConditi
   }
 }
 
-// x += alpha p ; r -= alpha w ; partial r.r ; last block: convergence test
+// Both forms are launched in the PCG loop; the one that does not match Scal::a32 returns at once
+// (kMode 2, the timing launch, always runs).  Separate kernels keep the pair form at 64 registers;
+// the FP32-matrix form is held to 80 (three blocks per SM: 0.140 ms at the 1.79 M-equation box
+// against 0.203 ms at its natural 105 registers and 0.210 ms one chunk at a time).
+template <int D, int kMode>
+__global__ void __launch_bounds__(kThreads) k_spmv_pair(Args g, cudaGraphConditionalHandle hc) {
+  if (kMode != 2 && g.s->a32) return;
+  spmv_rows<D, kMode, false>(g, hc);
+}
+
+template <int D, int kMode>
+__global__ void __launch_bounds__(kThreads, 3) k_spmv_a32(Args g, cudaGraphConditionalHandle hc) {
+  if (kMode != 2 && !g.s->a32) return;
+  spmv_rows<D, kMode, true>(g, hc);
+}
+
+// x += alpha p ; r -= alpha w ; partial r.r and |x - x0|^2 ; last block: convergence test.
+// With the FP32 matrix Ah (Scal::a32) the true residual is within lo_norm |x - x0| of the
+// recursive one, so the test is |r| + lo_norm |x - x0| <= tol |b|; once that bound alone passes
+// half the tolerance the solve restarts from x0 in pairs (Scal::restart).
 template <int kMode>
 __global__ void k_update(Args g, cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
   const double alpha = g.s->alpha;
-  double prr = 0.0;
+  double prr = 0.0, pdd = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
-    g.x[i] = fma(alpha, g.p[i], g.x[i]);
+    const double x = fma(alpha, g.p[i], g.x[i]);
+    g.x[i] = x;
+    const double dx = x - g.x0[i];
+    pdd += dx * dx;
     const double r = fma(-alpha, g.w[i], g.r[i]);
     g.r[i] = r;
     g.r32[i] = (float)r;
     prr += r * r;
   }
-  const double t = block_sum(prr, sh);
+  double t = block_sum(prr, sh);
   if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 1] = t;
+  t = block_sum(pdd, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 2] = t;
   if (last_block(&g.s->ticket)) {
     const double rr = reduce_parts(g.part, 1, sh);
+    const double dd = reduce_parts(g.part, 2, sh);
     if (threadIdx.x == 0) {
       Scal* s = g.s;
       s->ticket = 0;
       s->rr = rr;
+      s->dd = dd;
       s->it += 1;
-      bool done = rr <= s->tol2 * s->bb;
+      bool done;
+      if (s->a32) {
+        const double tb = sqrt(s->tol2 * s->bb), e = s->lo_norm * sqrt(dd);
+        if (e > 0.5 * tb) {
+          s->a32 = 0;
+          s->restart = 1;
+          s->restarts += 1;
+          done = false;
+        } else {
+          done = sqrt(rr) + e <= tb;
+        }
+      } else {
+        done = rr <= s->tol2 * s->bb;
+      }
       if (!done && s->it >= s->max_it) {
         if (!s->status) s->status = SC_NOT_CONVERGED;
         done = true;
@@ -663,6 +762,8 @@ __global__ void k_advance(Args g) {
     if (s->it > s->max_seen) s->max_seen = s->it;
     s->t += 1;
     if (s->res_fp64_next) s->res_fp64 = 1;  // the next step's predictor and residual see it
+    if (s->rr0 > 0.0 && s->dd > 0.0) s->rho = sqrt(s->dd / s->rr0);
+    s->a32 = 0;
     warm_start_advance(s, g.pred_order);
   }
 }
@@ -952,6 +1053,11 @@ __global__ void k_init_scal(Scal* s, double tol2, int max_it) {
   s->fsai_fallback = 0;
   s->ticket = 0;
   s->res_fp64 = s->res_fp64_next = 0;
+  s->a32 = s->restart = 0;
+  s->lo_norm = 0.0;
+  s->rr0 = s->dd = 0.0;
+  s->rho = -1.0;
+  s->a32_steps = s->restarts = 0;
   warm_start_init(s);
 }
 
@@ -1019,7 +1125,10 @@ int build_graph(sc_nb_newmark* h) {
     if ((rc = check(cudaStreamBeginCaptureToGraph(c2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
                     "capture body")))
       break;
-    if (g.spmv_pair) k_spmv_pair<D, 0><<<nbk, kThreads, 0, c2>>>(g, hc);
+    if (g.spmv_pair) {
+      k_spmv_pair<D, 0><<<nbk, kThreads, 0, c2>>>(g, hc);
+      k_spmv_a32<D, 0><<<nbk, kThreads, 0, c2>>>(g, hc);
+    }
     else k_spmv<D, 0><<<nbk, kThreads, 0, c2>>>(g, hc);
     k_update<0><<<vbk, 256, 0, c2>>>(g, hc);
     k_prec_lower<D><<<nbk, kThreads, 0, c2>>>(g);
@@ -1060,6 +1169,76 @@ void drop_graph(sc_nb_newmark* h) {
 
 // Sliced-ELL copies of K, A, M (full pattern), G (lower) and G^T (upper) for the per-step
 // kernels; allocated here (setup) from the stream-ordered pool and freed by sc_nb_destroy.
+// lo_norm = sqrt(||Al||_1 ||Al||_inf) >= ||Al||_2 for Al = A - Ah, the lo parts of the pair
+// planes: each row's sum of |lo| (largest kept by an atomic max on the bits of a non-negative
+// double, which order like the values) and each column's (atomic adds into colsum)
+template <int D>
+__global__ void k_lo_sums(Args g, double* colsum, unsigned long long* rowmax) {
+  SELL_ROW_LOOP(g.sf_ptr) {
+    SELL_ROW_BEGIN(g.sf_ptr)
+    double rs[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) rs[c] = 0.0;
+    for (int64_t q = 0; q < nq; ++q) {
+      const int64_t pos = p0 + 128 * q;
+      int cl[4];
+      cols4(g.sf_col, pos, cl, 1);
+#pragma unroll
+      for (int c = 0; c < D; ++c)
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const double lo = fabs((double)g.APS[(int64_t)(c * D + d) * g.sf_n + pos + e].y);
+            if (lo > 0.0) {
+              rs[c] += lo;
+              atomicAdd(colsum + (int64_t)cl[e] * D + d, lo);
+            }
+          }
+    }
+    if (row < g.n_nodes) {
+      double m = 0.0;
+#pragma unroll
+      for (int c = 0; c < D; ++c) m = fmax(m, rs[c]);
+      atomicMax(rowmax, (unsigned long long)__double_as_longlong(m));
+    }
+  }
+}
+
+__global__ void k_col_max(int64_t n, const double* colsum, unsigned long long* colmax) {
+  double m = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmax(m, colsum[i]);
+  atomicMax(colmax, (unsigned long long)__double_as_longlong(m));
+}
+
+__global__ void k_lo_norm(const unsigned long long* mx, Scal* s) {
+  s->lo_norm = sqrt(__longlong_as_double((long long)mx[0]) * __longlong_as_double((long long)mx[1]));
+}
+
+static int lo_norm(sc_nb_newmark* h) {
+  Args& g = h->g;
+  cudaStream_t st = h->user;
+  double* colsum = nullptr;
+  unsigned long long* mx = nullptr;
+  int rc = check(cudaMallocAsync((void**)&colsum, 8 * g.n_s, st), "malloc");
+  if (rc) return rc;
+  if ((rc = check(cudaMallocAsync((void**)&mx, 16, st), "malloc"))) {
+    cudaFreeAsync(colsum, st);
+    return rc;
+  }
+  cudaMemsetAsync(colsum, 0, 8 * g.n_s, st);
+  cudaMemsetAsync(mx, 0, 16, st);
+  if (g.D == 3) k_lo_sums<3><<<h->node_blocks, kThreads, 0, st>>>(g, colsum, mx);
+  else k_lo_sums<2><<<h->node_blocks, kThreads, 0, st>>>(g, colsum, mx);
+  k_col_max<<<grid_for(g.n_s, 256, 152 * 8), 256, 0, st>>>(g.n_s, colsum, mx + 1);
+  k_lo_norm<<<1, 1, 0, st>>>(mx, g.s);
+  rc = check_launch("lo norm");
+  cudaFreeAsync(colsum, st);
+  cudaFreeAsync(mx, st);
+  return rc;
+}
+
 static int build_sell(sc_nb_newmark* h, const double* KB, const double* AB, const double* MS, const float* GB,
                       const float* GTB, float gscale) {
   Args& g = h->g;
@@ -1099,10 +1278,14 @@ static int build_sell(sc_nb_newmark* h, const double* KB, const double* AB, cons
       k_sell_permute<double><<<pb, 256, 0, st>>>(D2, total, g.nnzb, src, AB, as);
       k_sell_permute<double><<<pb, 256, 0, st>>>(1, total, g.nnzb, src, MS, ms);
       float2* ap = nullptr;
+      float* ah = nullptr;
       if ((rc = alloc((void**)&ap, 8 * D2 * total))) break;
+      if ((rc = alloc((void**)&ah, 4 * D2 * total))) break;
       k_split_pairs<<<pb, 256, 0, st>>>((int64_t)D2 * total, as, ap);
+      k_hi_parts<<<pb, 256, 0, st>>>((int64_t)D2 * total, ap, ah);
       g.sf_ptr = ptr; g.sf_col = col; g.sf_n = total; g.KS = ks; g.AS = as; g.MSS = ms;
       g.APS = ap;
+      g.AHS = ah;
     } else {
       __half* gs = nullptr;
       if ((rc = alloc((void**)&gs, 2 * D2 * total))) break;
@@ -1139,8 +1322,8 @@ extern "C" int64_t sc_nb_workspace_bytes(int n_nodes, int dim, int64_t nnzb) {
   b += 2 * align256(8 * D2 * nnzb);           // KB, AB
   b += align256(8 * nnzb);                    // MS
   b += 2 * align256(4 * D2 * nnzb);           // GB, GTB
-  b += (kHistMax + 11) * align256(8 * ns);    // history ah[kHistMax], q1 q2 y1 x0 x r z p w f, p2
-  b += 2 * align256(4 * ns);                  // t32, r32
+  b += (kHistMax + 12) * align256(8 * ns);    // history ah[kHistMax], q1 q2 y1 x0 x r z p w f, p2, r0
+  b += 3 * align256(4 * ns);                  // t32, r32, r032
   b += align256(8 * 4 * 152 * 16);            // partials
   b += align256(sizeof(Scal));
   return b;
@@ -1218,6 +1401,9 @@ extern "C" int sc_nb_create(sc_nb_newmark** out, int n_nodes, int dim, const int
   g.spmv_pair = 1;
   g.t32 = (float*)take(4 * ns);
   g.r32 = (float*)take(4 * ns);
+  g.r0 = (double*)take(8 * ns);
+  g.r032 = (float*)take(4 * ns);
+  g.a32_mode = 1;
   g.part = (double*)take(8 * 4 * 152 * 16);
   g.s = (Scal*)take(sizeof(Scal));
   h->node_blocks = node_grid(n_nodes);
@@ -1264,6 +1450,7 @@ extern "C" int sc_nb_create(sc_nb_newmark** out, int n_nodes, int dim, const int
     // the power of two that brings the largest FSAI entry into [0.5, 1)
     const float gscale = gmax > 0.f ? ldexpf(1.f, -(ilogbf(gmax) + 1)) : 1.f;
     if ((rc = build_sell(h, KB, AB, MS, GB, GTB, gscale))) break;
+    if ((rc = lo_norm(h))) break;
     int hf[2] = {0, 0};
     if ((rc = check(cudaMemcpyAsync(hf, dflag, 2 * sizeof(int), cudaMemcpyDeviceToHost, st), "memcpy"))) break;
     if ((rc = check(cudaStreamSynchronize(st), "sync"))) break;
@@ -1300,10 +1487,11 @@ extern "C" int sc_nb_set_predictor(sc_nb_newmark* h, int order) {
 }
 
 extern "C" int sc_nb_set_options(sc_nb_newmark* h, int options) {
-  if (!h || options < 0 || options > 7) return SC_BAD_ARG;
+  if (!h || options < 0 || options > 31 || (options & 24) == 24) return SC_BAD_ARG;
   h->g.spmv_pair = (options & 1) ? 0 : 1;
   h->explicit_pair = (options & 2) ? 0 : 1;
   h->res_pair = (options & 4) ? 0 : 1;
+  h->g.a32_mode = !h->g.spmv_pair || (options & 8) ? 0 : ((options & 16) ? 2 : 1);
   drop_graph(h);
   drop_explicit_graphs(h);
   return SC_OK;
@@ -1369,7 +1557,10 @@ static int eager_step(sc_nb_newmark* h) {
       return rc;
     if ((rc = check(cudaStreamSynchronize(st), "sync eager"))) return rc;
     if (done) break;
-    if (g.spmv_pair) k_spmv_pair<D, 1><<<nbk, kThreads, 0, st>>>(g, none);
+    if (g.spmv_pair) {
+      k_spmv_pair<D, 1><<<nbk, kThreads, 0, st>>>(g, none);
+      k_spmv_a32<D, 1><<<nbk, kThreads, 0, st>>>(g, none);
+    }
     else k_spmv<D, 1><<<nbk, kThreads, 0, st>>>(g, none);
     k_update<1><<<vbk, 256, 0, st>>>(g, none);
     k_prec_lower<D><<<nbk, kThreads, 0, st>>>(g);
@@ -1459,8 +1650,26 @@ extern "C" int sc_nb_status(sc_nb_newmark* h, int64_t* total_iters, int* max_ite
   return s.status;
 }
 
+extern "C" int sc_nb_a32_status(sc_nb_newmark* h, int64_t* a32_steps, int64_t* restarts, double* lo_norm) {
+  if (!h) return SC_BAD_ARG;
+  Scal s;
+  int rc = check(cudaStreamSynchronize(h->user), "sync");
+  if (rc) return rc;
+  if ((rc = check(cudaMemcpy(&s, h->g.s, sizeof(s), cudaMemcpyDeviceToHost), "read"))) return rc;
+  if (a32_steps) *a32_steps = s.a32_steps;
+  if (restarts) *restarts = s.restarts;
+  if (lo_norm) *lo_norm = s.lo_norm;
+  return SC_OK;
+}
+
 extern "C" int sc_nb_time_spmv(sc_nb_newmark* h, int reps, float* ms_per_launch, int64_t* bytes_per_launch) {
-  if (!h || reps <= 0 || !ms_per_launch) return SC_BAD_ARG;
+  return sc_nb_time_spmv_a32(h, 0, reps, ms_per_launch, bytes_per_launch);
+}
+
+extern "C" int sc_nb_time_spmv_a32(sc_nb_newmark* h, int a32, int reps, float* ms_per_launch,
+                                   int64_t* bytes_per_launch) {
+  if (!h || reps <= 0 || !ms_per_launch || (a32 != 0 && a32 != 1)) return SC_BAD_ARG;
+  if (a32 && !h->g.spmv_pair) return SC_BAD_ARG;
   cudaStream_t st = h->user;
   cudaEvent_t e0, e1;
   int rc = check(cudaEventCreate(&e0), "event");
@@ -1473,8 +1682,13 @@ extern "C" int sc_nb_time_spmv(sc_nb_newmark* h, int reps, float* ms_per_launch,
   const unsigned nbk = h->node_blocks;
   auto launch = [&]() {
     if (h->g.spmv_pair) {
-      if (h->g.D == 3) k_spmv_pair<3, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
-      else k_spmv_pair<2, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
+      if (a32) {
+        if (h->g.D == 3) k_spmv_a32<3, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
+        else k_spmv_a32<2, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
+      } else {
+        if (h->g.D == 3) k_spmv_pair<3, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
+        else k_spmv_pair<2, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
+      }
     } else {
       if (h->g.D == 3) k_spmv<3, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
       else k_spmv<2, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
@@ -1491,8 +1705,9 @@ extern "C" int sc_nb_time_spmv(sc_nb_newmark* h, int reps, float* ms_per_launch,
   *ms_per_launch = ms / reps;
   if (bytes_per_launch) {
     const int64_t D2 = (int64_t)h->g.D * h->g.D;
-    // A blocks + block columns + row pointers + one read of p + the write of w
-    *bytes_per_launch = h->g.nnzb * (8 * D2 + 4) + (int64_t)(h->g.n_slices + 1) * 8 + h->g.n_s * 16;
+    // A blocks (4 B per value for the FP32 matrix) + block columns + row pointers + one read of p
+    // + the write of w
+    *bytes_per_launch = h->g.nnzb * ((a32 ? 4 : 8) * D2 + 4) + (int64_t)(h->g.n_slices + 1) * 8 + h->g.n_s * 16;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -222,7 +222,7 @@ class NodeBlockNewmark:
     entries, receivers and outputs from/to the reference's equation numbering."""
 
     def __init__(self, g, dt, rtol=1e-12, max_iter=1000, precond="fsai", spmv="pair", explicit="pair",
-                 residual="pair"):
+                 residual="pair", fp32_matrix="auto"):
         if g.adj_ptr is None:
             raise ValueError("GenerateMatrix has no node structure")
         self.g = g
@@ -273,9 +273,19 @@ class NodeBlockNewmark:
         self.dt = dt
         # bit 0: PCG SpMV in FP64 instead of FP32 pairs; bit 1: explicit K w in FP64; bit 2: the
         # step's residual always in FP64 (by default it runs in pairs and hands over to FP64 by
-        # itself when the load is nearly balanced by the elastic and inertial forces)
+        # itself when the load is nearly balanced by the elastic and inertial forces); bits 3, 4:
+        # the PCG on the FP32 matrix (A's hi parts) never / at every step, instead of when the
+        # bound on its error allows (the answer meets rtol either way)
         nat.call("sc_nb_set_options", self.h, {"pair": 0, "fp64": 1}[spmv] | {"pair": 0, "fp64": 2}[explicit] |
-                 {"pair": 0, "fp64": 4}[residual])
+                 {"pair": 0, "fp64": 4}[residual] | {"auto": 0, "never": 8, "always": 16}[fp32_matrix])
+
+    def fp32_matrix_status(self):
+        """(steps whose PCG ran on the FP32 matrix, restarts in pairs, the bound L on ||A - Ah||_2)."""
+        a = ctypes.c_int64()
+        r = ctypes.c_int64()
+        lo = ctypes.c_double()
+        nat.call("sc_nb_a32_status", self.h, ctypes.byref(a), ctypes.byref(r), ctypes.byref(lo))
+        return a.value, r.value, lo.value
 
     def residual_fp64(self):
         """True when the step's residual runs in FP64 (synchronises)."""
@@ -353,10 +363,12 @@ class NodeBlockNewmark:
         self.fsai_fallback_rows = fb.value
         return rc, tot.value, mx.value
 
-    def time_spmv(self, reps=20):
+    def time_spmv(self, reps=20, a32=False):
+        """ms per launch and algorithmic bytes per launch of the PCG SpMV; a32: the form that
+        applies the FP32 matrix (A's hi planes) alone."""
         ms = ctypes.c_float()
         by = ctypes.c_int64()
-        nat.call("sc_nb_time_spmv", self.h, int(reps), ctypes.byref(ms), ctypes.byref(by))
+        nat.call("sc_nb_time_spmv_a32", self.h, int(bool(a32)), int(reps), ctypes.byref(ms), ctypes.byref(by))
         return ms.value, by.value
 
     def apply(self, which, x_eq):
@@ -424,11 +436,14 @@ class NewmarkExplicit:
     device (pinned memory) instead of the whole history at set-up.  ``close()`` frees the
     device solver."""
 
-    def __init__(self, rtol=1e-12, max_iter=1000, layout="node-block", spmv="pair", residual="pair"):
+    def __init__(self, rtol=1e-12, max_iter=1000, layout="node-block", spmv="pair", residual="pair",
+                 fp32_matrix="auto"):
         self.output_interval = 1
         self.layout = layout  # "node-block" (matrices from GenerateMatrix) or "csr"
         self.spmv = spmv  # PCG SpMV arithmetic (both layouts): "pair" (FP32 pairs) or "fp64"
         self.residual = residual  # node-block step residual: "pair" (hands over to FP64 by itself) or "fp64"
+        # node-block PCG on the FP32 matrix when its error bound allows ("auto"), "never" or "always"
+        self.fp32_matrix = fp32_matrix
         self.update_rhs_at_time_step_func = None
         self.rtol = rtol
         self.max_iter = max_iter
@@ -494,7 +509,7 @@ class NewmarkExplicit:
                 solver = NewmarkGPU(pat, Md, Cd, Kd, dt, self.rtol, self.max_iter, spmv=self.spmv)
             else:
                 solver = NodeBlockNewmark(g, dt, self.rtol, self.max_iter, precond=kind, spmv=self.spmv,
-                                          residual=self.residual)
+                                          residual=self.residual, fp32_matrix=self.fp32_matrix)
             solver.set_force(table, stream=self.stream_force)
             solver.set_output(self.output_interval, rec, n_out)
             if ic is not None:
@@ -523,7 +538,7 @@ class NewmarkExplicit:
         else:
             g = generator_of(M, C, K)
         key = (id(g) if g is not None else (id(M), id(C), id(K)), id(self.time), id(self.force_table),
-               self.layout, self.spmv, self.residual, self.output_interval)
+               self.layout, self.spmv, self.residual, self.fp32_matrix, self.output_interval)
         live = self._live
         if live is not None and live[0] == key and t_start_idx == live[2] and t_end_idx >= t_start_idx:
             solver = live[1]

@@ -222,3 +222,34 @@ def test_residual_arithmetic_and_handover(cuda, residual):
     U, V, _, _ = newmark.solve(M, C, K, Fd, time, 1)
     assert rel_l2(out["u"], U) <= 1e-10
     assert rel_l2(out["v"], V) <= 1e-10
+
+
+def test_fp32_matrix_meets_the_tolerance(cuda):
+    """The PCG on the FP32 matrix (A's hi parts) stops on |r| + L |x - x0| <= rtol |b|, with L
+    a bound on ||A - Ah||_2: every mode reaches the pair-only displacements to the PCG
+    tolerance.  'always' starts every step on Ah and restarts the early steps (large r0) in
+    pairs; 'auto' takes Ah only where the bound allows and needs no restart on this smooth load."""
+    from scatter_gb300.solvers import NodeBlockNewmark
+
+    g, table, rec, dt, n_t = _ricker_box()
+    out = {}
+    for mode in ("never", "auto", "always"):
+        s = NodeBlockNewmark(g, dt, fp32_matrix=mode)
+        s.set_force(table)
+        s.set_output(1, rec, n_t, what=("u",))
+        s.initial_acceleration()
+        s.run(0, n_t - 1)
+        rc, iters, _ = s.status()
+        assert rc == 0, mode
+        out[mode] = (s.outputs()["u"].copy(), iters, s.fp32_matrix_status())
+        s.close()
+    ref = out["never"][0]
+    assert np.abs(ref).max() > 0
+    a32, restarts, lo = out["never"][2]
+    assert a32 == 0 and restarts == 0 and lo > 0
+    for mode in ("auto", "always"):
+        assert rel_l2(out[mode][0], ref) <= 1e-10, mode
+    a32, restarts, _ = out["always"][2]
+    assert a32 > 0 and restarts > 0
+    a32, restarts, _ = out["auto"][2]
+    assert restarts == 0
