@@ -70,24 +70,35 @@ __global__ void k_predict(Args g) {
     float rec[R];
 #pragma unroll
     for (int k = 6 * D; k < R; ++k) rec[k] = 0.f;
+    // the node's loads first (no store between them, so they are all in flight together)
+    double av[D], vv[D], uv[D], xs[D];
+    int fx[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) {
       const int64_t i = n * D + c;
-      const double ai = g.a[i], vi = g.v[i];
+      av[c] = g.a[i];
+      vv[c] = g.v[i];
+      uv[c] = g.u[i];
+      fx[c] = g.fixed[i];
+      // x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k}, terms summed in a fixed order
+      xs[c] = cf[0] * av[c];
+#pragma unroll
+      for (int k = 1; k <= kHistMax; ++k)
+        if (k <= p) xs[c] += cf[k] * hs[k - 1][i];
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const int64_t i = n * D + c;
+      const double ai = av[c], vi = vv[c];
       const double vp = vi + h * ai;
-      const double up = g.u[i] + dt * vi + qq * ai;
+      const double up = uv[c] + dt * vi + qq * ai;
       const double q1 = up + g.beta_r * vp, q2 = g.alpha_r * vp;
       if (fp64_res) {
         g.q1[i] = q1;
         g.q2[i] = q2;
       }
       g.y1[i] = vp;
-      // x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k}, terms summed in a fixed order
-      double x0 = cf[0] * ai;
-#pragma unroll
-      for (int k = 1; k <= kHistMax; ++k)
-        if (k <= p) x0 += cf[k] * hs[k - 1][i];
-      if (g.fixed[i]) x0 = 0.0;
+      const double x0 = fx[c] ? 0.0 : xs[c];
       g.x0[i] = x0;
       if (g.spmv_pair && fp64_res) g.p2[i] = split_pair(x0);  // p2 is scratch until p is first written
       if (g.res_pair) {
