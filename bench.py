@@ -265,6 +265,8 @@ def run_gb300(args):
     residual_fp64 = solver.residual_fp64()
     solver.close()
 
+    # the same steps in IEEE FP64 throughout the PCG (what the default arithmetic saves)
+    fp64 = None if args.no_e2e else ieee_fp64_run(g, table, rec_eq, W, K_steps, n, v_gpu)
     # end to end through the drop-in call: the same steps as the timed region, from a fresh
     # solver given the same warm-up
     e2e = None if args.no_e2e else e2e_run(g, table, time_grid, rec_eq, W, K_steps, n)
@@ -296,6 +298,7 @@ def run_gb300(args):
                        "gpu_solver_setup_fsai": round(t_solver_setup, 3)},
            "fsai_fallback_rows": solver.fsai_fallback_rows,
            "fp32_matrix": {"timed_steps": a32_steps, "restarts": restarts, "lo_norm_bound": lo_norm},
+           "ieee_fp64": fp64,
            "gpu_launches": 9 * K_steps + 6 * iters,
            "roofline": {"bound": "hbm",
                         "kernel": ("nb::k_spmv_a32 (PCG w = Ah p, the FP32 matrix, 3x3 node blocks, pair products)"
@@ -667,6 +670,41 @@ def adjoint_run(n_steps=4000, checkpoint=200, n_fd=20):
             "elements": n_el, "steps": n_steps, "checkpoint": checkpoint, "fd_max_rel_err": worst, "fd_checks": len(checks),
             "timing": "forward: CUDA events around the explicit run; gradient: host wall clock around the whole "
                       "sc_nb_adjoint call (forward with checkpoints, recompute, backward, graph set-up, copies)"}
+
+
+def ieee_fp64_run(g, table, rec_eq, w, k, n, v_ref):
+    """The same steps with IEEE FP64 throughout the PCG (FP64 SpMV and FP64 residual, no FP32
+    matrix): what the default arithmetic saves, and how far its receiver velocities are from
+    the all-FP64 ones."""
+    import torch
+
+    from scatter_gb300.solvers import NodeBlockNewmark
+
+    s = NodeBlockNewmark(g, DT, spmv="fp64", residual="fp64")
+    s.set_force(table)
+    s.set_output(1, rec_eq, len(table.f_ptr) - 1, what=("v",))
+    s.initial_acceleration()
+    s.run(0, w)
+    rc, it_w, _ = s.status()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    s.run(w, w + k)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    rc, it_all, _ = s.status()
+    v = s.outputs()["v"][1:w + k + 1]
+    s.close()
+    if rc != 0:
+        raise SystemExit(f"FP64 solver status {rc}")
+    rel = float(np.linalg.norm(v - v_ref) / max(np.linalg.norm(v), 1e-300))
+    return {"value": n * k / (ms / 1e3), "unit": "DOF-steps/s", "ms_per_step": ms / k, "steps": k,
+            "cg_iters_per_step": (it_all - it_w) / k,
+            "rel_l2_default_vs_fp64": rel,
+            "note": "PCG SpMV (A as FP64) and step residual in IEEE FP64, same warm start, preconditioner and "
+                    "tolerance; receiver velocities of the default arithmetic compared with these"}
 
 
 def e2e_run(g, table, time_grid, rec_eq, w, k, n):
