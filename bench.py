@@ -229,7 +229,7 @@ def run_gb300(args):
     solver.initial_acceleration()
     solver.run(0, W)
     rc, it_w, _ = solver.status()
-    a32_w, restarts_w, _ = solver.fp32_matrix_status()
+    a32_w, switched_w, restarts_w, _ = solver.fp32_matrix_status()
     torch.cuda.synchronize()
     replicas.barrier()
     torch.cuda.synchronize()
@@ -246,8 +246,8 @@ def run_gb300(args):
     if rc != 0:
         raise SystemExit(f"solver status {rc} during the timed region")
     iters = it_all - it_w
-    a32_all, restarts_all, lo_norm = solver.fp32_matrix_status()
-    a32_steps, restarts = a32_all - a32_w, restarts_all - restarts_w
+    a32_all, switched_all, restarts_all, lo_norm = solver.fp32_matrix_status()
+    a32_steps, switched, restarts = a32_all - a32_w, switched_all - switched_w, restarts_all - restarts_w
     # every rank advances its own replica: the job's rate is all ranks' DOF-steps over the
     # longest rank's time
     ms, value = replicas.job_rate(ms, n * K_steps, device="cuda")
@@ -297,7 +297,8 @@ def run_gb300(args):
            "setup_s": {"host_mesh_and_loads": round(t_host, 2), "gpu_assembly_lysmer_rayleigh": round(t_assembly, 3),
                        "gpu_solver_setup_fsai": round(t_solver_setup, 3)},
            "fsai_fallback_rows": solver.fsai_fallback_rows,
-           "fp32_matrix": {"timed_steps": a32_steps, "restarts": restarts, "lo_norm_bound": lo_norm},
+           "fp32_matrix": {"timed_steps_started": a32_steps, "timed_steps_switched": switched,
+                           "restarts": restarts, "lo_norm_bound": lo_norm},
            "ieee_fp64": fp64,
            "gpu_launches": 9 * K_steps + 6 * iters,
            "roofline": {"bound": "hbm",

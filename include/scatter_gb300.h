@@ -262,12 +262,16 @@ int sc_nb_set_predictor(sc_nb_newmark* h, int order);
  * differs from the PCG's recursive one by -Al (x - x0), so the loop stops at
  * |r| + L |x - x0| <= rtol |b|: the answer meets the same tolerance.  A step uses Ah when the
  * previous step's |x - x0| / |r0|, applied to this step's r0, keeps L |x - x0| below
- * rtol |b| / 16; if the bound passes rtol |b| / 2 during the solve, the PCG restarts from x0
- * with the pairs.  bit 3: never use Ah.  bit 4: use Ah at every step (exercises the restart).
+ * rtol |b| / 16; a step that starts on the pairs switches to Ah (continuing the CG, x and r
+ * becoming the new x0 and r0) once |r| is that small.  If the bound passes rtol |b| / 2 during
+ * the solve, the PCG restarts from x0 with the pairs and stays there for the step.
+ * bit 3: never use Ah.  bit 4: start every step on Ah (exercises the restart).
  * Bits 3 and 4 together, and options outside 0..31, are rejected. */
 int sc_nb_set_options(sc_nb_newmark* h, int options);
-/* steps whose PCG ran on the FP32 matrix, restarts in pairs, and L (synchronises) */
-int sc_nb_a32_status(sc_nb_newmark* h, int64_t* a32_steps, int64_t* restarts, double* lo_norm);
+/* steps whose PCG started on the FP32 matrix, steps that switched to it during the solve,
+ * restarts in pairs, and L (synchronises) */
+int sc_nb_a32_status(sc_nb_newmark* h, int64_t* a32_steps, int64_t* switched, int64_t* restarts,
+                     double* lo_norm);
 /* Whether the step's residual runs in FP64 (always with option bit 2 or the FP64 SpMV, else
  * once the pair residual has handed over); synchronises the stream (no reference
  * counterpart). */

@@ -33,10 +33,13 @@ struct Scal {
   // lo_norm |x - x0| (lo_norm >= ||Al||_2)
   int a32;            // 1: this step's PCG SpMV applies Ah alone
   int restart;        // 1: the bound failed; the next preconditioner pass restarts from x0, r0 in pairs
+  int sw;             // 1: the solve switches to Ah now; the next preconditioner pass makes x, r the new x0, r0
+  int no_switch;      // 1: this step restarted in pairs and stays there
   double lo_norm;     // sqrt(||Al||_1 ||Al||_inf)
   double rr0, dd;     // |r0|^2 of the step, |x - x0|^2 after the last update
+  double dd_pre;      // |x - x0|^2 at a switch (x0 before the switch)
   double rho;         // |x - x0| / |r0| of the last step that moved (-1: none yet)
-  long long a32_steps, restarts;
+  long long a32_steps, switched, restarts;
 };
 
 struct Args {

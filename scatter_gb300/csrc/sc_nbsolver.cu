@@ -407,8 +407,10 @@ template <int D, int kMode>
 __global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
   double prz = 0.0, prr = 0.0;
-  // a restart (inside the PCG): x, r back to x0, r0 and a fresh direction (beta = 0)
+  // a restart (inside the PCG): x, r back to x0, r0 and a fresh direction (beta = 0); a switch
+  // to Ah: x, r become x0, r0 (the CG goes on)
   const bool rs = mode == 0 && g.s->restart;
+  const bool sw = mode == 0 && g.s->sw;
   SELL_ROW_LOOP(g.su_ptr) {
     SELL_ROW_BEGIN(g.su_ptr)
     float s[D];
@@ -424,6 +426,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cu
         if (rs) {
           g.r[i] = r;
           g.x[i] = g.x0[i];
+        } else if (sw) {
+          g.r0[i] = r;
+          g.r032[i] = g.r32[i];
+          g.x0[i] = g.x[i];
         }
         g.z[i] = z;
         if (mode == 1) {
@@ -451,8 +457,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cu
         s->rz = rz;
         s->rr = rr;
         s->rr0 = rr;
-        s->dd = 0.0;
-        s->restart = 0;
+        s->dd = s->dd_pre = 0.0;
+        s->restart = s->sw = s->no_switch = 0;
         const bool done = rr <= s->tol2 * s->bb;
         // the FP32 matrix when the last step's |x - x0| / |r0|, scaled to this r0, keeps the
         // bound lo_norm |x - x0| below tol |b| / kA32Margin
@@ -467,6 +473,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cu
         s->beta = rs ? 0.0 : (s->rz != 0.0 ? rz / s->rz : 0.0);
         s->rz = rz;
         if (rs) s->restart = 0;
+        if (sw) s->sw = 0;
       }
     }
   }
@@ -670,7 +677,9 @@ __global__ void __launch_bounds__(kThreads, 3) k_spmv_a32(Args g, cudaGraphCondi
 // x += alpha p ; r -= alpha w ; partial r.r and |x - x0|^2 ; last block: convergence test.
 // With the FP32 matrix Ah (Scal::a32) the true residual is within lo_norm |x - x0| of the
 // recursive one, so the test is |r| + lo_norm |x - x0| <= tol |b|; once that bound alone passes
-// half the tolerance the solve restarts from x0 in pairs (Scal::restart).
+// half the tolerance the solve restarts from x0 in pairs (Scal::restart).  A solve on the pairs
+// switches to Ah (Scal::sw) when |r| has fallen as far as a step needs r0 to start on Ah; x and
+// r then become the x0 and r0 that the bound and a restart refer to.
 template <int kMode>
 __global__ void k_update(Args g, cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
@@ -705,6 +714,7 @@ __global__ void k_update(Args g, cudaGraphConditionalHandle hc) {
         if (e > 0.5 * tb) {
           s->a32 = 0;
           s->restart = 1;
+          s->no_switch = 1;
           s->restarts += 1;
           done = false;
         } else {
@@ -712,6 +722,14 @@ __global__ void k_update(Args g, cudaGraphConditionalHandle hc) {
         }
       } else {
         done = rr <= s->tol2 * s->bb;
+        // switch to Ah once |r| is as small as a step that starts on Ah needs its r0 to be
+        if (!done && g.a32_mode == 1 && !s->no_switch && s->rho >= 0.0 &&
+            s->lo_norm * s->rho * sqrt(rr) * kA32Margin <= sqrt(s->tol2 * s->bb)) {
+          s->a32 = 1;
+          s->sw = 1;
+          s->dd_pre = dd;
+          s->switched += 1;
+        }
       }
       if (!done && s->it >= s->max_it) {
         if (!s->status) s->status = SC_NOT_CONVERGED;
@@ -773,7 +791,9 @@ __global__ void k_advance(Args g) {
     if (s->it > s->max_seen) s->max_seen = s->it;
     s->t += 1;
     if (s->res_fp64_next) s->res_fp64 = 1;  // the next step's predictor and residual see it
-    if (s->rr0 > 0.0 && s->dd > 0.0) s->rho = sqrt(s->dd / s->rr0);
+    // |x - x0| over the whole step (across a switch: the two legs' lengths added)
+    const double dx = sqrt(s->dd_pre) + sqrt(s->dd);
+    if (s->rr0 > 0.0 && dx > 0.0) s->rho = dx / sqrt(s->rr0);
     s->a32 = 0;
     warm_start_advance(s, g.pred_order);
   }
@@ -1064,11 +1084,11 @@ __global__ void k_init_scal(Scal* s, double tol2, int max_it) {
   s->fsai_fallback = 0;
   s->ticket = 0;
   s->res_fp64 = s->res_fp64_next = 0;
-  s->a32 = s->restart = 0;
+  s->a32 = s->restart = s->sw = s->no_switch = 0;
   s->lo_norm = 0.0;
-  s->rr0 = s->dd = 0.0;
+  s->rr0 = s->dd = s->dd_pre = 0.0;
   s->rho = -1.0;
-  s->a32_steps = s->restarts = 0;
+  s->a32_steps = s->switched = s->restarts = 0;
   warm_start_init(s);
 }
 
@@ -1661,13 +1681,15 @@ extern "C" int sc_nb_status(sc_nb_newmark* h, int64_t* total_iters, int* max_ite
   return s.status;
 }
 
-extern "C" int sc_nb_a32_status(sc_nb_newmark* h, int64_t* a32_steps, int64_t* restarts, double* lo_norm) {
+extern "C" int sc_nb_a32_status(sc_nb_newmark* h, int64_t* a32_steps, int64_t* switched, int64_t* restarts,
+                                double* lo_norm) {
   if (!h) return SC_BAD_ARG;
   Scal s;
   int rc = check(cudaStreamSynchronize(h->user), "sync");
   if (rc) return rc;
   if ((rc = check(cudaMemcpy(&s, h->g.s, sizeof(s), cudaMemcpyDeviceToHost), "read"))) return rc;
   if (a32_steps) *a32_steps = s.a32_steps;
+  if (switched) *switched = s.switched;
   if (restarts) *restarts = s.restarts;
   if (lo_norm) *lo_norm = s.lo_norm;
   return SC_OK;

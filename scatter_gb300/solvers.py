@@ -280,12 +280,14 @@ class NodeBlockNewmark:
                  {"pair": 0, "fp64": 4}[residual] | {"auto": 0, "never": 8, "always": 16}[fp32_matrix])
 
     def fp32_matrix_status(self):
-        """(steps whose PCG ran on the FP32 matrix, restarts in pairs, the bound L on ||A - Ah||_2)."""
+        """(steps whose PCG started on the FP32 matrix, steps that switched to it during the
+        solve, restarts in pairs, the bound L on ||A - Ah||_2)."""
         a = ctypes.c_int64()
+        w = ctypes.c_int64()
         r = ctypes.c_int64()
         lo = ctypes.c_double()
-        nat.call("sc_nb_a32_status", self.h, ctypes.byref(a), ctypes.byref(r), ctypes.byref(lo))
-        return a.value, r.value, lo.value
+        nat.call("sc_nb_a32_status", self.h, ctypes.byref(a), ctypes.byref(w), ctypes.byref(r), ctypes.byref(lo))
+        return a.value, w.value, r.value, lo.value
 
     def residual_fp64(self):
         """True when the step's residual runs in FP64 (synchronises)."""

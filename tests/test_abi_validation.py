@@ -88,7 +88,7 @@ def test_node_block_option_and_residual_checks(lib):
     flag = ctypes.c_int()
     assert lib.sc_nb_residual_fp64(None, ctypes.byref(flag)) == SC_BAD_ARG
     n = ctypes.c_int64()
-    assert lib.sc_nb_a32_status(None, ctypes.byref(n), ctypes.byref(n), None) == SC_BAD_ARG
+    assert lib.sc_nb_a32_status(None, ctypes.byref(n), ctypes.byref(n), ctypes.byref(n), None) == SC_BAD_ARG
     ms = ctypes.c_float()
     assert lib.sc_nb_time_spmv_a32(None, 1, 5, ctypes.byref(ms), None) == SC_BAD_ARG
 

@@ -228,7 +228,8 @@ def test_fp32_matrix_meets_the_tolerance(cuda):
     """The PCG on the FP32 matrix (A's hi parts) stops on |r| + L |x - x0| <= rtol |b|, with L
     a bound on ||A - Ah||_2: every mode reaches the pair-only displacements to the PCG
     tolerance.  'always' starts every step on Ah and restarts the early steps (large r0) in
-    pairs; 'auto' takes Ah only where the bound allows and needs no restart on this smooth load."""
+    pairs; 'auto' starts a step on Ah, or switches to it during the solve, only where the bound
+    allows, and needs no restart on this smooth load."""
     from scatter_gb300.solvers import NodeBlockNewmark
 
     g, table, rec, dt, n_t = _ricker_box()
@@ -245,11 +246,11 @@ def test_fp32_matrix_meets_the_tolerance(cuda):
         s.close()
     ref = out["never"][0]
     assert np.abs(ref).max() > 0
-    a32, restarts, lo = out["never"][2]
-    assert a32 == 0 and restarts == 0 and lo > 0
+    a32, switched, restarts, lo = out["never"][2]
+    assert a32 == 0 and switched == 0 and restarts == 0 and lo > 0
     for mode in ("auto", "always"):
         assert rel_l2(out[mode][0], ref) <= 1e-10, mode
-    a32, restarts, _ = out["always"][2]
+    a32, switched, restarts, _ = out["always"][2]
     assert a32 > 0 and restarts > 0
-    a32, restarts, _ = out["auto"][2]
-    assert restarts == 0
+    a32, switched, restarts, _ = out["auto"][2]
+    assert a32 + switched > 0 and restarts == 0
