@@ -230,6 +230,7 @@ def run_gb300(args):
     solver.run(0, W)
     rc, it_w, _ = solver.status()
     a32_w, switched_w, restarts_w, _ = solver.fp32_matrix_status()
+    _, capped_w = solver.warm_start_status()
     torch.cuda.synchronize()
     replicas.barrier()
     torch.cuda.synchronize()
@@ -247,6 +248,7 @@ def run_gb300(args):
         raise SystemExit(f"solver status {rc} during the timed region")
     iters = it_all - it_w
     a32_all, switched_all, restarts_all, lo_norm = solver.fp32_matrix_status()
+    order_end, capped_all = solver.warm_start_status()
     a32_steps, switched, restarts = a32_all - a32_w, switched_all - switched_w, restarts_all - restarts_w
     # every rank advances its own replica: the job's rate is all ranks' DOF-steps over the
     # longest rank's time
@@ -300,6 +302,7 @@ def run_gb300(args):
            "fp32_matrix": {"timed_steps_started": a32_steps, "timed_steps_switched": switched,
                            "restarts": restarts, "lo_norm_bound": lo_norm},
            "ieee_fp64": fp64,
+           "warm_start": {"order_at_end": order_end, "timed_steps_capped": capped_all - capped_w},
            "gpu_launches": 9 * K_steps + 6 * iters,
            "roofline": {"bound": "hbm",
                         "kernel": ("nb::k_spmv_a32 (PCG w = Ah p, the FP32 matrix, 3x3 node blocks, pair products)"

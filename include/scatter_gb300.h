@@ -266,8 +266,17 @@ int sc_nb_set_predictor(sc_nb_newmark* h, int order);
  * becoming the new x0 and r0) once |r| is that small.  If the bound passes rtol |b| / 2 during
  * the solve, the PCG restarts from x0 with the pairs and stays there for the step.
  * bit 3: never use Ah.  bit 4: start every step on Ah (exercises the restart).
- * Bits 3 and 4 together, and options outside 0..31, are rejected. */
+ * bit 5: no cap on the warm-start order from the force history.  By default each step takes
+ * the largest order, up to the controller's, whose extrapolation of the force table itself
+ * reproduces the newest row to 1e-6 of the rows' largest entry: a window of
+ * accelerations that straddles a kink in the load (the end of a ramp, a load that starts to
+ * move) extrapolates badly, and a lower order whose window lies after the kink does better.
+ * The cap changes the iteration count, not the answer.
+ * Bits 3 and 4 together, and options outside 0..63, are rejected. */
 int sc_nb_set_options(sc_nb_newmark* h, int options);
+/* the controller's current warm-start order and the steps whose order the force history
+ * capped (synchronises) */
+int sc_nb_warm_start_status(sc_nb_newmark* h, int* order, int64_t* capped_steps);
 /* steps whose PCG started on the FP32 matrix, steps that switched to it during the solve,
  * restarts in pairs, and L (synchronises) */
 int sc_nb_a32_status(sc_nb_newmark* h, int64_t* a32_steps, int64_t* switched, int64_t* restarts,

@@ -65,6 +65,7 @@ SIGNATURES = {
     "sc_nb_create": (I, [ctypes.POINTER(P), I, I, P, P, P, L, P, P, P, P, P, L, P, P, P, D, D, D, D, I, I, P, P, P, P,
                          L, P]),
     "sc_nb_set_options": (I, [P, I]),
+    "sc_nb_warm_start_status": (I, [P, ctypes.POINTER(I), ctypes.POINTER(L)]),
     "sc_nb_a32_status": (I, [P, ctypes.POINTER(L), ctypes.POINTER(L), ctypes.POINTER(L),
                              ctypes.POINTER(ctypes.c_double)]),
     "sc_nb_residual_fp64": (I, [P, ctypes.POINTER(I)]),

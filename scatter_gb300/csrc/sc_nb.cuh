@@ -40,6 +40,8 @@ struct Scal {
   double dd_pre;      // |x - x0|^2 at a switch (x0 before the switch)
   double rho;         // |x - x0| / |r0| of the last step that moved (-1: none yet)
   long long a32_steps, switched, restarts;
+  int pcap;           // this step's cap on the warm-start order from the force history (k_order_cap)
+  long long capped;   // steps whose order the cap lowered
 };
 
 struct Args {
@@ -90,6 +92,7 @@ struct Args {
   double* r0;   // the step's initial residual, and its FP32 copy: a restart of the PCG starts from them
   float* r032;
   int a32_mode;  // FP32 matrix in the PCG: 0 never, 1 when the bound allows (default), 2 every step
+  int order_cap; // 1: cap the warm-start order where the force history has a kink (default)
   double* part;
   Scal* s;
   // force (slot indices)

@@ -222,7 +222,7 @@ class NodeBlockNewmark:
     entries, receivers and outputs from/to the reference's equation numbering."""
 
     def __init__(self, g, dt, rtol=1e-12, max_iter=1000, precond="fsai", spmv="pair", explicit="pair",
-                 residual="pair", fp32_matrix="auto"):
+                 residual="pair", fp32_matrix="auto", order_cap=True):
         if g.adj_ptr is None:
             raise ValueError("GenerateMatrix has no node structure")
         self.g = g
@@ -275,9 +275,18 @@ class NodeBlockNewmark:
         # step's residual always in FP64 (by default it runs in pairs and hands over to FP64 by
         # itself when the load is nearly balanced by the elastic and inertial forces); bits 3, 4:
         # the PCG on the FP32 matrix (A's hi parts) never / at every step, instead of when the
-        # bound on its error allows (the answer meets rtol either way)
+        # bound on its error allows (the answer meets rtol either way); bit 5: no cap on the
+        # warm-start order at kinks of the force history
         nat.call("sc_nb_set_options", self.h, {"pair": 0, "fp64": 1}[spmv] | {"pair": 0, "fp64": 2}[explicit] |
-                 {"pair": 0, "fp64": 4}[residual] | {"auto": 0, "never": 8, "always": 16}[fp32_matrix])
+                 {"pair": 0, "fp64": 4}[residual] | {"auto": 0, "never": 8, "always": 16}[fp32_matrix] |
+                 (0 if order_cap else 32))
+
+    def warm_start_status(self):
+        """(the controller's current warm-start order, steps whose order the force history capped)."""
+        o = ctypes.c_int()
+        c = ctypes.c_int64()
+        nat.call("sc_nb_warm_start_status", self.h, ctypes.byref(o), ctypes.byref(c))
+        return o.value, c.value
 
     def fp32_matrix_status(self):
         """(steps whose PCG started on the FP32 matrix, steps that switched to it during the

@@ -91,6 +91,8 @@ def test_node_block_option_and_residual_checks(lib):
     assert lib.sc_nb_a32_status(None, ctypes.byref(n), ctypes.byref(n), ctypes.byref(n), None) == SC_BAD_ARG
     ms = ctypes.c_float()
     assert lib.sc_nb_time_spmv_a32(None, 1, 5, ctypes.byref(ms), None) == SC_BAD_ARG
+    order = ctypes.c_int()
+    assert lib.sc_nb_warm_start_status(None, ctypes.byref(order), ctypes.byref(n)) == SC_BAD_ARG
 
 
 def test_csr_option_checks(lib):

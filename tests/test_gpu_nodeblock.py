@@ -254,3 +254,43 @@ def test_fp32_matrix_meets_the_tolerance(cuda):
     assert a32 > 0 and restarts > 0
     a32, switched, restarts, _ = out["auto"][2]
     assert a32 + switched > 0 and restarts == 0
+
+
+def test_order_cap_at_a_load_kink(cuda):
+    """A heaviside load that ramps over 5 steps: the warm-start order is capped while its window
+    straddles the ramp's end, which takes fewer PCG iterations over the first 30 steps, and the
+    answer is the uncapped one to the PCG tolerance."""
+    from scatter_gb300 import meshgen
+    from scatter_gb300.force_external import Force
+    from scatter_gb300.solvers import NodeBlockNewmark
+    from scatter_gb300.system_matrix import GenerateMatrix
+
+    mats = {"lower": {"density": 2000.0, "Young": 150e6, "poisson": 0.25},
+            "upper": {"density": 1800.0, "Young": 30e6, "poisson": 0.3}}
+    m = meshgen.box_model(10, 6, 6, 0.5, layers=[(0.0, "lower"), (1.5, "upper")], bottom="020", x_faces="200",
+                          z_faces="002")
+    g = GenerateMatrix(m.number_eq, 2)
+    g.generate_stiffness_and_mass(m, mats)
+    g.absorbing_boundaries(m, mats, [1, 1], 1e3)
+    g.damping_Rayleigh([1, 0.02, 50, 0.02])
+    dt, n_t = 5e-5, 31
+    time = np.arange(n_t) * dt
+    top = m.top_nodes()
+    load = {"type": "heaviside", "force": [0, -1e4, 0], "node": [int(top[len(top) // 2])], "time": time[-1],
+            "ini_steps": 5}
+    F = Force()
+    F.initialise_load(load, time, m, None)
+    out = {}
+    for cap in (True, False):
+        s = NodeBlockNewmark(g, dt, order_cap=cap)
+        s.set_force(F.table)
+        s.set_output(1, np.arange(m.number_eq), n_t, what=("u",))
+        s.initial_acceleration()
+        s.run(0, n_t - 1)
+        rc, iters, _ = s.status()
+        assert rc == 0
+        out[cap] = (s.outputs()["u"].copy(), iters, s.warm_start_status()[1])
+        s.close()
+    assert out[True][2] > 0 and out[False][2] == 0
+    assert out[True][1] < out[False][1]
+    assert rel_l2(out[True][0], out[False][0]) <= 1e-10
