@@ -286,7 +286,7 @@ struct sc_nb_newmark {
   void* sell_mem[16] = {};
   int n_sell_mem = 0;
   cudaStream_t user = nullptr, cap = nullptr, cap2 = nullptr;
-  unsigned node_blocks = 1, vec_blocks = 1;
+  unsigned node_blocks = 1, vec_blocks = 1, pred_blocks = 1;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   // ---- explicit scheme (sc_explicit.cu), allocated on first use

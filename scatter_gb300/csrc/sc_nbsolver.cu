@@ -149,9 +149,16 @@ __global__ void k_force(Args g) {
 //     = f - K (up + beta vp) - M (alpha vp) - Cabs vp
 //   x0 = warm start;  A x0 = aM M x0 + aK K x0 + aC Cabs x0
 // stored: q1 = up + beta vp, q2 = alpha vp, y1 = vp, x0.
-// One thread per node: the pair residual's record of the node leaves in whole 16-byte stores.
+// One thread per slot (coalesced loads and stores), kPredNodes nodes per block of
+// D * kPredNodes threads: the pair residual's records of the block's nodes are assembled in
+// shared memory and leave as whole 16-byte stores.
+constexpr int kPredNodes = 128;
+
 template <int D>
-__global__ void k_predict(Args g) {
+__global__ void __launch_bounds__(D * kPredNodes) k_predict(Args g) {
+  constexpr int R = kRecFloats(D);
+  __shared__ float4 srec[kPredNodes * R / 4];
+  float* sr = reinterpret_cast<float*>(srec);
   const double dt = g.dt, h = 0.5 * dt, qq = 0.25 * dt * dt;
   // warm-start order p = min(history, order, the force history's cap) and its coefficients,
   // once per thread
@@ -164,57 +171,48 @@ __global__ void k_predict(Args g) {
   for (int k = 0; k < kHistMax; ++k) hs[k] = g.ah[hist_slot(g.s->head, k)];
   // while the pair residual runs, q1, q2 and the pair copy of x0 are read by no one
   const bool fp64_res = !g.res_pair || g.s->res_fp64;
-  constexpr int R = kRecFloats(D);
-  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < g.n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
-    float rec[R];
-#pragma unroll
-    for (int k = 6 * D; k < R; ++k) rec[k] = 0.f;
-    // the node's loads first (no store between them, so they are all in flight together)
-    double av[D], vv[D], uv[D], xs[D];
-    int fx[D];
-#pragma unroll
-    for (int c = 0; c < D; ++c) {
-      const int64_t i = n * D + c;
-      av[c] = g.a[i];
-      vv[c] = g.v[i];
-      uv[c] = g.u[i];
-      fx[c] = g.fixed[i];
+  for (int64_t n0 = (int64_t)blockIdx.x * kPredNodes; n0 < g.n_nodes; n0 += (int64_t)gridDim.x * kPredNodes) {
+    const int64_t i = n0 * D + threadIdx.x;
+    const int ln = threadIdx.x / D, c = threadIdx.x - ln * D;
+    if (i < g.n_s) {
+      const double ai = g.a[i], vi = g.v[i], ui = g.u[i];
+      const int fx = g.fixed[i];
       // x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k}, terms summed in a fixed order
-      xs[c] = cf[0] * av[c];
+      double xs = cf[0] * ai;
 #pragma unroll
       for (int k = 1; k <= kHistMax; ++k)
-        if (k <= p) xs[c] += cf[k] * hs[k - 1][i];
-    }
-#pragma unroll
-    for (int c = 0; c < D; ++c) {
-      const int64_t i = n * D + c;
-      const double ai = av[c], vi = vv[c];
+        if (k <= p) xs += cf[k] * hs[k - 1][i];
       const double vp = vi + h * ai;
-      const double up = uv[c] + dt * vi + qq * ai;
+      const double up = ui + dt * vi + qq * ai;
       const double q1 = up + g.beta_r * vp, q2 = g.alpha_r * vp;
       if (fp64_res) {
         g.q1[i] = q1;
         g.q2[i] = q2;
       }
       g.y1[i] = vp;
-      const double x0 = fx[c] ? 0.0 : xs[c];
+      const double x0 = fx ? 0.0 : xs;
       g.x0[i] = x0;
       if (g.spmv_pair && fp64_res) g.p2[i] = split_pair(x0);  // p2 is scratch until p is first written
       if (g.res_pair) {
         const float2 zk = split_pair(fma(g.aK, x0, q1)), zm = split_pair(fma(g.aM, x0, q2));
+        float* rec = sr + ln * R;
         rec[kRecM + 2 * c] = zm.x;
         rec[kRecM + 2 * c + 1] = zm.y;
         rec[kRecM + 2 * D + c] = (float)q2;
         rec[kRecK(D) + 2 * c] = zk.x;
         rec[kRecK(D) + 2 * c + 1] = zk.y;
         rec[kRecK(D) + 2 * D + c] = (float)q1;
+        if (c == 0)
+          for (int k = 6 * D; k < R; ++k) rec[k] = 0.f;
         g.zc[i] = fma(g.aC, x0, vp);
       }
     }
     if (g.res_pair) {
-      float4* rp = reinterpret_cast<float4*>(g.rrec + n * R);
-#pragma unroll
-      for (int k = 0; k < R / 4; ++k) rp[k] = make_float4(rec[4 * k], rec[4 * k + 1], rec[4 * k + 2], rec[4 * k + 3]);
+      __syncthreads();
+      const int64_t nodes = g.n_nodes - n0 < kPredNodes ? g.n_nodes - n0 : kPredNodes;
+      float4* dst = reinterpret_cast<float4*>(g.rrec + n0 * R);
+      for (int k = threadIdx.x; k < nodes * (R / 4); k += blockDim.x) dst[k] = srec[k];
+      __syncthreads();
     }
   }
 }
@@ -1227,7 +1225,7 @@ int build_graph(sc_nb_newmark* h) {
                     "capture")))
       break;
     k_force<<<1, 256, 0, cs>>>(g);
-    k_predict<D><<<vbk, 256, 0, cs>>>(g);
+    k_predict<D><<<h->pred_blocks, D * kPredNodes, 0, cs>>>(g);
     if (g.res_pair) {
       k_residual_kp<D><<<nbk, kThreads, 0, cs>>>(g);
       k_residual<D, true><<<nbk, kThreads, 0, cs>>>(g, 1);
@@ -1546,6 +1544,7 @@ extern "C" int sc_nb_create(sc_nb_newmark** out, int n_nodes, int dim, const int
     h->tpr_blocks = (unsigned)(want < 152 * 16 ? (want < 1 ? 1 : want) : 152 * 16);
   }
   h->vec_blocks = grid_for(ns, 256, 152 * 16);
+  h->pred_blocks = grid_for(n_nodes, kPredNodes, 152 * 16);
   cudaStream_t st = h->user;
   int rc = SC_OK;
   int* dflag = nullptr;
@@ -1673,7 +1672,7 @@ static int eager_step(sc_nb_newmark* h) {
   const unsigned nbk = h->node_blocks, vbk = h->vec_blocks;
   cudaGraphConditionalHandle none = 0;
   k_force<<<1, 256, 0, st>>>(g);
-  k_predict<D><<<vbk, 256, 0, st>>>(g);
+  k_predict<D><<<h->pred_blocks, D * kPredNodes, 0, st>>>(g);
   if (g.res_pair) {
     k_residual_kp<D><<<nbk, kThreads, 0, st>>>(g);
     k_residual<D, true><<<nbk, kThreads, 0, st>>>(g, 1);
