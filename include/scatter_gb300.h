@@ -184,8 +184,13 @@ int sc_newmark_set_predictor(sc_newmark* h, int order);
 /* options bit 0: run the PCG SpMV in FP64 (one FP64 FMA per stored value) instead of the
  * default FP32-pair arithmetic (A and M copied once as hi + lo FP32 pairs, 8 bytes per value
  * like FP64, products and the row sum by exact TwoProd/TwoSum, about 48 bits; the residual,
- * dot products and state stay FP64).  No reference counterpart. */
+ * dot products and state stay FP64).  bit 1: no cap on the warm-start order at kinks of the
+ * force history (the cap is on by default, as for sc_nb_set_options bit 5).  Options outside
+ * 0..3 are rejected.  No reference counterpart. */
 int sc_newmark_set_options(sc_newmark* h, int options);
+/* the controller's current warm-start order and the steps whose order the force history
+ * capped (synchronises) */
+int sc_newmark_warm_start_status(sc_newmark* h, int* order, int64_t* capped_steps);
 /* synchronous: CG status of the run so far (SC_OK / SC_NOT_CONVERGED / SC_BREAKDOWN),
  * total and maximum CG iterations per step */
 int sc_newmark_status(sc_newmark* h, int64_t* total_iters, int* max_iters_per_step);

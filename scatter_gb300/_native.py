@@ -42,6 +42,7 @@ SIGNATURES = {
     "sc_newmark_run": (I, [P, I, I]),
     "sc_newmark_set_predictor": (I, [P, I]),
     "sc_newmark_set_options": (I, [P, I]),
+    "sc_newmark_warm_start_status": (I, [P, ctypes.POINTER(I), ctypes.POINTER(L)]),
     "sc_newmark_status": (I, [P, ctypes.POINTER(L), ctypes.POINTER(I)]),
     "sc_newmark_time_spmv": (I, [P, I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(L)]),
     "sc_newmark_destroy": (I, [P]),

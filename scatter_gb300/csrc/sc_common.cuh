@@ -97,10 +97,113 @@ __device__ __forceinline__ int warm_start_order(const S* s, int fixed) {
 static_assert((kHistMax & (kHistMax - 1)) == 0, "the history ring's index wraps with a mask");
 __device__ __forceinline__ int hist_slot(int head, int k) { return (head + k) & (kHistMax - 1); }
 
+// The warm start's order cap.  The accelerations respond to the load at once, so a window of
+// past accelerations that straddles a kink in the load history (the end of a ramp, a load that
+// starts to move, a point load that moves onto another face) extrapolates badly, and a lower
+// order whose window lies after the kink does better (at the benchmark workload, the steps
+// after a 5-step ramp took 15, 14, 12, 10, 8, 6 PCG iterations at orders 1..5 against 18, 19,
+// 19, 18, 17, 15 at order 6).  So each step takes the largest order q <= the controller's order
+// whose extrapolation of the force itself reproduces, to kCapTol of the rows' largest entry,
+// the force of the newest row from the q + 1 rows before it.  One block (the force kernel's);
+// each distinct index of the rows is summed by the thread holding its first entry, rows in a
+// fixed order (deterministic); windows whose rows hold more than kCapRow entries keep the order.
+constexpr double kCapTol = 1e-6;
+constexpr int kCapRow = 256;
+
+// the force table: rows 0..n_t-1, row t's entries ptr[t] .. ptr[t+1]-1 at indices idx, values val
+struct ForceRows {
+  int n_t;
+  const int64_t* ptr;
+  const int* idx;
+  const double* val;
+  __device__ int64_t find(int row, int i) const {
+    if (row < 0 || row >= n_t) return -1;
+    for (int64_t e = ptr[row]; e < ptr[row + 1]; ++e)
+      if (idx[e] == i) return e;
+    return -1;
+  }
+};
+
+// max |f_{m+1} - sum_{k<=q} cf[k] f_{m-k}| / max |f| over those rows (0 when they hold no force),
+// in thread 0
+__device__ inline double cap_misfit(const ForceRows& F, int q, int m, const double* cf) {
+  __shared__ double mx[2][32];
+  double rmx = 0.0, fmx = 0.0;
+  for (int j = 0; j <= q + 1; ++j) {  // rows in the order m+1, m, m-1, ..., m-q
+    const int row = m + 1 - j;
+    if (row < 0 || row >= F.n_t) continue;
+    for (int64_t e = F.ptr[row] + threadIdx.x; e < F.ptr[row + 1]; e += blockDim.x) {
+      const int i = F.idx[e];
+      fmx = fmax(fmx, fabs(F.val[e]));
+      bool first = true;
+      for (int k = 0; k < j && first; ++k) first = F.find(m + 1 - k, i) < 0;
+      if (!first) continue;
+      double r = 0.0;
+      for (int k = 0; k <= q + 1; ++k) {
+        const int64_t h = k == j ? e : F.find(m + 1 - k, i);
+        if (h >= 0) r += (k == 0 ? 1.0 : -cf[k - 1]) * F.val[h];
+      }
+      rmx = fmax(rmx, fabs(r));
+    }
+  }
+  // block maxima (order-independent, so the cap is deterministic)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    rmx = fmax(rmx, __shfl_xor_sync(0xffffffffu, rmx, o));
+    fmx = fmax(fmx, __shfl_xor_sync(0xffffffffu, fmx, o));
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) {
+    mx[0][wid] = rmx;
+    mx[1][wid] = fmx;
+  }
+  __syncthreads();
+  double r = 0.0, f = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      r = fmax(r, mx[0][w]);
+      f = fmax(f, mx[1][w]);
+    }
+  return f > 0.0 ? r / f : 0.0;
+}
+
+// sets s->pcap for step s->t (counting in s->capped the steps it lowers); all threads of the
+// block call it
+template <class S>
+__device__ void warm_start_order_cap(S* s, int fixed, int enabled, const ForceRows& F) {
+  __shared__ int cap_s;
+  const int t = s->t;
+  const int p = warm_start_order(s, fixed);
+  int cap = p;
+  bool small = enabled && F.ptr && p > 0;
+  if (small)
+    for (int row = t - p; row <= t + 1; ++row)
+      if (row >= 0 && row < F.n_t && F.ptr[row + 1] - F.ptr[row] > kCapRow) small = false;
+  if (small) {
+    double cf[kHistMax + 1];
+    for (cap = p; cap > 0; --cap) {
+      warm_start_coeffs(cap, cf);
+      const double e1 = cap_misfit(F, cap, t, cf);
+      if (threadIdx.x == 0) cap_s = e1 <= kCapTol ? 1 : 0;
+      __syncthreads();
+      const int ok = cap_s;
+      __syncthreads();
+      if (ok) break;
+    }
+  }
+  if (threadIdx.x == 0) {
+    s->pcap = cap;
+    if (cap < p) s->capped += 1;
+  }
+}
+
 template <class S>
 __device__ inline void warm_start_init(S* s) {
   s->hist = 0;
   s->head = 0;
+  s->pcap = kHistMax;
+  s->capped = 0;
   s->pord = kPredStart;
   s->pdir = 1;
   s->win_n = s->win_it = s->probing = s->hold = 0;

@@ -35,98 +35,6 @@ namespace nb {
 
 // ------------------------------------------------------------------ per-step kernels
 
-// The warm start's order cap.  The accelerations respond to the load at once, so a window of
-// past accelerations that straddles a kink in the load history (the end of a ramp, a load that
-// starts to move, a point load that moves onto another face) extrapolates badly, and a lower
-// order whose window lies after the kink does better (at the benchmark workload, the steps
-// after a 5-step ramp took 15, 14, 12, 10, 8, 6 PCG iterations at orders 1..5 against 18, 19,
-// 19, 18, 17, 15 at order 6).  So each step takes the largest order q <= the controller's order
-// whose extrapolation of the force itself reproduces, to kCapTol of the rows' largest entry,
-// the force of the newest row from the q + 1 rows before it.  One block;
-// each distinct slot of the rows is summed by the thread holding its first entry, rows in a
-// fixed order (deterministic); windows whose rows hold more than kCapRow entries keep the order.
-constexpr double kCapTol = 1e-6;
-constexpr int kCapRow = 256;
-
-__device__ inline int64_t row_find(const Args& g, int row, int slot) {
-  if (row < 0 || row >= g.n_t) return -1;
-  for (int64_t e = g.f_ptr[row]; e < g.f_ptr[row + 1]; ++e)
-    if (g.f_slot[e] == slot) return e;
-  return -1;
-}
-
-// max |f_{m+1} - sum_{k<=q} cf[k] f_{m-k}| / max |f| over those rows (0 when they hold no force),
-// in thread 0
-__device__ double cap_misfit(const Args& g, int q, int m, const double* cf) {
-  __shared__ double mx[2][32];
-  double rmx = 0.0, fmx = 0.0;
-  for (int j = 0; j <= q + 1; ++j) {  // rows in the order m+1, m, m-1, ..., m-q
-    const int row = m + 1 - j;
-    if (row < 0 || row >= g.n_t) continue;
-    for (int64_t e = g.f_ptr[row] + threadIdx.x; e < g.f_ptr[row + 1]; e += blockDim.x) {
-      const int slot = g.f_slot[e];
-      fmx = fmax(fmx, fabs(g.f_val[e]));
-      bool first = true;
-      for (int i = 0; i < j && first; ++i) first = row_find(g, m + 1 - i, slot) < 0;
-      if (!first) continue;
-      double r = 0.0;
-      for (int i = 0; i <= q + 1; ++i) {
-        const int64_t h = i == j ? e : row_find(g, m + 1 - i, slot);
-        if (h >= 0) r += (i == 0 ? 1.0 : -cf[i - 1]) * g.f_val[h];
-      }
-      rmx = fmax(rmx, fabs(r));
-    }
-  }
-  // block maxima (order-independent, so the cap is deterministic)
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    rmx = fmax(rmx, __shfl_xor_sync(0xffffffffu, rmx, o));
-    fmx = fmax(fmx, __shfl_xor_sync(0xffffffffu, fmx, o));
-  }
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) {
-    mx[0][wid] = rmx;
-    mx[1][wid] = fmx;
-  }
-  __syncthreads();
-  double r = 0.0, f = 0.0;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      r = fmax(r, mx[0][w]);
-      f = fmax(f, mx[1][w]);
-    }
-  return f > 0.0 ? r / f : 0.0;
-}
-
-__device__ void order_cap(const Args& g) {
-  __shared__ int cap_s;
-  Scal* s = g.s;
-  const int t = s->t;
-  const int p = warm_start_order(s, g.pred_order);
-  int cap = p;
-  bool small = g.order_cap && g.f_ptr && p > 0;
-  if (small)
-    for (int row = t - p; row <= t + 1; ++row)
-      if (row >= 0 && row < g.n_t && g.f_ptr[row + 1] - g.f_ptr[row] > kCapRow) small = false;
-  if (small) {
-    double cf[kHistMax + 1];
-    for (cap = p; cap > 0; --cap) {
-      warm_start_coeffs(cap, cf);
-      const double e1 = cap_misfit(g, cap, t, cf);
-      if (threadIdx.x == 0) cap_s = e1 <= kCapTol ? 1 : 0;
-      __syncthreads();
-      const int ok = cap_s;
-      __syncthreads();
-      if (ok) break;
-    }
-  }
-  if (threadIdx.x == 0) {
-    s->pcap = cap;
-    if (cap < p) s->capped += 1;
-  }
-}
-
 // The step's force (step t's entries cleared, step t + 1's added), then the warm start's order cap
 // (one block)
 __global__ void k_force(Args g) {
@@ -140,7 +48,7 @@ __global__ void k_force(Args g) {
       for (int64_t k = g.f_ptr[t1] + threadIdx.x; k < g.f_ptr[t1 + 1]; k += blockDim.x)
         g.f[g.f_slot[k]] += g.f_val[k];
   }
-  order_cap(g);
+  warm_start_order_cap(g.s, g.pred_order, g.order_cap, ForceRows{g.n_t, g.f_ptr, g.f_slot, g.f_val});
 }
 
 // Predictor vectors (slot space):
@@ -1186,8 +1094,6 @@ __global__ void k_init_scal(Scal* s, double tol2, int max_it) {
   s->rr0 = s->dd = s->dd_pre = 0.0;
   s->rho = -1.0;
   s->a32_steps = s->switched = s->restarts = 0;
-  s->pcap = kHistMax;
-  s->capped = 0;
   warm_start_init(s);
 }
 

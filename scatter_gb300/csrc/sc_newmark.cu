@@ -48,6 +48,8 @@ struct NmScalars {
   unsigned int ticket;
   // adaptive warm-start order: current order, probing direction, window and hold counters
   int pord, pdir, win_n, win_it, probing, hold;
+  int pcap;          // this step's cap on the order from the force history (warm_start_order_cap)
+  long long capped;  // steps whose order the cap lowered
 };
 
 struct NmArgs {
@@ -59,6 +61,7 @@ struct NmArgs {
   double *vp, *up, *x, *r, *z, *p, *w, *dinv, *f;
   double* ah[kHistMax];  // previous accelerations, a ring: a_{n-1-k} in ah[hist_slot(head, k)]
   int pred_order;        // warm-start order (1..kHistMax), 0: adaptive (NmScalars::pord)
+  int order_cap;         // 1: cap the order where the force history has a kink (default)
   double* part;          // [nblocks][4]
   NmScalars* s;
   double dt;
@@ -93,21 +96,26 @@ __device__ inline double reduce_parts(const double* part, int k, double* sh) {
 }
 
 __global__ void k_force(NmArgs g) {
-  // clear the entries of step t, write those of step t+1 (dense f)
+  // clear the entries of step t, write those of step t+1 (dense f); then the warm start's order
+  // cap from the force history (one block)
   const int t = g.s->t;
-  if (g.f_ptr == nullptr) return;
-  if (t >= 0 && t < g.n_t)
-    for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f[g.f_eq[k]] = 0.0;
-  __syncthreads();
-  const int t1 = t + 1;
-  if (t1 >= 0 && t1 < g.n_t)
-    for (int64_t k = g.f_ptr[t1] + threadIdx.x; k < g.f_ptr[t1 + 1]; k += blockDim.x) g.f[g.f_eq[k]] += g.f_val[k];
+  if (g.f_ptr != nullptr) {
+    if (t >= 0 && t < g.n_t)
+      for (int64_t k = g.f_ptr[t] + threadIdx.x; k < g.f_ptr[t + 1]; k += blockDim.x) g.f[g.f_eq[k]] = 0.0;
+    __syncthreads();
+    const int t1 = t + 1;
+    if (t1 >= 0 && t1 < g.n_t)
+      for (int64_t k = g.f_ptr[t1] + threadIdx.x; k < g.f_ptr[t1 + 1]; k += blockDim.x)
+        g.f[g.f_eq[k]] += g.f_val[k];
+  }
+  warm_start_order_cap(g.s, g.pred_order, g.order_cap, ForceRows{g.n_t, g.f_ptr, g.f_eq, g.f_val});
 }
 
 // vp, up ; the warm start x0 into w (w is scratch until the first k_spmv of the step)
 __global__ void k_predict(NmArgs g) {
   const double dt = g.dt, h = 0.5 * dt, q = 0.25 * dt * dt;
-  const int p = warm_start_order(g.s, g.pred_order);
+  const int p0 = warm_start_order(g.s, g.pred_order);
+  const int p = g.s->pcap < p0 ? g.s->pcap : p0;  // the force history's cap
   double cf[kHistMax + 1];
   warm_start_coeffs(p, cf);
   const double* hs[kHistMax];  // a_{n-1-k}
@@ -557,6 +565,7 @@ extern "C" int sc_newmark_create(sc_newmark** out, int64_t n_eq, const int64_t* 
     p += n_eq;
   }
   g.pred_order = 0;  // adaptive
+  g.order_cap = 1;
   h->row_blocks = row_blocks_for(n_eq);
   h->vec_blocks = grid_for(n_eq, 256, 152 * 16);
   g.part = p; p += 4 * (int64_t)(h->row_blocks > h->vec_blocks ? h->row_blocks : h->vec_blocks);
@@ -653,11 +662,24 @@ int pair_prepare(sc_newmark* h) {
 }
 }  // namespace
 
-// options bit 0: the SpMV in FP64 instead of FP32-pair arithmetic
+// options bit 0: the SpMV in FP64 instead of FP32-pair arithmetic; bit 1: no cap on the
+// warm-start order at kinks of the force history
 extern "C" int sc_newmark_set_options(sc_newmark* h, int options) {
-  if (!h || options < 0 || options > 1) return SC_BAD_ARG;
+  if (!h || options < 0 || options > 3) return SC_BAD_ARG;
   h->pair = (options & 1) ? 0 : 1;
+  h->g.order_cap = (options & 2) ? 0 : 1;
   drop_graphs(h);
+  return SC_OK;
+}
+
+extern "C" int sc_newmark_warm_start_status(sc_newmark* h, int* order, int64_t* capped_steps) {
+  if (!h) return SC_BAD_ARG;
+  int rc = check(cudaStreamSynchronize(h->user), "sync status");
+  if (rc) return rc;
+  NmScalars s;
+  if ((rc = check(cudaMemcpy(&s, h->g.s, sizeof(s), cudaMemcpyDeviceToHost), "read scalars"))) return rc;
+  if (order) *order = h->g.pred_order > 0 ? h->g.pred_order : s.pord;
+  if (capped_steps) *capped_steps = s.capped;
   return SC_OK;
 }
 

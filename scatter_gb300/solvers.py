@@ -133,7 +133,7 @@ def _device_matrices(M, C, K):
 class NewmarkGPU:
     """Device state + step loop on a shared CSR pattern (thin owner of the C-ABI handle)."""
 
-    def __init__(self, pattern, M, C, K, dt, rtol=1e-12, max_iter=1000, spmv="pair"):
+    def __init__(self, pattern, M, C, K, dt, rtol=1e-12, max_iter=1000, spmv="pair", order_cap=True):
         self.pattern = pattern
         n = pattern.n
         self.n = n
@@ -149,9 +149,17 @@ class NewmarkGPU:
                  M.data_ptr(), C.data_ptr(), K.data_ptr(), self.A.data_ptr(), float(dt), float(rtol), int(max_iter),
                  self.u.data_ptr(), self.v.data_ptr(), self.a.data_ptr(), self.ws.data_ptr(), wsn, dv.stream_ptr())
         self.h = h
-        # bit 0: the PCG SpMV in FP64 instead of FP32 pairs
-        nat.call("sc_newmark_set_options", self.h, {"pair": 0, "fp64": 1}[spmv])
+        # bit 0: the PCG SpMV in FP64 instead of FP32 pairs; bit 1: no cap on the warm-start
+        # order at kinks of the force history
+        nat.call("sc_newmark_set_options", self.h, {"pair": 0, "fp64": 1}[spmv] | (0 if order_cap else 2))
         self._keep = []
+
+    def warm_start_status(self):
+        """(the controller's current warm-start order, steps whose order the force history capped)."""
+        o = ctypes.c_int()
+        c = ctypes.c_int64()
+        nat.call("sc_newmark_warm_start_status", self.h, ctypes.byref(o), ctypes.byref(c))
+        return o.value, c.value
 
     def set_force(self, table: ForceTable, stream=False):
         """Force history (equation indices).  stream=True: values copied per run (push_force)."""

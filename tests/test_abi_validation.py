@@ -97,3 +97,5 @@ def test_node_block_option_and_residual_checks(lib):
 
 def test_csr_option_checks(lib):
     assert lib.sc_newmark_set_options(None, 0) == SC_BAD_ARG
+    order, n = ctypes.c_int(), ctypes.c_int64()
+    assert lib.sc_newmark_warm_start_status(None, ctypes.byref(order), ctypes.byref(n)) == SC_BAD_ARG

@@ -256,13 +256,14 @@ def test_fp32_matrix_meets_the_tolerance(cuda):
     assert a32 + switched > 0 and restarts == 0
 
 
-def test_order_cap_at_a_load_kink(cuda):
+@pytest.mark.parametrize("layout", ["node-block", "csr"])
+def test_order_cap_at_a_load_kink(cuda, layout):
     """A heaviside load that ramps over 5 steps: the warm-start order is capped while its window
     straddles the ramp's end, which takes fewer PCG iterations over the first 30 steps, and the
-    answer is the uncapped one to the PCG tolerance."""
+    answer is the uncapped one to the PCG tolerance (both Newmark solvers)."""
     from scatter_gb300 import meshgen
     from scatter_gb300.force_external import Force
-    from scatter_gb300.solvers import NodeBlockNewmark
+    from scatter_gb300.solvers import NewmarkGPU, NodeBlockNewmark, _device_matrices
     from scatter_gb300.system_matrix import GenerateMatrix
 
     mats = {"lower": {"density": 2000.0, "Young": 150e6, "poisson": 0.25},
@@ -281,8 +282,13 @@ def test_order_cap_at_a_load_kink(cuda):
     F = Force()
     F.initialise_load(load, time, m, None)
     out = {}
+    if layout == "csr":
+        pat, Md, Cd, Kd = _device_matrices(g.M, g.C, g.K)
     for cap in (True, False):
-        s = NodeBlockNewmark(g, dt, order_cap=cap)
+        if layout == "csr":
+            s = NewmarkGPU(pat, Md, Cd, Kd, dt, order_cap=cap)
+        else:
+            s = NodeBlockNewmark(g, dt, order_cap=cap)
         s.set_force(F.table)
         s.set_output(1, np.arange(m.number_eq), n_t, what=("u",))
         s.initial_acceleration()
