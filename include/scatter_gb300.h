@@ -379,8 +379,9 @@ int sc_batch_create(sc_batch** h, const sc_batch_desc* desc, double* u, double* 
 /* The step kernel and its shape (realisations per thread, threads per block) are picked at
  * create time, and again by sc_batch_set_hex8_grid, by timing the candidates on scratch
  * copies of the state (no reference counterpart); this reports the choice, its per-step time
- * and which kernel it is: 0 the incidence-list kernel, 1 the uniform hexa8 grid kernel, 2 the
- * tensor-core kernel (realisations_per_thread then reports its column segment length). */
+ * and which kernel it is: 0 the incidence-list kernel, 1 the uniform hexa8 grid kernel (tiled),
+ * 2 the tensor-core kernel (realisations_per_thread then reports its column segment length),
+ * 3 the node-centric uniform hexa8 kernel. */
 int sc_batch_config(sc_batch* h, int* realisations_per_thread, int* threads_per_block, float* ms_per_step,
                     int* grid_kernel);
 /* Uniform hexa8 grids (no reference counterpart; the meshes scatter/mesher.py reads from
@@ -391,9 +392,11 @@ int sc_batch_config(sc_batch* h, int* realisations_per_thread, int* threads_per_
  * the nodes of each tile grown by one point on every side, point (hx, hy, hz) of the 6 x 6 x 4
  * box at hx + 6 (hy + 6 hz) (-1 where the lattice has no node); elem8 [n_nodes][8] int32 the
  * element in which the node is local node la (-1 where none).  The incidence lists must be
- * sorted by the node's local index in the element (that order is the summation order of both
- * kernels, so they give bitwise the same results).  Device arrays owned by the caller; the
- * tuner then times both kernels. */
+ * sorted by the node's local index in the element (that order is the summation order of the
+ * kernels, so they give bitwise the same results).  Two kernels use these tables: the tiled
+ * one (the tiles' w staged in shared memory) and a node-centric one that takes each incident
+ * element's local index at compile time, so that every K1 entry is an operand of its FMAs
+ * rather than a load.  Device arrays owned by the caller; the tuner then times all kernels. */
 int sc_batch_set_hex8_grid(sc_batch* h, int n_tiles, const int* halo, const int* elem8);
 /* The tensor-core step on a uniform hexa8 grid (no reference counterpart): the element
  * products D = W K1 for 128 realisations at a time on tcgen05 (TF32 in three hi/lo products,
@@ -411,10 +414,13 @@ int sc_batch_set_hex8_columns(sc_batch* h, int n_col, int nzp, const int* nodes,
 int sc_batch_status(sc_batch* h);
 /* testing aids: force a shape of the incidence-list kernel (realisations per thread in
  * {1, 2, 4, 8} dividing R, by 4 for 4 and 8; threads per block a multiple of R / rpt, at most
- * 256), or of the uniform hexa8 grid kernel (1 or 2 realisations per thread, 128 or 256
- * threads per block), or the tensor-core kernel with column segments of seg points */
+ * 256), or of the tiled uniform hexa8 grid kernel (1 or 2 realisations per thread, 128 or 256
+ * threads per block), or of the node-centric uniform hexa8 kernel (2, 4 or 8 realisations per
+ * thread dividing R, by 4 for 4 and 8; 128 or 256 threads per block, at least R / rpt), or the
+ * tensor-core kernel with column segments of seg points */
 int sc_batch_set_shape(sc_batch* h, int realisations_per_thread, int threads_per_block);
 int sc_batch_set_grid_shape(sc_batch* h, int realisations_per_thread, int threads_per_block);
+int sc_batch_set_node_shape(sc_batch* h, int realisations_per_thread, int threads_per_block);
 int sc_batch_set_tc_shape(sc_batch* h, int seg);
 int sc_batch_set_force(sc_batch* h, int n_t, const int64_t* f_ptr, const int* f_slot, const double* f_val);
 /* receivers record v [n_out][n_rec][R] every out_interval steps */

@@ -287,20 +287,22 @@ class BatchedExplicit:
         self.l_c = dv.to_dev(c.astype(np.float32), torch.float32)
         self.l_s = dv.to_dev(sv.astype(np.float32), torch.float32)
 
-    KERNELS = {0: "incidence lists (k_batch_step)", 1: "uniform hexa8 grid (k_batch_step_hex8g)",
-               2: "tensor cores (k_batch_step_tc)"}
+    KERNELS = {0: "incidence lists (k_batch_step)", 1: "uniform hexa8 grid, tiled (k_batch_step_hex8g)",
+               2: "tensor cores (k_batch_step_tc)", 3: "uniform hexa8 grid, node-centric (k_batch_step_hex8c)"}
 
     def config(self):
         """(realisations per thread, threads per block, tuned ms per step, kernel) of the step
-        kernel; kernel 0 incidence lists, 1 the uniform hexa8 grid kernel, 2 the tensor-core
-        kernel (whose first value is then its column segment length)."""
+        kernel; kernel 0 incidence lists, 1 the tiled uniform hexa8 grid kernel, 2 the
+        tensor-core kernel (whose first value is then its column segment length), 3 the
+        node-centric uniform hexa8 kernel."""
         rpt, tpb, ms, grid = ctypes.c_int(), ctypes.c_int(), ctypes.c_float(), ctypes.c_int()
         nat.call("sc_batch_config", self.h, ctypes.byref(rpt), ctypes.byref(tpb), ctypes.byref(ms), ctypes.byref(grid))
         return rpt.value, tpb.value, ms.value, grid.value
 
     def set_shape(self, realisations_per_thread, threads_per_block, grid=False):
-        """Override the tuned kernel and shape (testing aid)."""
-        fn = "sc_batch_set_grid_shape" if grid else "sc_batch_set_shape"
+        """Override the tuned kernel and shape (testing aid): grid False the incidence-list
+        kernel, True the tiled uniform hexa8 kernel, "node" the node-centric one."""
+        fn = {False: "sc_batch_set_shape", True: "sc_batch_set_grid_shape", "node": "sc_batch_set_node_shape"}[grid]
         nat.call(fn, self.h, int(realisations_per_thread), int(threads_per_block))
 
     def set_tensor_core_shape(self, segment):

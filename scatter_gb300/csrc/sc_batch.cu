@@ -407,6 +407,64 @@ __device__ __forceinline__ void lds_f(const float* p, float (&v)[RPT]) {
   }
 }
 
+// One step for all realisations on a uniform hexa8 grid, node-centric like k_batch_step (tpn
+// threads per node, RPT realisations each).  elem8 gives the node's incident elements with its
+// local index la known at compile time, so every K1 entry is a constant-bank operand of its
+// FMAs (k1 is a kernel parameter): per node the loads are the 8 elements' node lists (the same
+// for the whole warp), their w as RPT-vectors and E, against 576 RPT FMAs.  k_batch_step instead
+// loads each K1 entry it uses (576 per node and thread).  The elements are taken in la order and
+// the products in the same order as there, so the results are bitwise the same.
+template <int RPT>
+__global__ void __launch_bounds__(256) k_batch_step_hex8c(Args g, const __grid_constant__ K1Hex8 k1,
+                                                         const int* __restrict__ elem8, const float* __restrict__ w_in,
+                                                         float* __restrict__ w_out, const float* __restrict__ vf_in,
+                                                         float* __restrict__ vf_out, int tpn) {
+  const int npb = blockDim.x / tpn;
+  const int sub = threadIdx.x / tpn;
+  const int r0 = (threadIdx.x % tpn) * RPT;
+  const bool active = sub < npb && r0 < g.d.R;
+  const int step = *g.t + 1;
+  const bool rec_now = record_now(g, step);
+  const int R = g.d.R;
+  for (int a = blockIdx.x * npb + sub; active && a < g.d.n_nodes; a += gridDim.x * npb) {
+    float acc[3][RPT];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) acc[c][r] = 0.f;
+#pragma unroll
+    for (int la = 0; la < 8; ++la) {
+      const int e = __ldg(elem8 + (int64_t)a * 8 + la);
+      if (e < 0) continue;
+      const int* en = g.d.elem + (int64_t)e * 8;
+      float t[3][RPT];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) t[c][r] = 0.f;
+#pragma unroll
+      for (int lb = 0; lb < 8; ++lb) {
+        const int64_t bs = (int64_t)__ldg(en + lb) * 3;
+        float w0[RPT], w1[RPT], w2[RPT];
+        ldf<RPT>(w_in + (bs + 0) * R + r0, w0);
+        ldf<RPT>(w_in + (bs + 1) * R + r0, w1);
+        ldf<RPT>(w_in + (bs + 2) * R + r0, w2);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float* kr = k1.k + (3 * la + c) * 24 + 3 * lb;
+          fma3<RPT>(t[c], kr[0], kr[1], kr[2], w0, w1, w2);
+        }
+      }
+      float Ee[RPT];
+      ldf<RPT>(g.d.young + (int64_t)e * R + r0, Ee);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) fma1<RPT>(acc[c], Ee, t[c]);
+    }
+    node_update<RPT>(g, a, r0, acc, w_in, w_out, vf_in, vf_out, step, rec_now);
+  }
+  step_epilogue(g, step);
+}
+
 // One step for all realisations on a uniform hexa8 grid: grid (tiles, realisation chunks of
 // 32 RPT), dynamic shared memory kHN * 3 * 32 RPT floats.
 template <int RPT>
@@ -980,7 +1038,8 @@ static void launch_hex8g(const sc_batch* h, const Args& g, int threads, cudaStre
 }
 
 // grid = 1: the uniform hexa8 grid kernel (threads per block, realisations per thread; tpn unused);
-// grid = 2: the tensor-core kernel (rpt = points per column segment along the sweep axis)
+// grid = 2: the tensor-core kernel (rpt = points per column segment along the sweep axis);
+// grid = 3: the node-centric uniform hexa8 kernel (shapes as grid = 0)
 static void batch_launch(const sc_batch* h, const Args& g, int grid, int rpt, int threads, int tpn, cudaStream_t st,
                          const float* wi, float* wo, const float* vi, float* vo) {
   if (grid == 2) {
@@ -991,7 +1050,7 @@ static void batch_launch(const sc_batch* h, const Args& g, int grid, int rpt, in
                       st>>>(g, h->k1, tt, wi, wo, vi, vo);
     return;
   }
-  if (grid) {
+  if (grid == 1) {
     if (rpt == 2) launch_hex8g<2>(h, g, threads, st, wi, wo, vi, vo);
     else launch_hex8g<1>(h, g, threads, st, wi, wo, vi, vo);
     return;
@@ -999,6 +1058,14 @@ static void batch_launch(const sc_batch* h, const Args& g, int grid, int rpt, in
   const int npb = threads / tpn;
   const int64_t want = ((int64_t)g.d.n_nodes + npb - 1) / npb;
   const unsigned blocks = (unsigned)(want < 152 * 32 ? want : 152 * 32);
+  if (grid == 3) {
+    switch (rpt) {
+      case 8: k_batch_step_hex8c<8><<<blocks, threads, 0, st>>>(g, h->k1, h->elem8, wi, wo, vi, vo, tpn); break;
+      case 4: k_batch_step_hex8c<4><<<blocks, threads, 0, st>>>(g, h->k1, h->elem8, wi, wo, vi, vo, tpn); break;
+      default: k_batch_step_hex8c<2><<<blocks, threads, 0, st>>>(g, h->k1, h->elem8, wi, wo, vi, vo, tpn); break;
+    }
+    return;
+  }
   if (g.d.node_nen) {
     k_batch_step_mixed<<<blocks, threads, 0, st>>>(g, wi, wo, vi, vo);
     return;
@@ -1068,10 +1135,17 @@ static int batch_tune(sc_batch* h) {
       for (int bi = 0; bi < (mixed ? 3 : 2); ++bi)
         if (tpn <= tpbs[bi]) cands.push_back({0, rpt, (tpbs[bi] / tpn) * tpn, tpn});
     }
-    if (h->halo)
+    if (h->halo) {
       for (int rpt = 1; rpt <= 2; ++rpt)
         if (R % rpt == 0)
           for (int threads : {256, 128}) cands.push_back({1, rpt, threads, 0});
+      for (int rpt : {2, 4, 8}) {
+        if (R % rpt != 0 || (rpt >= 4 && R % 4 != 0)) continue;
+        const int tpn = R / rpt;
+        for (int threads : {128, 256})
+          if (tpn <= threads) cands.push_back({3, rpt, (threads / tpn) * tpn, tpn});
+      }
+    }
     if (h->tt.nodes) {  // tensor-core kernel: segments of the whole column, a half, a third, a quarter
       int last = 0;
       for (int parts = 1; parts <= 4; ++parts) {
@@ -1241,6 +1315,23 @@ extern "C" int sc_batch_set_grid_shape(sc_batch* h, int realisations_per_thread,
   h->rpt = rpt;
   h->threads = threads_per_block;
   h->tpn = 0;
+  batch_drop_graphs(h);
+  return SC_OK;
+}
+
+// Selects the node-centric uniform hexa8 kernel with 2, 4 or 8 realisations per thread and 128
+// or 256 threads per block (testing aid; needs sc_batch_set_hex8_grid).
+extern "C" int sc_batch_set_node_shape(sc_batch* h, int realisations_per_thread, int threads_per_block) {
+  if (!h || !h->halo) return SC_BAD_ARG;
+  const int rpt = realisations_per_thread, R = h->g.d.R;
+  if ((rpt != 2 && rpt != 4 && rpt != 8) || R % rpt != 0 || (rpt >= 4 && R % 4 != 0)) return SC_BAD_ARG;
+  if (threads_per_block != 128 && threads_per_block != 256) return SC_BAD_ARG;
+  const int tpn = R / rpt;
+  if (tpn > threads_per_block) return SC_BAD_ARG;
+  h->grid = 3;
+  h->rpt = rpt;
+  h->threads = (threads_per_block / tpn) * tpn;
+  h->tpn = tpn;
   batch_drop_graphs(h);
   return SC_OK;
 }

@@ -112,8 +112,9 @@ def test_batched_matches_per_realisation_fp64(cuda):
 
 def test_batched_shapes_agree_bitwise(cuda):
     """Every kernel and shape the tuner may pick (the incidence-list kernel with 1 to 8
-    realisations per thread, the uniform hexa8 grid kernel with 1 or 2) gives bitwise the same
-    histories: the per-realisation arithmetic and summation order are the same."""
+    realisations per thread, the tiled uniform hexa8 grid kernel with 1 or 2, the node-centric
+    one with 2 to 8) gives bitwise the same histories: the per-realisation arithmetic and
+    summation order are the same."""
     from scatter_gb300 import meshgen
     from scatter_gb300.batched import BatchedExplicit
     from scatter_gb300.force_external import ricker_table
@@ -129,7 +130,7 @@ def test_batched_shapes_agree_bitwise(cuda):
     rec = [int(m.eq_nb_dof[m.node_index()[n], 1]) for n in top[::5]]
     results = []
     shapes = ((1, 128, False), (1, 256, False), (2, 128, False), (4, 256, False), (8, 128, False), (1, 128, True),
-              (1, 256, True), (2, 128, True), (2, 256, True))
+              (1, 256, True), (2, 128, True), (2, 256, True), (2, 128, "node"), (4, 256, "node"), (8, 128, "node"))
     for rpt, tpb, grid in shapes:
         b = BatchedExplicit(m, young, 0.3, 1900.0, [1, 0.02, 50, 0.02], [1, 1], 1e3, dt)
         assert b.grid_tables is not None
@@ -146,9 +147,9 @@ def test_batched_shapes_agree_bitwise(cuda):
 
 
 def test_batched_grid_kernel_on_a_notched_mesh(cuda):
-    """The tiled uniform-grid kernel on a box with a block of elements cut out of a top
-    corner (halo points without nodes, nodes with fewer than 8 elements) gives bitwise the
-    incidence-list kernel's histories."""
+    """The uniform-grid kernels (tiled and node-centric) on a box with a block of elements cut
+    out of a top corner (halo points without nodes, nodes with fewer than 8 elements) give
+    bitwise the incidence-list kernel's histories."""
     from scatter_gb300 import meshgen
     from scatter_gb300.batched import BatchedExplicit
     from scatter_gb300.force_external import ricker_table
@@ -176,7 +177,7 @@ def test_batched_grid_kernel_on_a_notched_mesh(cuda):
     table = ricker_table(m, int(top[0]), -1e4, 40.0, 0.002, time)
     rec = [int(m.eq_nb_dof[m.node_index()[n], 1]) for n in top[::2]]
     results = []
-    for rpt, tpb, grid in ((4, 256, False), (1, 256, True), (2, 256, True)):
+    for rpt, tpb, grid in ((4, 256, False), (1, 256, True), (2, 256, True), (4, 128, "node"), (8, 256, "node")):
         b = BatchedExplicit(m, young, 0.3, 1900.0, [1, 0.02, 50, 0.02], [1, 1], 1e3, dt)
         assert b.grid_tables is not None
         b.set_shape(rpt, tpb, grid)
