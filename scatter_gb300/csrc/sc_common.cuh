@@ -116,9 +116,18 @@ struct ForceRows {
   const int64_t* ptr;
   const int* idx;
   const double* val;
-  __device__ int64_t find(int row, int i) const {
-    if (row < 0 || row >= n_t) return -1;
-    for (int64_t e = ptr[row]; e < ptr[row + 1]; ++e)
+};
+
+// rows r0 .. r0 + nr - 1 of a force table staged in shared memory (the cap reads them many times)
+constexpr int kCapStage = 2048;
+struct CapRows {
+  int r0, nr;
+  const int* ptr;  // nr + 1 offsets into idx / val
+  const int* idx;
+  const double* val;
+  __device__ int find(int row, int i) const {
+    if (row < r0 || row >= r0 + nr) return -1;
+    for (int e = ptr[row - r0]; e < ptr[row - r0 + 1]; ++e)
       if (idx[e] == i) return e;
     return -1;
   }
@@ -126,13 +135,13 @@ struct ForceRows {
 
 // max |f_{m+1} - sum_{k<=q} cf[k] f_{m-k}| / max |f| over those rows (0 when they hold no force),
 // in thread 0
-__device__ inline double cap_misfit(const ForceRows& F, int q, int m, const double* cf) {
+__device__ inline double cap_misfit(const CapRows& F, int q, int m, const double* cf) {
   __shared__ double mx[2][32];
   double rmx = 0.0, fmx = 0.0;
   for (int j = 0; j <= q + 1; ++j) {  // rows in the order m+1, m, m-1, ..., m-q
     const int row = m + 1 - j;
-    if (row < 0 || row >= F.n_t) continue;
-    for (int64_t e = F.ptr[row] + threadIdx.x; e < F.ptr[row + 1]; e += blockDim.x) {
+    if (row < F.r0 || row >= F.r0 + F.nr) continue;
+    for (int e = F.ptr[row - F.r0] + threadIdx.x; e < F.ptr[row - F.r0 + 1]; e += blockDim.x) {
       const int i = F.idx[e];
       fmx = fmax(fmx, fabs(F.val[e]));
       bool first = true;
@@ -140,7 +149,7 @@ __device__ inline double cap_misfit(const ForceRows& F, int q, int m, const doub
       if (!first) continue;
       double r = 0.0;
       for (int k = 0; k <= q + 1; ++k) {
-        const int64_t h = k == j ? e : F.find(m + 1 - k, i);
+        const int h = k == j ? e : F.find(m + 1 - k, i);
         if (h >= 0) r += (k == 0 ? 1.0 : -cf[k - 1]) * F.val[h];
       }
       rmx = fmax(rmx, fabs(r));
@@ -169,22 +178,39 @@ __device__ inline double cap_misfit(const ForceRows& F, int q, int m, const doub
 }
 
 // sets s->pcap for step s->t (counting in s->capped the steps it lowers); all threads of the
-// block call it
+// block call it.  The window's rows t-p .. t+1 are staged in shared memory first; a window of
+// more than kCapStage entries, or a row of more than kCapRow, keeps the order.
 template <class S>
 __device__ void warm_start_order_cap(S* s, int fixed, int enabled, const ForceRows& F) {
   __shared__ int cap_s;
+  __shared__ int s_ptr[kHistMax + 3];
+  __shared__ int s_idx[kCapStage];
+  __shared__ double s_val[kCapStage];
   const int t = s->t;
   const int p = warm_start_order(s, fixed);
   int cap = p;
+  const int r0 = t - p < 0 ? 0 : t - p, r1 = t + 1 < F.n_t - 1 ? t + 1 : F.n_t - 1;  // rows r0..r1
+  const int nr = r1 >= r0 ? r1 - r0 + 1 : 0;
   bool small = enabled && F.ptr && p > 0;
-  if (small)
-    for (int row = t - p; row <= t + 1; ++row)
-      if (row >= 0 && row < F.n_t && F.ptr[row + 1] - F.ptr[row] > kCapRow) small = false;
+  if (small && nr > 0) {
+    for (int row = r0; row <= r1; ++row)
+      if (F.ptr[row + 1] - F.ptr[row] > kCapRow) small = false;
+    if (small && F.ptr[r1 + 1] - F.ptr[r0] > kCapStage) small = false;
+  }
   if (small) {
+    const int64_t base = nr > 0 ? F.ptr[r0] : 0;
+    if (threadIdx.x <= nr) s_ptr[threadIdx.x] = nr > 0 ? (int)(F.ptr[r0 + threadIdx.x] - base) : 0;
+    const int n = nr > 0 ? (int)(F.ptr[r1 + 1] - base) : 0;
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+      s_idx[e] = F.idx[base + e];
+      s_val[e] = F.val[base + e];
+    }
+    __syncthreads();
+    const CapRows C{r0, nr, s_ptr, s_idx, s_val};
     double cf[kHistMax + 1];
     for (cap = p; cap > 0; --cap) {
       warm_start_coeffs(cap, cf);
-      const double e1 = cap_misfit(F, cap, t, cf);
+      const double e1 = cap_misfit(C, cap, t, cf);
       if (threadIdx.x == 0) cap_s = e1 <= kCapTol ? 1 : 0;
       __syncthreads();
       const int ok = cap_s;
