@@ -194,6 +194,8 @@ int sc_newmark_warm_start_status(sc_newmark* h, int* order, int64_t* capped_step
 /* synchronous: CG status of the run so far (SC_OK / SC_NOT_CONVERGED / SC_BREAKDOWN),
  * total and maximum CG iterations per step */
 int sc_newmark_status(sc_newmark* h, int64_t* total_iters, int* max_iters_per_step);
+/* asynchronous form, as sc_nb_status_to */
+int sc_newmark_status_to(sc_newmark* h, int64_t* dev3);
 /* Timing aid: launches the step loop's SpMV kernel (w = A p, with its p.w partials) `reps`
  * times on the solver's stream between CUDA events, outside any graph; returns the mean
  * device time per launch and the algorithmic bytes of one launch (12 B per stored entry +
@@ -296,6 +298,9 @@ int sc_nb_set_output(sc_nb_newmark* h, int out_interval, int n_rec, const int* r
 /* steps t_begin .. t_end-1 (asynchronous graph launches) */
 int sc_nb_run(sc_nb_newmark* h, int t_begin, int t_end);
 int sc_nb_status(sc_nb_newmark* h, int64_t* total_iters, int* max_iters_per_step, int* fsai_fallback_rows);
+/* asynchronous form: status, total iterations and the largest per-step count written to dev3
+ * (3 int64 in device memory) in stream order behind the queued steps; no synchronisation */
+int sc_nb_status_to(sc_nb_newmark* h, int64_t* dev3);
 /* timing aid: the step loop's block SpMV (w = A p) launched `reps` times between CUDA events */
 int sc_nb_time_spmv(sc_nb_newmark* h, int reps, float* ms_per_launch, int64_t* bytes_per_launch);
 /* the same with a32 = 1: the SpMV form that applies the FP32 matrix (A's hi planes) alone */

@@ -68,6 +68,8 @@ SIGNATURES = {
                          L, P]),
     "sc_nb_set_options": (I, [P, I]),
     "sc_nb_warm_start_status": (I, [P, ctypes.POINTER(I), ctypes.POINTER(L)]),
+    "sc_nb_status_to": (I, [P, P]),
+    "sc_newmark_status_to": (I, [P, P]),
     "sc_nb_a32_status": (I, [P, ctypes.POINTER(L), ctypes.POINTER(L), ctypes.POINTER(L),
                              ctypes.POINTER(ctypes.c_double)]),
     "sc_nb_residual_fp64": (I, [P, ctypes.POINTER(I)]),

@@ -1689,6 +1689,20 @@ extern "C" int sc_nb_status(sc_nb_newmark* h, int64_t* total_iters, int* max_ite
   return s.status;
 }
 
+__global__ void k_status3(const Scal* s, int64_t* out) {
+  out[0] = s->status;
+  out[1] = s->total_iters;
+  out[2] = s->max_seen;
+}
+
+// the run's status, total iterations and largest per-step count into dev3 (device, 3 int64),
+// queued on the solver's stream behind its steps: no synchronisation
+extern "C" int sc_nb_status_to(sc_nb_newmark* h, int64_t* dev3) {
+  if (!h || !dev3) return SC_BAD_ARG;
+  k_status3<<<1, 1, 0, h->user>>>(h->g.s, dev3);
+  return check_launch("status copy");
+}
+
 extern "C" int sc_nb_a32_status(sc_nb_newmark* h, int64_t* a32_steps, int64_t* switched, int64_t* restarts,
                                 double* lo_norm) {
   if (!h) return SC_BAD_ARG;

@@ -202,6 +202,10 @@ class NewmarkGPU:
         rc = nat.value("sc_newmark_status", self.h, ctypes.byref(tot), ctypes.byref(mx))
         return rc, tot.value, mx.value
 
+    def status_to(self, dev3):
+        """Queue (status, total iterations, largest per-step count) into dev3 (device int64[3])."""
+        nat.call("sc_newmark_status_to", self.h, dev3.data_ptr())
+
     def outputs(self):
         return {k: (None if t is None else dv.host(t).reshape(self.n_out, self.n_rec)) for k, t in self.out.items()}
 
@@ -382,6 +386,10 @@ class NodeBlockNewmark:
         self.fsai_fallback_rows = fb.value
         return rc, tot.value, mx.value
 
+    def status_to(self, dev3):
+        """Queue (status, total iterations, largest per-step count) into dev3 (device int64[3])."""
+        nat.call("sc_nb_status_to", self.h, dev3.data_ptr())
+
     def time_spmv(self, reps=20, a32=False):
         """ms per launch and algorithmic bytes per launch of the PCG SpMV; a32: the form that
         applies the FP32 matrix (A's hi planes) alone."""
@@ -453,7 +461,13 @@ class NewmarkExplicit:
     the run on the device, and fills rows t_start .. t_end of the outputs.  With
     ``stream_force = True`` each call copies the force values of its own steps host ->
     device (pinned memory) instead of the whole history at set-up.  ``close()`` frees the
-    device solver."""
+    device solver.
+
+    A continuing call returns once its steps, the device -> host copies of their outputs and
+    of the run's status are queued: the outputs (u, v, a, or u_rec, v_rec, a_rec with
+    receivers) and ``iterations`` are settled when they are read or at the next call, which
+    queues its own steps first, so the GPU runs one call's steps while the host handles the
+    previous call's results.  A failed step raises at that point."""
 
     def __init__(self, rtol=1e-12, max_iter=1000, layout="node-block", spmv="pair", residual="pair",
                  fp32_matrix="auto"):
@@ -469,9 +483,11 @@ class NewmarkExplicit:
         self.receivers = None  # optional equation subset for the outputs (default: all)
         self.force_table = None  # optional ForceTable (skips sampling the callback)
         self.stream_force = False
-        self.iterations = None
+        self._iterations = None
         self.preconditioner = None
         self._live = None  # (key, device solver, last step reached)
+        self._pending = None  # queued outputs and status of the last continuing call
+        self._rec = {}
 
     def initialise(self, number_equations, time):
         self.close()
@@ -485,6 +501,7 @@ class NewmarkExplicit:
         self._hist_shape = (n_out, self.number_equations)
 
     def _history(self, key):
+        self._settle()
         if key not in self._hist:
             self._hist[key] = np.zeros(self._hist_shape)  # zero pages, committed as written
         return self._hist[key]
@@ -492,6 +509,20 @@ class NewmarkExplicit:
     u = property(lambda self: self._history("u"), lambda self, x: self._hist.__setitem__("u", x))
     v = property(lambda self: self._history("v"), lambda self, x: self._hist.__setitem__("v", x))
     a = property(lambda self: self._history("a"), lambda self, x: self._hist.__setitem__("a", x))
+
+    def _receiver(self, key):
+        self._settle()
+        return self._rec.get(key)
+
+    u_rec = property(lambda self: self._receiver("u"))
+    v_rec = property(lambda self: self._receiver("v"))
+    a_rec = property(lambda self: self._receiver("a"))
+
+    @property
+    def iterations(self):
+        """(total PCG iterations of the run, largest per step)."""
+        self._settle()
+        return self._iterations
 
     def update(self, t_idx):
         self.t_idx = t_idx
@@ -563,39 +594,90 @@ class NewmarkExplicit:
             solver = live[1]
             solver.push_force(t_start_idx, t_end_idx)
             solver.run(t_start_idx, t_end_idx)
-            rc, tot, mx = solver.status()
-            rows = (t_start_idx, t_end_idx)
-        else:
-            self.close()
-            mats = (g.pattern, g.M_d, g.C_d, g.K_d) if g is not None else _device_matrices(M, C, K)
-            solver, rc, tot, mx, rows = self._start(g, mats, F, t_start_idx, t_end_idx)
-            key = key[:2] + (id(self.force_table),) + key[3:]
+            # the matrices stay referenced while the run is live, so their ids stay theirs
+            self._live = (key, solver, t_end_idx, (M, C, K))
+            # the previous call's results, while this call's steps run behind them
+            self._settle()
+            self._queue(solver, (t_start_idx, t_end_idx))
+            return
+        self.close()
+        mats = (g.pattern, g.M_d, g.C_d, g.K_d) if g is not None else _device_matrices(M, C, K)
+        solver, rc, tot, mx, rows = self._start(g, mats, F, t_start_idx, t_end_idx)
+        key = key[:2] + (id(self.force_table),) + key[3:]
         if rc != 0:
             solver.close()
-            self._live = None
             raise nat.ScatterGpuError("time loop", rc, nat.load().sc_status_string(rc).decode(), "")
-        # the matrices stay referenced while the run is live, so their ids stay theirs
         self._live = (key, solver, t_end_idx, (M, C, K))
-        self.iterations = (tot, mx)
+        self._iterations = (tot, mx)
         self._copy_outputs(solver, rows)
+
+    def _out_rows(self, solver, rows):
+        k = self.output_interval
+        return -(-rows[0] // k), min(rows[1] // k, solver.n_out - 1)
+
+    def _dst(self, solver):
+        """The host arrays the outputs go to."""
+        if self.receivers is None:
+            return {"u": self._history("u"), "v": self._history("v"), "a": self._history("a")}
+        nr = solver.n_rec
+        if self._rec.get("u") is None or self._rec["u"].shape != (solver.n_out, nr):
+            self._rec = {name: np.zeros((solver.n_out, nr)) for name in ("u", "v", "a")}
+        return self._rec
 
     def _copy_outputs(self, solver, rows):
         """Output rows of steps rows[0] .. rows[1] from the device into the host arrays."""
-        k = self.output_interval
-        r0 = -(-rows[0] // k)
-        r1 = min(rows[1] // k, solver.n_out - 1)
+        r0, r1 = self._out_rows(solver, rows)
         if r1 < r0:
             return
-        nr = solver.n_rec
-        if self.receivers is None:
-            dst = {"u": self.u, "v": self.v, "a": self.a}
-        else:
-            if getattr(self, "u_rec", None) is None or self.u_rec.shape != (solver.n_out, nr):
-                self.u_rec, self.v_rec, self.a_rec = (np.zeros((solver.n_out, nr)) for _ in range(3))
-            dst = {"u": self.u_rec, "v": self.v_rec, "a": self.a_rec}
+        dst = self._dst(solver)
         for name, rows_h in solver.output_rows(r0, r1).items():
             if rows_h is not None:
                 dst[name][r0:r1 + 1] = rows_h
+
+    def _queue(self, solver, rows):
+        """Queue the device -> host copies of the outputs of steps rows[0] .. rows[1] and of the
+        run's status into pinned buffers, and an event after them (no synchronisation)."""
+        r0, r1 = self._out_rows(solver, rows)
+        if getattr(self, "_st_dev", None) is None or self._st_dev.device != solver.u.device:
+            self._st_dev = torch.zeros(3, dtype=torch.int64, device=solver.u.device)
+            self._st_host = torch.zeros(3, dtype=torch.int64).pin_memory()
+            self._stage = {}
+        solver.status_to(self._st_dev)
+        self._st_host.copy_(self._st_dev, non_blocking=True)
+        staged = {}
+        if r1 >= r0:
+            nr = solver.n_rec
+            n = (r1 - r0 + 1) * nr
+            for name, t in solver.out.items():
+                if t is None:
+                    continue
+                buf = self._stage.get(name)
+                if buf is None or buf.numel() < n:
+                    buf = self._stage[name] = torch.empty(n, dtype=torch.float64).pin_memory()
+                buf[:n].copy_(t[r0 * nr:(r1 + 1) * nr], non_blocking=True)
+                staged[name] = buf[:n]
+        ev = torch.cuda.Event()
+        ev.record()
+        self._pending = (solver, r0, r1, staged, ev)
+
+    def _settle(self, raise_errors=True):
+        """Wait for the queued copies of the last continuing call and deliver them."""
+        p = getattr(self, "_pending", None)
+        if p is None:
+            return
+        self._pending = None
+        solver, r0, r1, staged, ev = p
+        ev.synchronize()
+        rc, tot, mx = (int(x) for x in self._st_host.tolist())
+        if staged:
+            dst = self._dst(solver)
+            nr = solver.n_rec
+            for name, buf in staged.items():
+                dst[name][r0:r1 + 1] = buf.numpy().reshape(-1, nr)
+        self._iterations = (tot, mx)
+        if rc != 0 and raise_errors:
+            self.close()
+            raise nat.ScatterGpuError("time loop", rc, nat.load().sc_status_string(rc).decode(), "")
 
     @property
     def device_solver(self):
@@ -603,6 +685,7 @@ class NewmarkExplicit:
         return None if self._live is None else self._live[1]
 
     def close(self):
+        self._settle(raise_errors=False)
         if getattr(self, "_live", None) is not None:
             self._live[1].close()
             self._live = None
