@@ -147,3 +147,31 @@ def test_nonzero_initial_state(torch_cuda, layout):
     assert rel_l2(s.u, U) <= 1e-10
     assert rel_l2(s.v, V) <= 1e-10
     s.close()
+
+
+def test_continuing_call_reports_a_failure_when_settled(torch_cuda):
+    """A continuing call queues its results and returns: a step that fails (here: the PCG
+    iteration limit) raises ScatterGpuError when the outputs are read, and the solver is closed."""
+    from scatter_gb300 import _native as nat
+    from scatter_gb300.solvers import ForceTable, NewmarkExplicit
+
+    g, m, time, F, top_eq = _column_system()
+    n_t = 40
+    t = F.table
+    # no load before step 10: those steps converge at once from rest; the load then needs
+    # more than the 2 iterations allowed
+    first = int(t.f_ptr[10])
+    ptr = np.concatenate([np.zeros(10, dtype=np.int64), t.f_ptr[10:n_t + 1] - first])
+    table = ForceTable(ptr, t.f_eq[first:t.f_ptr[n_t]], t.f_val[first:t.f_ptr[n_t]], m.number_eq)
+    s = NewmarkExplicit(max_iter=2)
+    s.output_interval = 1
+    s.initialise(m.number_eq, time[:n_t])
+    s.force_table = table
+    s.receivers = top_eq
+    s.update(0)
+    s.calculate(g, g, g, None, 0, 5)
+    assert np.abs(s.u_rec[:6]).max() == 0.0
+    s.calculate(g, g, g, None, 5, 15)  # queued: no error yet
+    with pytest.raises(nat.ScatterGpuError):
+        s.v_rec
+    assert s.device_solver is None
