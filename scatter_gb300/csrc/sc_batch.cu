@@ -74,6 +74,27 @@ __device__ __forceinline__ void ldf(const float* p, float (&v)[RPT]) {
     for (int q = 0; q < RPT; ++q) v[q] = __ldg(p + q);
   }
 }
+// ldf with the L1 eviction priority "last": the neighbours' w, read by up to 27 nodes' threads
+template <int RPT>
+__device__ __forceinline__ void ldf_keep(const float* p, float (&v)[RPT]) {
+  if constexpr (RPT % 4 == 0) {
+#pragma unroll
+    for (int q = 0; q < RPT / 4; ++q) {
+      float4 a;
+      asm("ld.global.nc.L1::evict_last.v4.f32 {%0, %1, %2, %3}, [%4];"
+          : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w)
+          : "l"(reinterpret_cast<const float4*>(p) + q));
+      v[4 * q] = a.x; v[4 * q + 1] = a.y; v[4 * q + 2] = a.z; v[4 * q + 3] = a.w;
+    }
+  } else if constexpr (RPT == 2) {
+    float2 a;
+    asm("ld.global.nc.L1::evict_last.v2.f32 {%0, %1}, [%2];" : "=f"(a.x), "=f"(a.y) : "l"(p));
+    v[0] = a.x; v[1] = a.y;
+  } else {
+    ldf<RPT>(p, v);
+  }
+}
+
 template <int RPT>
 __device__ __forceinline__ void stf(float* p, const float (&v)[RPT]) {
   if constexpr (RPT % 4 == 0) {
@@ -446,9 +467,9 @@ __global__ void __launch_bounds__(256) k_batch_step_hex8c(Args g, const __grid_c
       for (int lb = 0; lb < 8; ++lb) {
         const int64_t bs = (int64_t)__ldg(en + lb) * 3;
         float w0[RPT], w1[RPT], w2[RPT];
-        ldf<RPT>(w_in + (bs + 0) * R + r0, w0);
-        ldf<RPT>(w_in + (bs + 1) * R + r0, w1);
-        ldf<RPT>(w_in + (bs + 2) * R + r0, w2);
+        ldf_keep<RPT>(w_in + (bs + 0) * R + r0, w0);
+        ldf_keep<RPT>(w_in + (bs + 1) * R + r0, w1);
+        ldf_keep<RPT>(w_in + (bs + 2) * R + r0, w2);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const float* kr = k1.k + (3 * la + c) * 24 + 3 * lb;
