@@ -571,9 +571,10 @@ __global__ void __launch_bounds__(kThreads) k_spmv(Args g, cudaGraphConditionalH
 // in the block loop; same bytes as the FP64 kernel (A: 2 x 4 B per value, p: 8 B pairs).
 // With a32 it reads the hi parts alone (a copy, 4 B per value): w = Ah p, the FP32 matrix Ah
 // applied to p in the same pair arithmetic (to ~2^-46 for Ah itself).
-template <int D>
+template <int D, int kKeep>  // kKeep: the planes' load policy (g.keep_l2) fixed at compile time, or -1
 __device__ __forceinline__ void spmv_chunk(const Args& g, int64_t pos, const int (&cl)[4], bool a32, float (&hi)[D],
                                            float (&lo)[D]) {
+  const int keep = kKeep >= 0 ? kKeep : g.keep_l2;
   float2 pv[4][D];
 #pragma unroll
   for (int e = 0; e < 4; ++e)
@@ -586,12 +587,12 @@ __device__ __forceinline__ void spmv_chunk(const Args& g, int64_t pos, const int
       const int64_t off = (int64_t)(c * D + d) * g.sf_n + pos;
       if (a32) {
         float ah[4];
-        ld4(g.AHS + off, ah, g.keep_l2);
+        ld4(g.AHS + off, ah, keep);
 #pragma unroll
         for (int e = 0; e < 4; ++e) pair_fma(ah[e], 0.f, pv[e][d], hi[c], lo[c]);
       } else {
         float2 a4[4];
-        ld4(g.APS + off, a4, g.keep_l2);
+        ld4(g.APS + off, a4, keep);
 #pragma unroll
         for (int e = 0; e < 4; ++e) pair_fma(a4[e].x, a4[e].y, pv[e][d], hi[c], lo[c]);
       }
@@ -601,10 +602,11 @@ __device__ __forceinline__ void spmv_chunk(const Args& g, int64_t pos, const int
 // the SpMV's rows: pair planes one chunk at a time (kA32 = false), or the hi planes alone two
 // chunks at a time (half the bytes per chunk, so twice the loads in flight); then p.w and alpha
 constexpr bool kA32TwoChunks = true;
-template <int D, int kMode, bool kA32>
+template <int D, int kMode, bool kA32, int kKeep>
 __device__ __forceinline__ void spmv_rows(const Args& g, cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
   double ppw = 0.0;
+  const int keep = kKeep >= 0 ? kKeep : g.keep_l2;
   SELL_ROW_LOOP(g.sf_ptr) {
     SELL_ROW_BEGIN(g.sf_ptr)
     float hi[D], lo[D];
@@ -615,21 +617,21 @@ __device__ __forceinline__ void spmv_rows(const Args& g, cudaGraphConditionalHan
       for (; q + 1 < nq; q += 2) {
         const int64_t pos = p0 + 128 * q;
         int c0[4], c1[4];
-        cols4(g.sf_col, pos, c0, g.keep_l2);
-        cols4(g.sf_col, pos + 128, c1, g.keep_l2);
-        spmv_chunk<D>(g, pos, c0, true, hi, lo);
-        spmv_chunk<D>(g, pos + 128, c1, true, hi, lo);
+        cols4(g.sf_col, pos, c0, keep);
+        cols4(g.sf_col, pos + 128, c1, keep);
+        spmv_chunk<D, kKeep>(g, pos, c0, true, hi, lo);
+        spmv_chunk<D, kKeep>(g, pos + 128, c1, true, hi, lo);
       }
       if (q < nq) {
         int c0[4];
-        cols4(g.sf_col, p0 + 128 * q, c0, g.keep_l2);
-        spmv_chunk<D>(g, p0 + 128 * q, c0, true, hi, lo);
+        cols4(g.sf_col, p0 + 128 * q, c0, keep);
+        spmv_chunk<D, kKeep>(g, p0 + 128 * q, c0, true, hi, lo);
       }
     } else {
       for (int64_t q = 0; q < nq; ++q) {
         int c0[4];
-        cols4(g.sf_col, p0 + 128 * q, c0, g.keep_l2);
-        spmv_chunk<D>(g, p0 + 128 * q, c0, kA32, hi, lo);
+        cols4(g.sf_col, p0 + 128 * q, c0, keep);
+        spmv_chunk<D, kKeep>(g, p0 + 128 * q, c0, kA32, hi, lo);
       }
     }
     if (row < g.n_nodes) {
@@ -670,13 +672,20 @@ __device__ __forceinline__ void spmv_rows(const Args& g, cudaGraphConditionalHan
 template <int D, int kMode>
 __global__ void __launch_bounds__(kThreads) k_spmv_pair(Args g, cudaGraphConditionalHandle hc) {
   if (kMode != 2 && g.s->a32) return;
-  spmv_rows<D, kMode, false>(g, hc);
+  spmv_rows<D, kMode, false, -1>(g, hc);
+}
+
+// kKeep = g.keep_l2, fixed at compile time (the launch picks the instance)
+template <int D, int kMode, int kKeep>
+__global__ void __launch_bounds__(kThreads, 3) k_spmv_a32(Args g, cudaGraphConditionalHandle hc) {
+  if (kMode != 2 && !g.s->a32) return;
+  spmv_rows<D, kMode, true, kKeep>(g, hc);
 }
 
 template <int D, int kMode>
-__global__ void __launch_bounds__(kThreads, 3) k_spmv_a32(Args g, cudaGraphConditionalHandle hc) {
-  if (kMode != 2 && !g.s->a32) return;
-  spmv_rows<D, kMode, true>(g, hc);
+static void launch_spmv_a32(const Args& g, unsigned blocks, cudaStream_t st, cudaGraphConditionalHandle hc) {
+  if (g.keep_l2) k_spmv_a32<D, kMode, 1><<<blocks, kThreads, 0, st>>>(g, hc);
+  else k_spmv_a32<D, kMode, 0><<<blocks, kThreads, 0, st>>>(g, hc);
 }
 
 // x += alpha p ; r -= alpha w ; partial r.r and |x - x0|^2 ; last block: convergence test.
@@ -1163,7 +1172,7 @@ int build_graph(sc_nb_newmark* h) {
       break;
     if (g.spmv_pair) {
       k_spmv_pair<D, 0><<<nbk, kThreads, 0, c2>>>(g, hc);
-      k_spmv_a32<D, 0><<<nbk, kThreads, 0, c2>>>(g, hc);
+      launch_spmv_a32<D, 0>(g, nbk, c2, hc);
     }
     else k_spmv<D, 0><<<nbk, kThreads, 0, c2>>>(g, hc);
     k_update<0><<<vbk, 256, 0, c2>>>(g, hc);
@@ -1598,7 +1607,7 @@ static int eager_step(sc_nb_newmark* h) {
     if (done) break;
     if (g.spmv_pair) {
       k_spmv_pair<D, 1><<<nbk, kThreads, 0, st>>>(g, none);
-      k_spmv_a32<D, 1><<<nbk, kThreads, 0, st>>>(g, none);
+      launch_spmv_a32<D, 1>(g, nbk, st, none);
     }
     else k_spmv<D, 1><<<nbk, kThreads, 0, st>>>(g, none);
     k_update<1><<<vbk, 256, 0, st>>>(g, none);
@@ -1749,8 +1758,8 @@ extern "C" int sc_nb_time_spmv_a32(sc_nb_newmark* h, int a32, int reps, float* m
   auto launch = [&]() {
     if (h->g.spmv_pair) {
       if (a32) {
-        if (h->g.D == 3) k_spmv_a32<3, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
-        else k_spmv_a32<2, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
+        if (h->g.D == 3) launch_spmv_a32<3, 2>(h->g, nbk, st, none);
+        else launch_spmv_a32<2, 2>(h->g, nbk, st, none);
       } else {
         if (h->g.D == 3) k_spmv_pair<3, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
         else k_spmv_pair<2, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
