@@ -388,7 +388,7 @@ __device__ __forceinline__ void fsai_row(const __half* planes, int64_t plane_n, 
 }
 
 // t = G r  (lower pattern, FP16 factor planes, FP32 products and result)
-template <int D>
+template <int D, int kKeep>  // kKeep = g.keep_l2 at compile time
 __global__ void __launch_bounds__(kThreads, 4) k_prec_lower(Args g) {
   const float* rv = g.s->restart ? g.r032 : g.r32;  // a restart preconditions r0
   SELL_ROW_LOOP(g.sl_ptr) {
@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_prec_lower(Args g) {
     float s[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) s[c] = 0.f;
-    fsai_row<D>(g.GS, g.sl_n, g.sl_col, rv, p0, nq, g.keep_l2, s);
+    fsai_row<D>(g.GS, g.sl_n, g.sl_col, rv, p0, nq, kKeep, s);
     if (row < g.n_nodes) {
 #pragma unroll
       for (int c = 0; c < D; ++c) g.t32[row * D + c] = s[c];
@@ -408,7 +408,7 @@ constexpr double kA32Margin = 16.0;
 
 // z = G^T t ; partial r.z ; mode 0 (inside PCG): last block computes beta, rz;
 // mode 1 (after the residual): p = z, rz, rr and the conditional from |r| vs |b|.
-template <int D, int kMode>
+template <int D, int kMode, int kKeep>  // kKeep = g.keep_l2 at compile time
 __global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
   double prz = 0.0, prr = 0.0;
@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cu
     float s[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) s[c] = 0.f;
-    fsai_row<D>(g.GTS, g.su_n, g.su_col, g.t32, p0, nq, g.keep_l2, s);
+    fsai_row<D>(g.GTS, g.su_n, g.su_col, g.t32, p0, nq, kKeep, s);
     if (row < g.n_nodes) {
 #pragma unroll
       for (int c = 0; c < D; ++c) {
@@ -669,10 +669,10 @@ __device__ __forceinline__ void spmv_rows(const Args& g, cudaGraphConditionalHan
 // (kMode 2, the timing launch, always runs).  Separate kernels keep the pair form at 64 registers;
 // the FP32-matrix form is held to 80 (three blocks per SM: 0.140 ms at the 1.79 M-equation box
 // against 0.203 ms at its natural 105 registers and 0.210 ms one chunk at a time).
-template <int D, int kMode>
-__global__ void __launch_bounds__(kThreads) k_spmv_pair(Args g, cudaGraphConditionalHandle hc) {
+template <int D, int kMode, int kKeep>
+__global__ void __launch_bounds__(kThreads, 4) k_spmv_pair(Args g, cudaGraphConditionalHandle hc) {
   if (kMode != 2 && g.s->a32) return;
-  spmv_rows<D, kMode, false, -1>(g, hc);
+  spmv_rows<D, kMode, false, kKeep>(g, hc);
 }
 
 // kKeep = g.keep_l2, fixed at compile time (the launch picks the instance)
@@ -686,6 +686,22 @@ template <int D, int kMode>
 static void launch_spmv_a32(const Args& g, unsigned blocks, cudaStream_t st, cudaGraphConditionalHandle hc) {
   if (g.keep_l2) k_spmv_a32<D, kMode, 1><<<blocks, kThreads, 0, st>>>(g, hc);
   else k_spmv_a32<D, kMode, 0><<<blocks, kThreads, 0, st>>>(g, hc);
+}
+template <int D, int kMode>
+static void launch_spmv_pair(const Args& g, unsigned blocks, cudaStream_t st, cudaGraphConditionalHandle hc) {
+  if (g.keep_l2) k_spmv_pair<D, kMode, 1><<<blocks, kThreads, 0, st>>>(g, hc);
+  else k_spmv_pair<D, kMode, 0><<<blocks, kThreads, 0, st>>>(g, hc);
+}
+template <int D>
+static void launch_prec_lower(const Args& g, unsigned blocks, cudaStream_t st) {
+  if (g.keep_l2) k_prec_lower<D, 1><<<blocks, kThreads, 0, st>>>(g);
+  else k_prec_lower<D, 0><<<blocks, kThreads, 0, st>>>(g);
+}
+template <int D, int kMode>
+static void launch_prec_upper(const Args& g, unsigned blocks, cudaStream_t st, int mode,
+                              cudaGraphConditionalHandle hc) {
+  if (g.keep_l2) k_prec_upper<D, kMode, 1><<<blocks, kThreads, 0, st>>>(g, mode, hc);
+  else k_prec_upper<D, kMode, 0><<<blocks, kThreads, 0, st>>>(g, mode, hc);
 }
 
 // x += alpha p ; r -= alpha w ; partial r.r and |x - x0|^2 ; last block: convergence test.
@@ -1149,8 +1165,8 @@ int build_graph(sc_nb_newmark* h) {
     } else {
       k_residual<D, false><<<nbk, kThreads, 0, cs>>>(g, 0);
     }
-    k_prec_lower<D><<<nbk, kThreads, 0, cs>>>(g);
-    k_prec_upper<D, 0><<<nbk, kThreads, 0, cs>>>(g, 1, hc);
+    launch_prec_lower<D>(g, nbk, cs);
+    launch_prec_upper<D, 0>(g, nbk, cs, 1, hc);
     cudaStreamCaptureStatus stt;
     const cudaGraphNode_t* deps = nullptr;
     size_t ndeps = 0;
@@ -1171,13 +1187,13 @@ int build_graph(sc_nb_newmark* h) {
                     "capture body")))
       break;
     if (g.spmv_pair) {
-      k_spmv_pair<D, 0><<<nbk, kThreads, 0, c2>>>(g, hc);
+      launch_spmv_pair<D, 0>(g, nbk, c2, hc);
       launch_spmv_a32<D, 0>(g, nbk, c2, hc);
     }
     else k_spmv<D, 0><<<nbk, kThreads, 0, c2>>>(g, hc);
     k_update<0><<<vbk, 256, 0, c2>>>(g, hc);
-    k_prec_lower<D><<<nbk, kThreads, 0, c2>>>(g);
-    k_prec_upper<D, 0><<<nbk, kThreads, 0, c2>>>(g, 0, hc);
+    launch_prec_lower<D>(g, nbk, c2);
+    launch_prec_upper<D, 0>(g, nbk, c2, 0, hc);
     k_direction<<<vbk, 256, 0, c2>>>(g);
     cudaGraph_t bo;
     if ((rc = check(cudaStreamEndCapture(c2, &bo), "end body"))) break;
@@ -1596,8 +1612,8 @@ static int eager_step(sc_nb_newmark* h) {
   } else {
     k_residual<D, false><<<nbk, kThreads, 0, st>>>(g, 0);
   }
-  k_prec_lower<D><<<nbk, kThreads, 0, st>>>(g);
-  k_prec_upper<D, 1><<<nbk, kThreads, 0, st>>>(g, 1, none);
+  launch_prec_lower<D>(g, nbk, st);
+  launch_prec_upper<D, 1>(g, nbk, st, 1, none);
   int done = 0;
   int rc;
   for (int guard = 0; guard < 100000; ++guard) {
@@ -1606,13 +1622,13 @@ static int eager_step(sc_nb_newmark* h) {
     if ((rc = check(cudaStreamSynchronize(st), "sync eager"))) return rc;
     if (done) break;
     if (g.spmv_pair) {
-      k_spmv_pair<D, 1><<<nbk, kThreads, 0, st>>>(g, none);
+      launch_spmv_pair<D, 1>(g, nbk, st, none);
       launch_spmv_a32<D, 1>(g, nbk, st, none);
     }
     else k_spmv<D, 1><<<nbk, kThreads, 0, st>>>(g, none);
     k_update<1><<<vbk, 256, 0, st>>>(g, none);
-    k_prec_lower<D><<<nbk, kThreads, 0, st>>>(g);
-    k_prec_upper<D, 1><<<nbk, kThreads, 0, st>>>(g, 0, none);
+    launch_prec_lower<D>(g, nbk, st);
+    launch_prec_upper<D, 1>(g, nbk, st, 0, none);
     k_direction<<<vbk, 256, 0, st>>>(g);
   }
   k_finalize<<<vbk, 256, 0, st>>>(g);
@@ -1761,8 +1777,8 @@ extern "C" int sc_nb_time_spmv_a32(sc_nb_newmark* h, int a32, int reps, float* m
         if (h->g.D == 3) launch_spmv_a32<3, 2>(h->g, nbk, st, none);
         else launch_spmv_a32<2, 2>(h->g, nbk, st, none);
       } else {
-        if (h->g.D == 3) k_spmv_pair<3, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
-        else k_spmv_pair<2, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
+        if (h->g.D == 3) launch_spmv_pair<3, 2>(h->g, nbk, st, none);
+        else launch_spmv_pair<2, 2>(h->g, nbk, st, none);
       }
     } else {
       if (h->g.D == 3) k_spmv<3, 2><<<nbk, kThreads, 0, st>>>(h->g, none);
@@ -1849,10 +1865,10 @@ extern "C" int sc_nb_apply(sc_nb_newmark* h, int which, const double* x, double*
       // r <- x, t = G r, z = G^T t (the solver's own kernels), y <- z
       k_copy_r<<<grid_for(g.n_s, 256), 256, 0, st>>>(g.n_s, g.D, x, g.r, g.r32);
       if (g.D == 3) {
-        k_prec_lower<3><<<h->node_blocks, kThreads, 0, st>>>(g);
+        launch_prec_lower<3>(g, h->node_blocks, st);
         k_prec_upper_nograph<3><<<h->node_blocks, kThreads, 0, st>>>(g);
       } else {
-        k_prec_lower<2><<<h->node_blocks, kThreads, 0, st>>>(g);
+        launch_prec_lower<2>(g, h->node_blocks, st);
         k_prec_upper_nograph<2><<<h->node_blocks, kThreads, 0, st>>>(g);
       }
       k_copy<<<grid_for(g.n_s, 256), 256, 0, st>>>(g.n_s, g.z, y);
