@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(kThreads) k_residual(Args g, int gate) {
 // good to about kResRatio 2^-48 of |b|).  gate: returns at once when res_fp64 is set.
 constexpr double kResRatio = 30.0;
 
-template <int D>
+template <int D, int kKeep>  // kKeep = g.keep_l2 at compile time
 __global__ void __launch_bounds__(kThreads) k_residual_kp(Args g) {
   if (g.s->res_fp64) return;
   __shared__ double sh[32];
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(kThreads) k_residual_kp(Args g) {
     for (int c = 0; c < D; ++c) rh[c] = rl[c] = bq[c] = 0.f;
     for (int64_t q = 0; q < nq; ++q) {
       int cl[4];
-      cols4(g.sf_col, p0 + 128 * q, cl, g.keep_l2);
+      cols4(g.sf_col, p0 + 128 * q, cl, kKeep);
 #pragma unroll
       for (int hh = 0; hh < 2; ++hh) {  // two entries at a time (registers)
         const int64_t pos = p0 + 128 * q + 2 * hh;
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(kThreads) k_residual_kp(Args g) {
           ldrec<kRecM, 3 * D>(rp[0], mv[0]);
           ldrec<kRecM, 3 * D>(rp[1], mv[1]);
           float2 m2[2];
-          ld2(g.MSP + pos, m2, g.keep_l2);
+          ld2(g.MSP + pos, m2, kKeep);
 #pragma unroll
           for (int c = 0; c < D; ++c) {
             pair_fma(m2[0].x, m2[0].y, make_float2(mv[0][2 * c], mv[0][2 * c + 1]), rh[c], rl[c]);
@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(kThreads) k_residual_kp(Args g) {
 #pragma unroll
           for (int d = 0; d < D; ++d) {
             float2 k2[2];
-            ld2(g.KPS + (int64_t)(c * D + d) * g.sf_n + pos, k2, g.keep_l2);
+            ld2(g.KPS + (int64_t)(c * D + d) * g.sf_n + pos, k2, kKeep);
             pair_fma(k2[0].x, k2[0].y, make_float2(kv[0][2 * d], kv[0][2 * d + 1]), rh[c], rl[c]);
             pair_fma(k2[1].x, k2[1].y, make_float2(kv[1][2 * d], kv[1][2 * d + 1]), rh[c], rl[c]);
             bq[c] = fmaf(k2[1].x, kv[1][2 * D + d], fmaf(k2[0].x, kv[0][2 * D + d], bq[c]));
@@ -1158,7 +1158,8 @@ int build_graph(sc_nb_newmark* h) {
     k_force<<<1, 256, 0, cs>>>(g);
     k_predict<D><<<h->pred_blocks, D * kPredNodes, 0, cs>>>(g);
     if (g.res_pair) {
-      k_residual_kp<D><<<nbk, kThreads, 0, cs>>>(g);
+      if (g.keep_l2) k_residual_kp<D, 1><<<nbk, kThreads, 0, cs>>>(g);
+      else k_residual_kp<D, 0><<<nbk, kThreads, 0, cs>>>(g);
       k_residual<D, true><<<nbk, kThreads, 0, cs>>>(g, 1);
     } else if (g.spmv_pair) {
       k_residual<D, true><<<nbk, kThreads, 0, cs>>>(g, 0);
@@ -1605,7 +1606,8 @@ static int eager_step(sc_nb_newmark* h) {
   k_force<<<1, 256, 0, st>>>(g);
   k_predict<D><<<h->pred_blocks, D * kPredNodes, 0, st>>>(g);
   if (g.res_pair) {
-    k_residual_kp<D><<<nbk, kThreads, 0, st>>>(g);
+    if (g.keep_l2) k_residual_kp<D, 1><<<nbk, kThreads, 0, st>>>(g);
+    else k_residual_kp<D, 0><<<nbk, kThreads, 0, st>>>(g);
     k_residual<D, true><<<nbk, kThreads, 0, st>>>(g, 1);
   } else if (g.spmv_pair) {
     k_residual<D, true><<<nbk, kThreads, 0, st>>>(g, 0);
