@@ -79,7 +79,7 @@ __device__ __forceinline__ float pick(const float (&a)[D], int c) {
   return D == 2 ? (c == 0 ? a[0] : a[1]) : (c == 0 ? a[0] : (c == 1 ? a[1] : a[2]));
 }
 
-template <int D, int TPR>
+template <int D, int TPR, int kKeep>  // kKeep = g.keep_l2 at compile time
 __global__ void __launch_bounds__(kThreads) k_explicit_pair(Args g, PairStep p, const int* __restrict__ rec_map,
                                                             SegStore st) {
   const int step = g.s->t + 1;
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(kThreads) k_explicit_pair(Args g, PairStep p, 
     for (int64_t q = sub; q < nq; q += TPR) {
       const int64_t pos = p0 + 128 * q;
       int cl[4];
-      cols4(g.sf_col, pos, cl, g.keep_l2);
+      cols4(g.sf_col, pos, cl, kKeep);
       float2 wa[4][D];
 #pragma unroll
       for (int e = 0; e < 4; ++e)
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(kThreads) k_explicit_pair(Args g, PairStep p, 
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           float2 k4[4];
-          ld4(g.KPS + (int64_t)(c * D + d) * g.sf_n + pos, k4, g.keep_l2);
+          ld4(g.KPS + (int64_t)(c * D + d) * g.sf_n + pos, k4, kKeep);
 #pragma unroll
           for (int e = 0; e < 4; ++e) pair_fma(k4[e].x, k4[e].y, wa[e][d], hi[c], lo[c]);
         }
@@ -351,7 +351,10 @@ PairStep pair_step(const sc_nb_newmark* h, int k) {
 
 template <int D, int TPR>
 void launch_pair_t(const sc_nb_newmark* h, cudaStream_t st, int k, SegStore store) {
-  k_explicit_pair<D, TPR><<<h->tpr_blocks, kThreads, 0, st>>>(h->g, pair_step(h, k), h->rec_map, store);
+  if (h->g.keep_l2)
+    k_explicit_pair<D, TPR, 1><<<h->tpr_blocks, kThreads, 0, st>>>(h->g, pair_step(h, k), h->rec_map, store);
+  else
+    k_explicit_pair<D, TPR, 0><<<h->tpr_blocks, kThreads, 0, st>>>(h->g, pair_step(h, k), h->rec_map, store);
 }
 template <int D>
 void launch_pair(const sc_nb_newmark* h, cudaStream_t st, int k, SegStore store) {
