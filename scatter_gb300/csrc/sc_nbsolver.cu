@@ -601,7 +601,6 @@ __device__ __forceinline__ void spmv_chunk(const Args& g, int64_t pos, const int
 
 // the SpMV's rows: pair planes one chunk at a time (kA32 = false), or the hi planes alone two
 // chunks at a time (half the bytes per chunk, so twice the loads in flight); then p.w and alpha
-constexpr bool kA32TwoChunks = true;
 template <int D, int kMode, bool kA32, int kKeep>
 __device__ __forceinline__ void spmv_rows(const Args& g, cudaGraphConditionalHandle hc) {
   __shared__ double sh[32];
@@ -612,7 +611,7 @@ __device__ __forceinline__ void spmv_rows(const Args& g, cudaGraphConditionalHan
     float hi[D], lo[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) hi[c] = lo[c] = 0.f;
-    if (kA32 && kA32TwoChunks) {
+    if (kA32) {
       int64_t q = 0;
       for (; q + 1 < nq; q += 2) {
         const int64_t pos = p0 + 128 * q;
@@ -631,7 +630,7 @@ __device__ __forceinline__ void spmv_rows(const Args& g, cudaGraphConditionalHan
       for (int64_t q = 0; q < nq; ++q) {
         int c0[4];
         cols4(g.sf_col, p0 + 128 * q, c0, keep);
-        spmv_chunk<D, kKeep>(g, p0 + 128 * q, c0, kA32, hi, lo);
+        spmv_chunk<D, kKeep>(g, p0 + 128 * q, c0, false, hi, lo);
       }
     }
     if (row < g.n_nodes) {
