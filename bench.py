@@ -339,6 +339,7 @@ def explicit_run(g, table, rec_eq, k, w, n):
     s = NodeBlockNewmark(g, DT, precond="jacobi")
     s.set_force(table)
     s.set_output(1, rec_eq, len(table.f_ptr) - 1, what=("v",))
+    tpr = s.tune_explicit()[0]  # the step kernel's threads per row, register budget and load policy
     s.run_explicit(0, w)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -356,8 +357,10 @@ def explicit_run(g, table, rec_eq, k, w, n):
     return {"value": n * k / (ms / 1e3), "unit": "DOF-steps/s", "ms_per_step": ms / k, "steps": k,
             "dt": DT, "dt_critical_bound": dtc, "kernel_ms": ms_k,
             "kernel_gbs": bytes_step / (ms_k * 1e-3) / 1e9,
+            "threads_per_row": tpr,
             "note": "central difference, row-sum lumped mass (no reference counterpart); u, v, K w in FP32 (hi, lo) "
-                    "pairs, FP64 at the run boundary"}
+                    "pairs, FP64 at the run boundary; step kernel shape tuned (threads per row, register budget, "
+                    "load policy)"}
 
 
 def _top_receivers(model, n, seed):

@@ -386,7 +386,7 @@ int sc_batch_create(sc_batch** h, const sc_batch_desc* desc, double* u, double* 
  * copies of the state (no reference counterpart); this reports the choice, its per-step time
  * and which kernel it is: 0 the incidence-list kernel, 1 the uniform hexa8 grid kernel (tiled),
  * 2 the tensor-core kernel (realisations_per_thread then reports its column segment length),
- * 3 the node-centric uniform hexa8 kernel. */
+ * 3 the node-centric uniform hexa8 kernel, 4 the same at the wide register budget. */
 int sc_batch_config(sc_batch* h, int* realisations_per_thread, int* threads_per_block, float* ms_per_step,
                     int* grid_kernel);
 /* Uniform hexa8 grids (no reference counterpart; the meshes scatter/mesher.py reads from
@@ -426,6 +426,9 @@ int sc_batch_status(sc_batch* h);
 int sc_batch_set_shape(sc_batch* h, int realisations_per_thread, int threads_per_block);
 int sc_batch_set_grid_shape(sc_batch* h, int realisations_per_thread, int threads_per_block);
 int sc_batch_set_node_shape(sc_batch* h, int realisations_per_thread, int threads_per_block);
+/* wide = 1: the node-centric kernel at the wide register budget (one block per SM minimum; 2 or
+ * 4 realisations per thread); sc_batch_config reports it as kernel 4 */
+int sc_batch_set_node_shape_budget(sc_batch* h, int realisations_per_thread, int threads_per_block, int wide);
 int sc_batch_set_tc_shape(sc_batch* h, int seg);
 int sc_batch_set_force(sc_batch* h, int n_t, const int64_t* f_ptr, const int* f_slot, const double* f_val);
 /* receivers record v [n_out][n_rec][R] every out_interval steps */

@@ -56,6 +56,7 @@ SIGNATURES = {
     "sc_batch_set_shape": (I, [P, I, I]),
     "sc_batch_set_grid_shape": (I, [P, I, I]),
     "sc_batch_set_node_shape": (I, [P, I, I]),
+    "sc_batch_set_node_shape_budget": (I, [P, I, I, I]),
     "sc_batch_set_hex8_columns": (I, [P, I, I, P, P]),
     "sc_batch_set_tc_shape": (I, [P, I]),
     "sc_batch_status": (I, [P]),

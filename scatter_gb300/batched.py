@@ -288,7 +288,8 @@ class BatchedExplicit:
         self.l_s = dv.to_dev(sv.astype(np.float32), torch.float32)
 
     KERNELS = {0: "incidence lists (k_batch_step)", 1: "uniform hexa8 grid, tiled (k_batch_step_hex8g)",
-               2: "tensor cores (k_batch_step_tc)", 3: "uniform hexa8 grid, node-centric (k_batch_step_hex8c)"}
+               2: "tensor cores (k_batch_step_tc)", 3: "uniform hexa8 grid, node-centric (k_batch_step_hex8c)",
+               4: "uniform hexa8 grid, node-centric, wide register budget (k_batch_step_hex8c_wide)"}
 
     def config(self):
         """(realisations per thread, threads per block, tuned ms per step, kernel) of the step
@@ -301,7 +302,11 @@ class BatchedExplicit:
 
     def set_shape(self, realisations_per_thread, threads_per_block, grid=False):
         """Override the tuned kernel and shape (testing aid): grid False the incidence-list
-        kernel, True the tiled uniform hexa8 kernel, "node" the node-centric one."""
+        kernel, True the tiled uniform hexa8 kernel, "node" the node-centric one, "node-wide" the
+        node-centric one at the wide register budget."""
+        if grid == "node-wide":
+            nat.call("sc_batch_set_node_shape_budget", self.h, int(realisations_per_thread), int(threads_per_block), 1)
+            return
         fn = {False: "sc_batch_set_shape", True: "sc_batch_set_grid_shape", "node": "sc_batch_set_node_shape"}[grid]
         nat.call(fn, self.h, int(realisations_per_thread), int(threads_per_block))
 

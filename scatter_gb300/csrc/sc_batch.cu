@@ -436,10 +436,9 @@ __device__ __forceinline__ void lds_f(const float* p, float (&v)[RPT]) {
 // loads each K1 entry it uses (576 per node and thread).  The elements are taken in la order and
 // the products in the same order as there, so the results are bitwise the same.
 template <int RPT>
-__global__ void __launch_bounds__(256) k_batch_step_hex8c(Args g, const __grid_constant__ K1Hex8 k1,
-                                                         const int* __restrict__ elem8, const float* __restrict__ w_in,
-                                                         float* __restrict__ w_out, const float* __restrict__ vf_in,
-                                                         float* __restrict__ vf_out, int tpn) {
+__device__ __forceinline__ void hex8c_step(const Args& g, const K1Hex8& k1, const int* __restrict__ elem8,
+                                           const float* __restrict__ w_in, float* __restrict__ w_out,
+                                           const float* __restrict__ vf_in, float* __restrict__ vf_out, int tpn) {
   const int npb = blockDim.x / tpn;
   const int sub = threadIdx.x / tpn;
   const int r0 = (threadIdx.x % tpn) * RPT;
@@ -484,6 +483,26 @@ __global__ void __launch_bounds__(256) k_batch_step_hex8c(Args g, const __grid_c
     node_update<RPT>(g, a, r0, acc, w_in, w_out, vf_in, vf_out, step, rec_now);
   }
   step_epilogue(g, step);
+}
+
+// the node-centric step at the compiler's default register budget (64 at 256 threads) and at a
+// wide one (one block per SM minimum: 79 registers at 2 realisations per thread, 144 at 4);
+// both are tuner candidates
+template <int RPT>
+__global__ void __launch_bounds__(256) k_batch_step_hex8c(Args g, const __grid_constant__ K1Hex8 k1,
+                                                         const int* __restrict__ elem8, const float* __restrict__ w_in,
+                                                         float* __restrict__ w_out, const float* __restrict__ vf_in,
+                                                         float* __restrict__ vf_out, int tpn) {
+  hex8c_step<RPT>(g, k1, elem8, w_in, w_out, vf_in, vf_out, tpn);
+}
+template <int RPT>
+__global__ void __launch_bounds__(256, 1) k_batch_step_hex8c_wide(Args g, const __grid_constant__ K1Hex8 k1,
+                                                                 const int* __restrict__ elem8,
+                                                                 const float* __restrict__ w_in,
+                                                                 float* __restrict__ w_out,
+                                                                 const float* __restrict__ vf_in,
+                                                                 float* __restrict__ vf_out, int tpn) {
+  hex8c_step<RPT>(g, k1, elem8, w_in, w_out, vf_in, vf_out, tpn);
 }
 
 // One step for all realisations on a uniform hexa8 grid: grid (tiles, realisation chunks of
@@ -1079,6 +1098,11 @@ static void batch_launch(const sc_batch* h, const Args& g, int grid, int rpt, in
   const int npb = threads / tpn;
   const int64_t want = ((int64_t)g.d.n_nodes + npb - 1) / npb;
   const unsigned blocks = (unsigned)(want < 152 * 32 ? want : 152 * 32);
+  if (grid == 4) {  // the wide register budget
+    if (rpt == 4) k_batch_step_hex8c_wide<4><<<blocks, threads, 0, st>>>(g, h->k1, h->elem8, wi, wo, vi, vo, tpn);
+    else k_batch_step_hex8c_wide<2><<<blocks, threads, 0, st>>>(g, h->k1, h->elem8, wi, wo, vi, vo, tpn);
+    return;
+  }
   if (grid == 3) {
     switch (rpt) {
       case 8: k_batch_step_hex8c<8><<<blocks, threads, 0, st>>>(g, h->k1, h->elem8, wi, wo, vi, vo, tpn); break;
@@ -1164,7 +1188,10 @@ static int batch_tune(sc_batch* h) {
         if (R % rpt != 0 || (rpt >= 4 && R % 4 != 0)) continue;
         const int tpn = R / rpt;
         for (int threads : {128, 256})
-          if (tpn <= threads) cands.push_back({3, rpt, (threads / tpn) * tpn, tpn});
+          if (tpn <= threads) {
+            cands.push_back({3, rpt, (threads / tpn) * tpn, tpn});
+            if (rpt <= 4) cands.push_back({4, rpt, (threads / tpn) * tpn, tpn});
+          }
       }
     }
     if (h->tt.nodes) {  // tensor-core kernel: segments of the whole column, a half, a third, a quarter
@@ -1343,13 +1370,20 @@ extern "C" int sc_batch_set_grid_shape(sc_batch* h, int realisations_per_thread,
 // Selects the node-centric uniform hexa8 kernel with 2, 4 or 8 realisations per thread and 128
 // or 256 threads per block (testing aid; needs sc_batch_set_hex8_grid).
 extern "C" int sc_batch_set_node_shape(sc_batch* h, int realisations_per_thread, int threads_per_block) {
-  if (!h || !h->halo) return SC_BAD_ARG;
+  return sc_batch_set_node_shape_budget(h, realisations_per_thread, threads_per_block, 0);
+}
+
+// the same with wide = 1: the kernel at the wide register budget (2 or 4 realisations per thread)
+extern "C" int sc_batch_set_node_shape_budget(sc_batch* h, int realisations_per_thread, int threads_per_block,
+                                              int wide) {
+  if (!h || !h->halo || (wide != 0 && wide != 1)) return SC_BAD_ARG;
+  if (wide && realisations_per_thread == 8) return SC_BAD_ARG;
   const int rpt = realisations_per_thread, R = h->g.d.R;
   if ((rpt != 2 && rpt != 4 && rpt != 8) || R % rpt != 0 || (rpt >= 4 && R % 4 != 0)) return SC_BAD_ARG;
   if (threads_per_block != 128 && threads_per_block != 256) return SC_BAD_ARG;
   const int tpn = R / rpt;
   if (tpn > threads_per_block) return SC_BAD_ARG;
-  h->grid = 3;
+  h->grid = wide ? 4 : 3;
   h->rpt = rpt;
   h->threads = (threads_per_block / tpn) * tpn;
   h->tpn = tpn;

@@ -79,9 +79,10 @@ __device__ __forceinline__ float pick(const float (&a)[D], int c) {
   return D == 2 ? (c == 0 ? a[0] : a[1]) : (c == 0 ? a[0] : (c == 1 ? a[1] : a[2]));
 }
 
-template <int D, int TPR, int kKeep>  // kKeep = g.keep_l2 at compile time
-__global__ void __launch_bounds__(kThreads) k_explicit_pair(Args g, PairStep p, const int* __restrict__ rec_map,
-                                                            SegStore st) {
+template <int D, int TPR, int kKeep>  // kKeep: the planes' load policy at compile time, or -1 (g.keep_l2)
+__device__ __forceinline__ void explicit_pair_step(const Args& g, const PairStep& p, const int* __restrict__ rec_map,
+                                                   const SegStore& st) {
+  const int keep = kKeep >= 0 ? kKeep : g.keep_l2;
   const int step = g.s->t + 1;
   const int64_t kn = st.wp ? (int64_t)(step - 1 - *st.t0) * g.n_s : 0;
   const bool rec_now = g.n_rec > 0 && g.out_interval > 0 && (step % g.out_interval) == 0 &&
@@ -104,7 +105,7 @@ __global__ void __launch_bounds__(kThreads) k_explicit_pair(Args g, PairStep p, 
     for (int64_t q = sub; q < nq; q += TPR) {
       const int64_t pos = p0 + 128 * q;
       int cl[4];
-      cols4(g.sf_col, pos, cl, kKeep);
+      cols4(g.sf_col, pos, cl, keep);
       float2 wa[4][D];
 #pragma unroll
       for (int e = 0; e < 4; ++e)
@@ -115,7 +116,7 @@ __global__ void __launch_bounds__(kThreads) k_explicit_pair(Args g, PairStep p, 
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           float2 k4[4];
-          ld4(g.KPS + (int64_t)(c * D + d) * g.sf_n + pos, k4, kKeep);
+          ld4(g.KPS + (int64_t)(c * D + d) * g.sf_n + pos, k4, keep);
 #pragma unroll
           for (int e = 0; e < 4; ++e) pair_fma(k4[e].x, k4[e].y, wa[e][d], hi[c], lo[c]);
         }
@@ -176,6 +177,24 @@ __global__ void __launch_bounds__(kThreads) k_explicit_pair(Args g, PairStep p, 
       g.s->t = step;
     }
   }
+}
+
+// The explicit step at the compiler's default register budget (64 per thread at 256 threads) and
+// at a wide one (minimum one block per SM: up to 174 registers, no spills), each with the
+// planes' load policy read at run time or fixed at compile time; the tuner times them all with
+// each threads-per-row count, as the fastest depends on the mesh size (one thread per row, wide
+// budget, policy at compile time: 0.033 against 0.043 ms for the default form at 209 k DOF, but
+// slower at 1.79 M DOF; at 107 k DOF with two threads per row the compile-time policy made the
+// step 26 us against 21).
+template <int D, int TPR, int kKeep>
+__global__ void __launch_bounds__(kThreads) k_explicit_pair(Args g, PairStep p, const int* __restrict__ rec_map,
+                                                            SegStore st) {
+  explicit_pair_step<D, TPR, kKeep>(g, p, rec_map, st);
+}
+template <int D, int TPR, int kKeep>
+__global__ void __launch_bounds__(kThreads, 1) k_explicit_pair_wide(Args g, PairStep p,
+                                                                    const int* __restrict__ rec_map, SegStore st) {
+  explicit_pair_step<D, TPR, kKeep>(g, p, rec_map, st);
 }
 
 // FP64 step: the same scheme with FP64 products and update (reference precision)
@@ -349,12 +368,19 @@ PairStep pair_step(const sc_nb_newmark* h, int k) {
   return p;
 }
 
+template <int D, int TPR, int kKeep>
+void launch_pair_k(const sc_nb_newmark* h, cudaStream_t st, int k, SegStore store) {
+  if (h->ex_wide)
+    k_explicit_pair_wide<D, TPR, kKeep><<<h->tpr_blocks, kThreads, 0, st>>>(h->g, pair_step(h, k), h->rec_map,
+                                                                           store);
+  else
+    k_explicit_pair<D, TPR, kKeep><<<h->tpr_blocks, kThreads, 0, st>>>(h->g, pair_step(h, k), h->rec_map, store);
+}
 template <int D, int TPR>
 void launch_pair_t(const sc_nb_newmark* h, cudaStream_t st, int k, SegStore store) {
-  if (h->g.keep_l2)
-    k_explicit_pair<D, TPR, 1><<<h->tpr_blocks, kThreads, 0, st>>>(h->g, pair_step(h, k), h->rec_map, store);
-  else
-    k_explicit_pair<D, TPR, 0><<<h->tpr_blocks, kThreads, 0, st>>>(h->g, pair_step(h, k), h->rec_map, store);
+  if (!h->ex_keep_ct) launch_pair_k<D, TPR, -1>(h, st, k, store);
+  else if (h->g.keep_l2) launch_pair_k<D, TPR, 1>(h, st, k, store);
+  else launch_pair_k<D, TPR, 0>(h, st, k, store);
 }
 template <int D>
 void launch_pair(const sc_nb_newmark* h, cudaStream_t st, int k, SegStore store) {
@@ -557,6 +583,8 @@ extern "C" int sc_nb_tune_explicit(sc_nb_newmark* h, int reps, int* tpr_chosen, 
   const unsigned blocks0 = h->tpr_blocks;
   float best = -1.f;
   int best_tpr = tpr0;
+  const int wide0 = h->ex_wide, keep_ct0 = h->ex_keep_ct;
+  int best_wide = wide0, best_keep_ct = keep_ct0;
   do {
     if ((rc = check(cudaMallocAsync((void**)&f_save, 8 * ns, st), "tune malloc"))) break;
     cudaMemcpyAsync(f_save, h->f2, 8 * ns, cudaMemcpyDeviceToDevice, st);
@@ -564,11 +592,17 @@ extern "C" int sc_nb_tune_explicit(sc_nb_newmark* h, int reps, int* tpr_chosen, 
     g.n_rec = 0;  // no receiver records while timing
     // every candidate warmed up first, then timed in three rounds taken in turn (a candidate's
     // best round counts): a single pass ranked them by the order the clocks ramped in
-    const int cands[3] = {1, 2, 4};
-    float cms[3] = {-1.f, -1.f, -1.f};
+    // candidate ci: threads per row {1, 2, 4}[ci % 3], wide register budget (ci / 3) & 1, load
+    // policy at compile time ci / 6
+    constexpr int kCands = 12;
+    const int tprs[3] = {1, 2, 4};
+    float cms[kCands];
+    for (int ci = 0; ci < kCands; ++ci) cms[ci] = -1.f;
     for (int round = -1; round < 3 && !rc; ++round)
-      for (int ci = 0; ci < 3 && !rc; ++ci) {
-        h->tpr = cands[ci];
+      for (int ci = 0; ci < kCands && !rc; ++ci) {
+        h->tpr = tprs[ci % 3];
+        h->ex_wide = (ci / 3) & 1;
+        h->ex_keep_ct = ci / 6;
         const int64_t want = (((int64_t)g.n_nodes + 31) / 32 * 32 * h->tpr + kThreads - 1) / kThreads;
         h->tpr_blocks = (unsigned)(want < 152 * 16 ? (want < 1 ? 1 : want) : 152 * 16);
         if (round < 0) {
@@ -585,10 +619,12 @@ extern "C" int sc_nb_tune_explicit(sc_nb_newmark* h, int reps, int* tpr_chosen, 
         ms /= reps;
         if (cms[ci] < 0.f || ms < cms[ci]) cms[ci] = ms;
       }
-    for (int ci = 0; ci < 3 && !rc; ++ci)
+    for (int ci = 0; ci < kCands && !rc; ++ci)
       if (best < 0.f || cms[ci] < best) {
         best = cms[ci];
-        best_tpr = cands[ci];
+        best_tpr = tprs[ci % 3];
+        best_wide = (ci / 3) & 1;
+        best_keep_ct = ci / 6;
       }
     cudaMemcpyAsync(h->f2, f_save, 8 * ns, cudaMemcpyDeviceToDevice, st);
   } while (0);
@@ -599,10 +635,14 @@ extern "C" int sc_nb_tune_explicit(sc_nb_newmark* h, int reps, int* tpr_chosen, 
   if (f_save) cudaFree(f_save);
   if (rc || best < 0.f) {
     h->tpr = tpr0;
+    h->ex_wide = wide0;
+    h->ex_keep_ct = keep_ct0;
     h->tpr_blocks = blocks0;
     return rc ? rc : SC_BAD_ARG;
   }
   h->tpr = best_tpr;
+  h->ex_wide = best_wide;
+  h->ex_keep_ct = best_keep_ct;
   const int64_t want = (((int64_t)g.n_nodes + 31) / 32 * 32 * h->tpr + kThreads - 1) / kThreads;
   h->tpr_blocks = (unsigned)(want < 152 * 16 ? (want < 1 ? 1 : want) : 152 * 16);
   drop_explicit_graphs(h);

@@ -295,6 +295,8 @@ struct sc_nb_newmark {
   // the SMs have enough warps to cover load latency) and their grid
   int tpr = 1;
   unsigned tpr_blocks = 1;
+  int ex_wide = 0;     // explicit step kernel at the wide register budget (sc_nb_tune_explicit)
+  int ex_keep_ct = 0;  // explicit step kernel with the planes' load policy at compile time (the same)
   double *ML = nullptr, *IML = nullptr;  // lumped mass (row sums unless set by the caller)
   int ml_user = 0;                       // 1: ML set by sc_nb_set_lumped_mass
   double *v1 = nullptr, *w0 = nullptr, *w1 = nullptr;  // FP64 mode ping-pong buffers

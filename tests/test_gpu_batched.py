@@ -130,7 +130,8 @@ def test_batched_shapes_agree_bitwise(cuda):
     rec = [int(m.eq_nb_dof[m.node_index()[n], 1]) for n in top[::5]]
     results = []
     shapes = ((1, 128, False), (1, 256, False), (2, 128, False), (4, 256, False), (8, 128, False), (1, 128, True),
-              (1, 256, True), (2, 128, True), (2, 256, True), (2, 128, "node"), (4, 256, "node"), (8, 128, "node"))
+              (1, 256, True), (2, 128, True), (2, 256, True), (2, 128, "node"), (4, 256, "node"), (8, 128, "node"),
+              (2, 256, "node-wide"), (4, 128, "node-wide"))
     for rpt, tpb, grid in shapes:
         b = BatchedExplicit(m, young, 0.3, 1900.0, [1, 0.02, 50, 0.02], [1, 1], 1e3, dt)
         assert b.grid_tables is not None
