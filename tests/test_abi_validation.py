@@ -93,6 +93,13 @@ def test_node_block_option_and_residual_checks(lib):
     assert lib.sc_nb_time_spmv_a32(None, 1, 5, ctypes.byref(ms), None) == SC_BAD_ARG
     order = ctypes.c_int()
     assert lib.sc_nb_warm_start_status(None, ctypes.byref(order), ctypes.byref(n)) == SC_BAD_ARG
+    assert lib.sc_nb_status_to(None, FAKE) == SC_BAD_ARG
+    assert lib.sc_newmark_status_to(None, FAKE) == SC_BAD_ARG
+
+
+def test_batched_shape_checks(lib):
+    assert lib.sc_batch_set_node_shape(None, 4, 256) == SC_BAD_ARG
+    assert lib.sc_batch_set_node_shape_budget(None, 4, 256, 1) == SC_BAD_ARG
 
 
 def test_csr_option_checks(lib):
