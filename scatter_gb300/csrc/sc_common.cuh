@@ -61,6 +61,31 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return s;
 }
 
+// Block-wide sums of two doubles per thread in one pass (each summed in the same order as
+// block_sum would, so the results are the same bits).  Results valid in thread 0.  `sh` has at
+// least 64 doubles.
+__device__ __forceinline__ void block_sum2(double& a, double& b, double* sh) {
+  a = warp_sum(a);
+  b = warp_sum(b);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) {
+    sh[wid] = a;
+    sh[32 + wid] = b;
+  }
+  __syncthreads();
+  double sa = 0.0, sb = 0.0;
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    sa = lane < nw ? sh[lane] : 0.0;
+    sb = lane < nw ? sh[32 + lane] : 0.0;
+    sa = warp_sum(sa);
+    sb = warp_sum(sb);
+  }
+  a = sa;
+  b = sb;
+}
+
 // ------------------------------------------------ warm start of the per-step PCG (Newmark)
 // Both Newmark solvers start each step's PCG from the polynomial of degree p through the last
 // p+1 accelerations, evaluated one step ahead: x0 = sum_{k=0..p} (-1)^k C(p+1, k+1) a_{n-k}

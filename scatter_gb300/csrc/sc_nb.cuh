@@ -166,6 +166,17 @@ __device__ inline double reduce_parts(const double* part, int k, double* sh) {
   return block_sum(s, sh);
 }
 
+// reduce_parts of slots k0 and k1 in one pass (the same bits as two calls); sh: 64 doubles
+__device__ inline void reduce_parts2(const double* part, int k0, int k1, double* sh, double& s0, double& s1) {
+  s0 = 0.0;
+  s1 = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+    s0 += __ldcg(part + b * 4 + k0);
+    s1 += __ldcg(part + b * 4 + k1);
+  }
+  block_sum2(s0, s1, sh);
+}
+
 template <int D>
 __device__ inline void warp_sum3(double* s) {
 #pragma unroll

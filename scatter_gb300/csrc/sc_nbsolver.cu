@@ -711,7 +711,7 @@ static void launch_prec_upper(const Args& g, unsigned blocks, cudaStream_t st, i
 // r then become the x0 and r0 that the bound and a restart refer to.
 template <int kMode>
 __global__ void k_update(Args g, cudaGraphConditionalHandle hc) {
-  __shared__ double sh[32];
+  __shared__ double sh[64];
   const double alpha = g.s->alpha;
   double prr = 0.0, pdd = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
@@ -724,13 +724,14 @@ __global__ void k_update(Args g, cudaGraphConditionalHandle hc) {
     g.r32[i] = (float)r;
     prr += r * r;
   }
-  double t = block_sum(prr, sh);
-  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 1] = t;
-  t = block_sum(pdd, sh);
-  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 2] = t;
+  block_sum2(prr, pdd, sh);
+  if (threadIdx.x == 0) {
+    g.part[blockIdx.x * 4 + 1] = prr;
+    g.part[blockIdx.x * 4 + 2] = pdd;
+  }
   if (last_block(&g.s->ticket)) {
-    const double rr = reduce_parts(g.part, 1, sh);
-    const double dd = reduce_parts(g.part, 2, sh);
+    double rr, dd;
+    reduce_parts2(g.part, 1, 2, sh, rr, dd);
     if (threadIdx.x == 0) {
       Scal* s = g.s;
       s->ticket = 0;
