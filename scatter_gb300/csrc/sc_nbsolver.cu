@@ -257,7 +257,7 @@ constexpr double kResRatio = 30.0;
 template <int D, int kKeep>  // kKeep = g.keep_l2 at compile time
 __global__ void __launch_bounds__(kThreads) k_residual_kp(Args g) {
   if (g.s->res_fp64) return;
-  __shared__ double sh[32];
+  __shared__ double sh[64];
   double pbb = 0.0, pkq = 0.0;
   SELL_ROW_LOOP(g.sf_ptr) {
     SELL_ROW_BEGIN(g.sf_ptr)
@@ -328,13 +328,14 @@ __global__ void __launch_bounds__(kThreads) k_residual_kp(Args g) {
       }
     }
   }
-  double t = block_sum(pbb, sh);
-  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 2] = t;
-  t = block_sum(pkq, sh);
-  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 3] = t;
+  block_sum2(pbb, pkq, sh);
+  if (threadIdx.x == 0) {
+    g.part[blockIdx.x * 4 + 2] = pbb;
+    g.part[blockIdx.x * 4 + 3] = pkq;
+  }
   if (last_block(&g.s->ticket)) {
-    const double bb = reduce_parts(g.part, 2, sh);
-    const double kq = reduce_parts(g.part, 3, sh);
+    double bb, kq;
+    reduce_parts2(g.part, 2, 3, sh, bb, kq);
     if (threadIdx.x == 0) {
       g.s->bb = bb;
       if (kq > kResRatio * kResRatio * bb) g.s->res_fp64_next = 1;  // k_advance makes it current
@@ -410,7 +411,7 @@ constexpr double kA32Margin = 16.0;
 // mode 1 (after the residual): p = z, rz, rr and the conditional from |r| vs |b|.
 template <int D, int kMode, int kKeep>  // kKeep = g.keep_l2 at compile time
 __global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cudaGraphConditionalHandle hc) {
-  __shared__ double sh[32];
+  __shared__ double sh[64];
   double prz = 0.0, prr = 0.0;
   // a restart (inside the PCG): x, r back to x0, r0 and a fresh direction (beta = 0); a switch
   // to Ah: x, r become x0, r0 (the CG goes on)
@@ -446,15 +447,20 @@ __global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cu
       }
     }
   }
-  double t = block_sum(prz, sh);
-  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 0] = t;
   if (mode == 1) {
-    t = block_sum(prr, sh);
-    if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 1] = t;
+    block_sum2(prz, prr, sh);
+    if (threadIdx.x == 0) {
+      g.part[blockIdx.x * 4 + 0] = prz;
+      g.part[blockIdx.x * 4 + 1] = prr;
+    }
+  } else {
+    const double t = block_sum(prz, sh);
+    if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 0] = t;
   }
   if (last_block(&g.s->ticket)) {
-    const double rz = reduce_parts(g.part, 0, sh);
-    const double rr = mode == 1 ? reduce_parts(g.part, 1, sh) : 0.0;
+    double rz, rr = 0.0;
+    if (mode == 1) reduce_parts2(g.part, 0, 1, sh, rz, rr);
+    else rz = reduce_parts(g.part, 0, sh);
     if (threadIdx.x == 0) {
       Scal* s = g.s;
       s->ticket = 0;
