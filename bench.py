@@ -724,8 +724,9 @@ def e2e_run(g, table, time_grid, rec_eq, w, k, n):
     is set-up cost outside this metric).  The untimed first call (steps 0 .. w)
     builds the solver and runs the same warm-up as the device-timed leg; the timed region is
     then k calls of one step each, w .. w + k, each copying that step's force values host ->
-    device from pinned memory and its receiver outputs (u, v, a) device -> host into the
-    solver's host arrays before it returns."""
+    device from pinned memory and queueing the device -> host copies of its receiver outputs
+    (u, v, a) and of the run's status into pinned buffers; a call's outputs reach the solver's
+    host arrays at the next call (the last one's when the timed region ends)."""
     import torch
 
     from scatter_gb300.solvers import NewmarkExplicit
@@ -762,8 +763,8 @@ def e2e_run(g, table, time_grid, rec_eq, w, k, n):
             "d2h_bytes_per_step": 3 * len(rec_eq) * 8, "steps": k, "first_step": w, "ms_per_step": ms / k,
             "host_wall_s": wall, "cg_iters_per_step": (it_all - it_w) / k, "preconditioner": s.preconditioner,
             "api": "NewmarkExplicit.calculate(matrix, matrix, matrix, F, t, t + 1) once per step (GenerateMatrix "
-                   "for M, C, K; force values streamed from pinned host memory; receiver u, v, a copied back to the "
-                   "host each call)"}
+                   "for M, C, K; force values streamed from pinned host memory; each call queues the copies of its "
+                   "receiver u, v, a and of the run's status to pinned host buffers, delivered at the next call)"}
 
 
 def run_reference(args):
