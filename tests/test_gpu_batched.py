@@ -178,7 +178,8 @@ def test_batched_grid_kernel_on_a_notched_mesh(cuda):
     table = ricker_table(m, int(top[0]), -1e4, 40.0, 0.002, time)
     rec = [int(m.eq_nb_dof[m.node_index()[n], 1]) for n in top[::2]]
     results = []
-    for rpt, tpb, grid in ((4, 256, False), (1, 256, True), (2, 256, True), (4, 128, "node"), (8, 256, "node")):
+    for rpt, tpb, grid in ((4, 256, False), (1, 256, True), (2, 256, True), (4, 128, "node"), (8, 256, "node"),
+                           (2, 256, "node-wide")):
         b = BatchedExplicit(m, young, 0.3, 1900.0, [1, 0.02, 50, 0.02], [1, 1], 1e3, dt)
         assert b.grid_tables is not None
         b.set_shape(rpt, tpb, grid)
