@@ -303,7 +303,7 @@ def run_gb300(args):
                            "restarts": restarts, "lo_norm_bound": lo_norm},
            "ieee_fp64": fp64,
            "warm_start": {"order_at_end": order_end, "timed_steps_capped": capped_all - capped_w},
-           "gpu_launches": 9 * K_steps + 6 * iters,
+           "gpu_launches": 9 * K_steps + 5 * iters,
            "roofline": {"bound": "hbm",
                         "kernel": ("nb::k_spmv_a32 (PCG w = Ah p, the FP32 matrix, 3x3 node blocks, pair products)"
                                    if use_a32 else

@@ -388,10 +388,14 @@ __device__ __forceinline__ void fsai_row(const __half* planes, int64_t plane_n, 
   }
 }
 
-// t = G r  (lower pattern, FP16 factor planes, FP32 products and result)
-template <int D, int kKeep>  // kKeep = g.keep_l2 at compile time
+// t = G r  (lower pattern, FP16 factor planes, FP32 products and result).  With kDot (inside a
+// solve) also the PCG's r.z: the preconditioner is split, z = G^T G r, so r.z = (G r).(G r) =
+// |t|^2, and the last block forms beta and rz here.  The upper half then knows beta and writes
+// the new direction p = z + beta p itself (no separate direction pass, z never stored).
+template <int D, int kKeep, bool kDot>  // kKeep = g.keep_l2 at compile time
 __global__ void __launch_bounds__(kThreads, 4) k_prec_lower(Args g) {
   const float* rv = g.s->restart ? g.r032 : g.r32;  // a restart preconditions r0
+  double ptt = 0.0;
   SELL_ROW_LOOP(g.sl_ptr) {
     SELL_ROW_BEGIN(g.sl_ptr)
     float s[D];
@@ -400,23 +404,44 @@ __global__ void __launch_bounds__(kThreads, 4) k_prec_lower(Args g) {
     fsai_row<D>(g.GS, g.sl_n, g.sl_col, rv, p0, nq, kKeep, s);
     if (row < g.n_nodes) {
 #pragma unroll
-      for (int c = 0; c < D; ++c) g.t32[row * D + c] = s[c];
+      for (int c = 0; c < D; ++c) {
+        g.t32[row * D + c] = s[c];
+        if (kDot) ptt = fma((double)s[c], (double)s[c], ptt);
+      }
+    }
+  }
+  if (kDot) {
+    __shared__ double sh[32];
+    const double t = block_sum(ptt, sh);
+    if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 0] = t;
+    if (last_block(&g.s->ticket)) {
+      const double rz = reduce_parts(g.part, 0, sh);
+      if (threadIdx.x == 0) {
+        Scal* s = g.s;
+        s->ticket = 0;
+        // a restart starts a fresh direction; after the residual beta is not used (p = z)
+        s->beta = s->restart ? 0.0 : (s->rz != 0.0 ? rz / s->rz : 0.0);
+        s->rz = rz;
+      }
     }
   }
 }
 
 constexpr double kA32Margin = 16.0;
 
-// z = G^T t ; partial r.z ; mode 0 (inside PCG): last block computes beta, rz;
-// mode 1 (after the residual): p = z, rz, rr and the conditional from |r| vs |b|.
+// z = G^T t and the new direction from it.  mode 0 (inside the PCG): p = z + beta p, with beta
+// from the lower half; mode 1 (after the residual): p = z, rr, and the conditional from |r| vs
+// |b|.  rz comes from the lower half in both modes.
 template <int D, int kMode, int kKeep>  // kKeep = g.keep_l2 at compile time
 __global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cudaGraphConditionalHandle hc) {
-  __shared__ double sh[64];
-  double prz = 0.0, prr = 0.0;
+  __shared__ double sh[32];
+  double prr = 0.0;
   // a restart (inside the PCG): x, r back to x0, r0 and a fresh direction (beta = 0); a switch
-  // to Ah: x, r become x0, r0 (the CG goes on)
+  // to Ah: x, r become x0, r0 (the CG goes on).  k_update clears both flags before it decides
+  // the next iteration's.
   const bool rs = mode == 0 && g.s->restart;
   const bool sw = mode == 0 && g.s->sw;
+  const double beta = mode == 0 ? g.s->beta : 0.0;
   SELL_ROW_LOOP(g.su_ptr) {
     SELL_ROW_BEGIN(g.su_ptr)
     float s[D];
@@ -428,64 +453,49 @@ __global__ void __launch_bounds__(kThreads, 4) k_prec_upper(Args g, int mode, cu
       for (int c = 0; c < D; ++c) {
         const int64_t i = row * D + c;
         const double z = (double)s[c];
-        const double r = rs ? g.r0[i] : g.r[i];
-        if (rs) {
-          g.r[i] = r;
-          g.x[i] = g.x0[i];
-        } else if (sw) {
-          g.r0[i] = r;
-          g.r032[i] = g.r32[i];
-          g.x0[i] = g.x[i];
-        }
-        g.z[i] = z;
         if (mode == 1) {
+          const double r = g.r[i];
           g.p[i] = z;
           if (g.spmv_pair) g.p2[i] = make_float2(s[c], 0.f);  // z is an FP32 value: the pair is exact
+          prr += r * r;
+        } else {
+          if (rs) {
+            g.r[i] = g.r0[i];
+            g.x[i] = g.x0[i];
+          } else if (sw) {
+            g.r0[i] = g.r[i];
+            g.r032[i] = g.r32[i];
+            g.x0[i] = g.x[i];
+          }
+          const double pv = rs ? z : fma(beta, g.p[i], z);
+          g.p[i] = pv;
+          if (g.spmv_pair) g.p2[i] = split_pair(pv);
         }
-        prz += r * z;
-        prr += r * r;
       }
     }
   }
-  if (mode == 1) {
-    block_sum2(prz, prr, sh);
-    if (threadIdx.x == 0) {
-      g.part[blockIdx.x * 4 + 0] = prz;
-      g.part[blockIdx.x * 4 + 1] = prr;
-    }
-  } else {
-    const double t = block_sum(prz, sh);
-    if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 0] = t;
-  }
+  if (mode == 0) return;
+  const double t = block_sum(prr, sh);
+  if (threadIdx.x == 0) g.part[blockIdx.x * 4 + 1] = t;
   if (last_block(&g.s->ticket)) {
-    double rz, rr = 0.0;
-    if (mode == 1) reduce_parts2(g.part, 0, 1, sh, rz, rr);
-    else rz = reduce_parts(g.part, 0, sh);
+    const double rr = reduce_parts(g.part, 1, sh);
     if (threadIdx.x == 0) {
       Scal* s = g.s;
       s->ticket = 0;
-      if (mode == 1) {
-        s->rz = rz;
-        s->rr = rr;
-        s->rr0 = rr;
-        s->dd = s->dd_pre = 0.0;
-        s->restart = s->sw = s->no_switch = 0;
-        const bool done = rr <= s->tol2 * s->bb;
-        // the FP32 matrix when the last step's |x - x0| / |r0|, scaled to this r0, keeps the
-        // bound lo_norm |x - x0| below tol |b| / kA32Margin
-        int a = 0;
-        if (g.a32_mode == 2) a = 1;
-        else if (g.a32_mode == 1 && s->rho >= 0.0)
-          a = s->lo_norm * s->rho * sqrt(rr) * kA32Margin <= sqrt(s->tol2 * s->bb) ? 1 : 0;
-        s->a32 = a;
-        if (a && !done) s->a32_steps += 1;
-        pcg_continue<kMode>(hc, s, !done);
-      } else {
-        s->beta = rs ? 0.0 : (s->rz != 0.0 ? rz / s->rz : 0.0);
-        s->rz = rz;
-        if (rs) s->restart = 0;
-        if (sw) s->sw = 0;
-      }
+      s->rr = rr;
+      s->rr0 = rr;
+      s->dd = s->dd_pre = 0.0;
+      s->restart = s->sw = s->no_switch = 0;
+      const bool done = rr <= s->tol2 * s->bb;
+      // the FP32 matrix when the last step's |x - x0| / |r0|, scaled to this r0, keeps the
+      // bound lo_norm |x - x0| below tol |b| / kA32Margin
+      int a = 0;
+      if (g.a32_mode == 2) a = 1;
+      else if (g.a32_mode == 1 && s->rho >= 0.0)
+        a = s->lo_norm * s->rho * sqrt(rr) * kA32Margin <= sqrt(s->tol2 * s->bb) ? 1 : 0;
+      s->a32 = a;
+      if (a && !done) s->a32_steps += 1;
+      pcg_continue<kMode>(hc, s, !done);
     }
   }
 }
@@ -697,10 +707,10 @@ static void launch_spmv_pair(const Args& g, unsigned blocks, cudaStream_t st, cu
   if (g.keep_l2) k_spmv_pair<D, kMode, 1><<<blocks, kThreads, 0, st>>>(g, hc);
   else k_spmv_pair<D, kMode, 0><<<blocks, kThreads, 0, st>>>(g, hc);
 }
-template <int D>
+template <int D, bool kDot = true>
 static void launch_prec_lower(const Args& g, unsigned blocks, cudaStream_t st) {
-  if (g.keep_l2) k_prec_lower<D, 1><<<blocks, kThreads, 0, st>>>(g);
-  else k_prec_lower<D, 0><<<blocks, kThreads, 0, st>>>(g);
+  if (g.keep_l2) k_prec_lower<D, 1, kDot><<<blocks, kThreads, 0, st>>>(g);
+  else k_prec_lower<D, 0, kDot><<<blocks, kThreads, 0, st>>>(g);
 }
 template <int D, int kMode>
 static void launch_prec_upper(const Args& g, unsigned blocks, cudaStream_t st, int mode,
@@ -744,6 +754,7 @@ __global__ void k_update(Args g, cudaGraphConditionalHandle hc) {
       s->rr = rr;
       s->dd = dd;
       s->it += 1;
+      s->restart = s->sw = 0;  // the last iteration's, carried out by its preconditioner halves
       bool done;
       if (s->a32) {
         const double tb = sqrt(s->tol2 * s->bb), e = s->lo_norm * sqrt(dd);
@@ -774,15 +785,6 @@ __global__ void k_update(Args g, cudaGraphConditionalHandle hc) {
       if (s->status == SC_BREAKDOWN) done = true;
       if (done) pcg_continue<kMode>(hc, s, false);
     }
-  }
-}
-
-__global__ void k_direction(Args g) {
-  const double beta = g.s->beta;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n_s; i += (int64_t)gridDim.x * blockDim.x) {
-    const double pv = fma(beta, g.p[i], g.z[i]);
-    g.p[i] = pv;
-    if (g.spmv_pair) g.p2[i] = split_pair(pv);
   }
 }
 
@@ -1201,7 +1203,6 @@ int build_graph(sc_nb_newmark* h) {
     k_update<0><<<vbk, 256, 0, c2>>>(g, hc);
     launch_prec_lower<D>(g, nbk, c2);
     launch_prec_upper<D, 0>(g, nbk, c2, 0, hc);
-    k_direction<<<vbk, 256, 0, c2>>>(g);
     cudaGraph_t bo;
     if ((rc = check(cudaStreamEndCapture(c2, &bo), "end body"))) break;
     k_finalize<<<vbk, 256, 0, cs>>>(g);
@@ -1637,7 +1638,6 @@ static int eager_step(sc_nb_newmark* h) {
     k_update<1><<<vbk, 256, 0, st>>>(g, none);
     launch_prec_lower<D>(g, nbk, st);
     launch_prec_upper<D, 1>(g, nbk, st, 0, none);
-    k_direction<<<vbk, 256, 0, st>>>(g);
   }
   k_finalize<<<vbk, 256, 0, st>>>(g);
   k_record<<<vbk, 256, 0, st>>>(g);
@@ -1873,10 +1873,10 @@ extern "C" int sc_nb_apply(sc_nb_newmark* h, int which, const double* x, double*
       // r <- x, t = G r, z = G^T t (the solver's own kernels), y <- z
       k_copy_r<<<grid_for(g.n_s, 256), 256, 0, st>>>(g.n_s, g.D, x, g.r, g.r32);
       if (g.D == 3) {
-        launch_prec_lower<3>(g, h->node_blocks, st);
+        launch_prec_lower<3, false>(g, h->node_blocks, st);
         k_prec_upper_nograph<3><<<h->node_blocks, kThreads, 0, st>>>(g);
       } else {
-        launch_prec_lower<2>(g, h->node_blocks, st);
+        launch_prec_lower<2, false>(g, h->node_blocks, st);
         k_prec_upper_nograph<2><<<h->node_blocks, kThreads, 0, st>>>(g);
       }
       k_copy<<<grid_for(g.n_s, 256), 256, 0, st>>>(g.n_s, g.z, y);
